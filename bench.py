@@ -1,0 +1,338 @@
+"""Throughput of the D3Q19 wind-tunnel step on GB300 (MLUPS, % of HBM roofline).
+
+Default workload: the 320x160x128 mesh-body tunnel (6.55 M cells): no-slip
+floor (PAREDE), free-slip sides/top, equilibrium inlet, outlet + sponge, a
+seeded superellipsoid body; u_in = 0.06, Re 2000 on the 96-cell length
+(nu = 0.00288, omega+ = 1.98295), Smagorinsky Cs = 0.12, fp32 populations in
+the in-place layout.  One "step" = one D3Q19 step over every cell (MLUPS
+counts all nx*ny*nz cells, as the reference's tests/desempenho.html:67-70).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference's step on the host cores instead: the
+reference has no runnable CPU step of its own (its step exists only as
+generated WGSL/GLSL), so that arm runs the CPU restatement in oracle/ with all
+host threads on a bounded sample of the same workload.
+
+Multi-GPU: the tunnel does not shard here (replicas only): every rank runs its
+own copy and `value` sums the ranks' cells (weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+GRID = {"nx": 320, "ny": 160, "nz": 128}
+U_IN, RE, LEN, CS = 0.06, 2000.0, 96.0, 0.12
+BYTES_PER_CELL = {"f32": 152, "f16s": 76, "bf16s": 76, "f64": 304}
+
+
+def workload(body="mesh"):
+    """Cell types and parameters of the 320x160x128 mesh-body tunnel."""
+    from cfd__gb300.tunel import montarTipos
+
+    nu = U_IN * LEN / RE
+    omega = 1.0 / (3.0 * nu + 0.5)
+    if body == "mesh":
+        from cfd__gb300.geometry import corpo_config2
+        from cfd__gb300.voxel import voxelizar
+        pos, idx = corpo_config2(GRID)
+        vox = voxelizar(pos, idx, GRID)
+        corpo = vox["tipo"]
+        desc = "voxelized superellipsoid mesh 48x20x14 cells, 20k triangles, 0.3-cell jitter (GPU voxelizer)"
+    else:
+        from cfd__gb300.geometry import mascara_analitica
+        corpo = mascara_analitica(GRID, 48, 20, 14, 2.5, 3.0, (0.28 * 320 + 48, 80, 3 + 14))
+        desc = "analytic superellipsoid 48x20x14 cells"
+    mt = montarTipos(GRID, corpo=corpo, esteira=False)
+    cfg = dict(omegaPlus=omega, lesCs=CS, inletU=[U_IN, 0.0, 0.0], beltU=[0.0, 0.0, 0.0], esponja=mt["esponja"])
+    return mt["tipo"], cfg, desc
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs, copy burst)"
+    return 6800.0, "fallback 6.8 TB/s"
+
+
+def ncu_traffic(kernel="k_step_inplace", workload_key="320x160x128"):
+    """Per-launch DRAM bytes of the step kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "lbm_step_f32_320x160x128.md")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip())
+            except ValueError:
+                return None
+    return None
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_measure(tipo, cfg, target_s=10.0, threads=None):
+    """The oracle step on the host cores, bounded to ~target_s seconds."""
+    from oracle import oracle as O
+    threads = threads or (os.cpu_count() or 1)
+    lat = O.Lattice((GRID["nx"], GRID["ny"], GRID["nz"]), nthreads=threads)
+    lat.set_types(tipo)
+    lat.configure(omega_plus=cfg["omegaPlus"], les_cs=cfg["lesCs"], inlet_u=cfg["inletU"], belt_u=cfg["beltU"],
+                  sponge_start=cfg["esponja"]["inicio"], sponge_len=cfg["esponja"]["comprimento"])
+    lat.init()
+    lat.run(1)  # warm-up
+    t0 = time.perf_counter()
+    lat.run(1)
+    one = time.perf_counter() - t0
+    n = max(1, min(200, int(target_s / max(one, 1e-6))))
+    t0 = time.perf_counter()
+    lat.run(n)
+    dt = time.perf_counter() - t0
+    N = GRID["nx"] * GRID["ny"] * GRID["nz"]
+    return {"value": N * n / dt / 1e6, "unit": "MLUPS", "cores": threads, "kind": "port",
+            "sample": f"{n} steps of the 320x160x128 tunnel (fp32 oracle restatement, OpenMP)", "seconds": dt}
+
+
+def run_reference(args):
+    world, rank, local = dist_setup()
+    if rank != 0:
+        return 0
+    tipo, cfg, desc = workload(body="analytic")
+    res = []
+    for _ in range(args.warmup):
+        pass
+    for _ in range(max(1, args.steps)):
+        res.append(cpu_measure(tipo, cfg, target_s=max(2.0, 20.0 / max(1, args.steps))))
+    v = statistics.median(r["value"] for r in res)
+    line = {
+        "impl": "reference", "metric": "MLUPS (D3Q19 TRT+LES step, fp32)", "value": v, "unit": "MLUPS",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"320x160x128 tunnel, {desc}", "cells": int(tipo.size)},
+        "cpu_baseline": {k: res[0][k] for k in ("kind", "cores", "sample")} | {"value": v, "unit": "MLUPS"},
+        "e2e": {"value": v, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference's step exists only as generated WGSL/GLSL for a browser GPU; this arm times its "
+                "CPU restatement (oracle/) on all host threads",
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def time_steps(s, stream, K):
+    import torch
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    s.passo(K)
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def run_ours(args):
+    import torch
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from cfd__gb300 import SolverCUDA
+    from cfd__gb300 import build as B
+
+    B.build()
+    tipo, cfg, desc = workload(body=args.body)
+    N = int(tipo.size)
+    stream = torch.cuda.Stream()
+
+    def make(storage):
+        s = SolverCUDA(GRID, storage=storage, escrever_macros=False)
+        s.definirStream(stream.cuda_stream)
+        s.definirTipos(tipo)
+        s.configurar(**cfg)
+        s.inicializar()
+        return s
+
+    s = make(args.storage)
+    s.passo(args.warmup)
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    barrier()
+    with Clocks(local) as clk:
+        t0 = time.perf_counter()
+        ms = time_steps(s, stream, args.steps)
+        wall = time.perf_counter() - t0
+    barrier()
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    mlups = N * args.steps / (ms / 1e3) / 1e6 * world
+
+    # roofline of the step kernel (one launch per step)
+    peak, peak_src = peaks()
+    bpc = BYTES_PER_CELL[args.storage]
+    achieved = bpc * N / (ms_step / 1e3) / 1e9
+    traffic = ncu_traffic()
+
+    # end to end through the public API: every step configures (params by
+    # value in the launch), steps, and reads the step's force back (24 B)
+    E = max(20, args.steps // 4)
+    s.passoComForcas(1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(E):
+        s.configurar(**cfg)
+        s.passoComForcas(1)
+    e2e_s = time.perf_counter() - t0
+    e2e = {"value": N * E / e2e_s / 1e6 * world, "unit": "MLUPS", "h2d_bytes_per_step": 52,
+           "d2h_bytes_per_step": 24, "steps": E,
+           "path": "SolverCUDA.configurar + passoComForcas(1) per step (C ABI lbm_configure, lbm_step_forces)"}
+    s.destruir()
+
+    forms = {}
+    if not args.no_forms:
+        for st in ("f16s", "bf16s"):
+            s2 = make(st)
+            s2.passo(args.warmup)
+            ms2 = time_steps(s2, stream, args.steps)
+            m2 = N * args.steps / (ms2 / 1e3) / 1e6
+            forms[st] = {"MLUPS": m2, "vs_f32": m2 / (mlups / world),
+                         "roofline_frac": BYTES_PER_CELL[st] * N / (ms2 / args.steps / 1e3) / 1e9 / peak}
+            s2.destruir()
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_measure(tipo, cfg, target_s=args.cpu_seconds)
+        cpu.pop("seconds", None)
+    if rank == 0:
+        line = {
+            "metric": "MLUPS (D3Q19 TRT+LES step, fp32 plain; 16-bit storage forms beside it)",
+            "value": mlups, "unit": "MLUPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": {"f32": "f32", "f16s": "f16 storage / f32 math", "bf16s": "bf16 storage / f32 math",
+                      "f64": "f64"}[args.storage],
+            "data": "synthetic",
+            "config": {"workload": f"320x160x128 tunnel, {desc}, u_in 0.06, Re 2000, Cs 0.12",
+                       "cells": N, "storage": args.storage, "layout": "in-place (esoteric pull)",
+                       "parallelism": "replicas" if world > 1 else "single",
+                       "l2": f"state {N * 19 * (bpc // 38) / 1e6:.0f} MB > 126 MB L2 (inputs larger than L2)"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
+                         "kernel": "k_step_inplace", "algorithmic_bytes_per_cell": bpc},
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": args.steps,
+            "clocks": clk.summary(),
+            "forms": forms,
+            "wall_s_timed": wall,
+        }
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=40)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--storage", default="f32", choices=["f32", "f16s", "bf16s", "f64"])
+    ap.add_argument("--body", default="mesh", choices=["mesh", "analytic"])
+    ap.add_argument("--no-forms", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,112 @@
+"""ctypes binding of include/lbm.h (and the voxelizer ABI in include/vox.h).
+
+The library is built in-tree by ``cfd__gb300.build.build()``.  There is no CPU
+fallback: if the library is missing or cannot be loaded, every solver call
+raises ``NativeUnavailable``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+from . import build as _build
+
+F32, F16S, BF16S, F64 = 0, 1, 2, 3
+FLAG_WRITE_MACROS, FLAG_PINGPONG = 1, 2
+
+OK, EINVAL, ENOMEM, ECUDA, ETIMEDOUT, ESTATE, ENOTSUP = 0, -1, -2, -3, -4, -5, -6
+_NAMES = {EINVAL: "EINVAL", ENOMEM: "ENOMEM", ECUDA: "ECUDA", ETIMEDOUT: "ETIMEDOUT",
+          ESTATE: "ESTATE", ENOTSUP: "ENOTSUP"}
+
+
+class NativeUnavailable(RuntimeError):
+    """The sm_103a library is not built or not loadable."""
+
+
+class LbmError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Dims(C.Structure):
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32)]
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("omega_plus", C.c_float), ("magic", C.c_float), ("les_cs", C.c_float),
+        ("belt_u", C.c_float * 3), ("inlet_u", C.c_float * 3),
+        ("sponge_start", C.c_float), ("sponge_len", C.c_float),
+        ("bl_thickness", C.c_float), ("closure", C.c_int32),
+    ]
+
+
+class Info(C.Structure):
+    _fields_ = [("n_cells", C.c_int64), ("device_bytes", C.c_int64), ("storage", C.c_int32),
+                ("flags", C.c_int32), ("steps", C.c_int64), ("parity", C.c_int32), ("block_x", C.c_int32)]
+
+
+_lib = None
+_lock = threading.Lock()
+
+# name -> (restype, argtypes); every entry point declared in include/*.h
+SIGNATURES = {
+    "lbm_create": (C.c_int, [C.POINTER(Dims), C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
+    "lbm_destroy": (C.c_int, [C.c_void_p]),
+    "lbm_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "lbm_configure": (C.c_int, [C.c_void_p, C.POINTER(Params)]),
+    "lbm_set_types": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    "lbm_init_equilibrium": (C.c_int, [C.c_void_p]),
+    "lbm_set_populations": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    "lbm_get_populations": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    "lbm_step": (C.c_int, [C.c_void_p, C.c_int]),
+    "lbm_step_forces": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "lbm_update_macros": (C.c_int, [C.c_void_p]),
+    "lbm_read_macros": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    "lbm_forces": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "lbm_mass": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "lbm_sync": (C.c_int, [C.c_void_p]),
+    "lbm_get_info": (C.c_int, [C.c_void_p, C.POINTER(Info)]),
+    "lbm_last_error": (C.c_char_p, []),
+    "lbm_set_block": (C.c_int, [C.c_void_p, C.c_int]),
+}
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = False):
+    """Load the library (optionally building it first).  Raises NativeUnavailable."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = lib_path()
+        if not os.path.exists(path):
+            if not build_if_missing:
+                raise NativeUnavailable(
+                    f"{path} is missing: build it with cfd__gb300.build.build() (nvcc, sm_103a)")
+            _build.build()
+        try:
+            L = C.CDLL(path)
+        except OSError as e:  # pragma: no cover - depends on the machine
+            raise NativeUnavailable(f"cannot load {path}: {e}") from e
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+        return L
+
+
+def check(rc: int) -> None:
+    if rc != OK:
+        msg = _lib.lbm_last_error().decode("utf-8", "replace") if _lib is not None else ""
+        raise LbmError(rc, msg)
+
+
+def ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)

@@ -1,0 +1,463 @@
+// lbm_api.cu — the C ABI of include/lbm.h: solver contexts, the link-word
+// builder, deterministic reductions and the dispatch into the per-storage
+// kernel instantiations (lbm_inst_*.cu).
+//
+// Member-by-member counterpart of the reference's SolverWebGPU
+// (src/backend/webgpu/solver.js:36-528); each function cites its member.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/lbm.h"
+#include "lbm_kernels.cuh"
+
+using namespace lbm;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  char buf[256];
+  snprintf(buf, sizeof buf, "%s: %s (%s)", what, cudaGetErrorString(e), cudaGetErrorName(e));
+  return fail(LBM_ECUDA, buf);
+}
+
+#define CK(call, what)                                 \
+  do {                                                 \
+    cudaError_t _e = (call);                           \
+    if (_e != cudaSuccess) return cuda_fail(_e, what); \
+  } while (0)
+
+// Per-cell link words (see LINK_* in lbm_core.cuh).
+__global__ void k_links(const uint8_t* __restrict__ tipo, uint32_t* __restrict__ link, int nx, int ny, int nz) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  if (x >= nx || y >= ny) return;
+  const int64_t cell = ((int64_t)z * ny + y) * nx + x;
+  const Wrap w = wrap3(x, y, z, nx, ny, nz);
+  uint32_t bits = 0;
+  bool has_body = false, has_wall = false, has_belt = false;
+#pragma unroll
+  for (int k = 1; k < Q; ++k) {
+    const uint32_t t = tipo[nbr(k, -1, x, y, z, w, nx, ny)];
+    if (is_solid(t)) {
+      bits |= 1u << (k - 1);
+      has_body |= t == SOLIDO;
+      has_wall |= t == PAREDE;
+      has_belt |= t == SOLIDO_MOVEL;
+    }
+  }
+  uint32_t lw = bits | ((uint32_t)tipo[cell] << LINK_CLASS_SHIFT);
+  if (has_belt || (has_body && has_wall)) lw |= LINK_SLOW;
+  if (has_body && !has_wall && !has_belt) lw |= LINK_BODY;
+  link[cell] = lw;
+}
+
+// Deterministic single-block sum of n triples: each thread walks a fixed
+// stride, then a fixed tree.  out[3].
+__global__ void k_reduce3(const double* __restrict__ part, int64_t n, double* __restrict__ out) {
+  __shared__ double sh[3][256];
+  const int t = threadIdx.x;
+  double a = 0, b = 0, c = 0;
+  for (int64_t i = t; i < n; i += 256) {
+    a += part[3 * i];
+    b += part[3 * i + 1];
+    c += part[3 * i + 2];
+  }
+  sh[0][t] = a; sh[1][t] = b; sh[2][t] = c;
+  __syncthreads();
+  for (int s = 128; s > 0; s >>= 1) {
+    if (t < s) {
+      sh[0][t] += sh[0][t + s];
+      sh[1][t] += sh[1][t + s];
+      sh[2][t] += sh[2][t + s];
+    }
+    __syncthreads();
+  }
+  if (t == 0) { out[0] = sh[0][0]; out[1] = sh[1][0]; out[2] = sh[2][0]; }
+}
+
+}  // namespace
+
+struct lbm_ctx {
+  lbm_dims dims{};
+  int64_t N = 0;
+  int storage = LBM_F32;
+  int flags = 0;
+  bool inplace = true;
+  Ops ops{};
+  void* pop = nullptr;    // in-place set, or ping-pong front
+  void* pop2 = nullptr;   // ping-pong back
+  uint8_t* tipo = nullptr;
+  uint32_t* link = nullptr;
+  float4* macros = nullptr;
+  double* partials = nullptr;
+  int64_t npart = 0;
+  double* red = nullptr;       // 3 doubles
+  double* fbuf = nullptr;      // per-step fused forces
+  int64_t fbuf_cap = 0;        // in steps
+  double* stage = nullptr;     // N doubles for set/get
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  Params P{};
+  bool configured = false, types_set = false, state_set = false;
+  int64_t steps = 0;
+  int block_x = 0, block_y = 1;
+  int64_t dev_bytes = 0;
+};
+
+namespace {
+
+Ops ops_for(int storage) {
+  switch (storage) {
+    case LBM_F32: return ops_f32();
+    case LBM_F64: return ops_f64();
+    case LBM_F16S: return ops_f16s();
+    default: return ops_bf16s();
+  }
+}
+
+Launch cell_launch(const lbm_ctx* c) {
+  int bx = c->block_x;
+  if (bx <= 0) {
+    bx = 128;
+    const int rx = ((c->dims.nx + 31) / 32) * 32;
+    if (rx < bx) bx = rx;
+  }
+  int by = c->block_y > 0 ? c->block_y : 1;
+  while (bx * by > 256) by = std::max(1, by / 2);
+  Launch L;
+  L.block = dim3(bx, by, 1);
+  L.grid = dim3((c->dims.nx + bx - 1) / bx, (c->dims.ny + by - 1) / by, c->dims.nz);
+  return L;
+}
+
+Dev dev_of(const lbm_ctx* c) {
+  Dev d;
+  d.nx = c->dims.nx; d.ny = c->dims.ny; d.nz = c->dims.nz;
+  d.N = c->N;
+  d.pop = c->pop; d.pop2 = c->pop2;
+  d.tipo = c->tipo; d.link = c->link;
+  d.macros = c->macros;
+  d.force = nullptr;
+  return d;
+}
+
+int dalloc(lbm_ctx* c, void** p, size_t bytes, const char* what) {
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    char buf[256];
+    snprintf(buf, sizeof buf, "device allocation of %.3f GB for %s failed (%dx%dx%d): %s",
+             bytes / 1e9, what, c->dims.nx, c->dims.ny, c->dims.nz, cudaGetErrorString(e));
+    *p = nullptr;
+    return fail(LBM_ENOMEM, buf);
+  }
+  c->dev_bytes += (int64_t)bytes;
+  return LBM_OK;
+}
+
+int ensure_macros(lbm_ctx* c) {
+  if (c->macros) return LBM_OK;
+  return dalloc(c, (void**)&c->macros, sizeof(float4) * (size_t)c->N, "macros");
+}
+
+int ensure_partials(lbm_ctx* c, int64_t n) {
+  if (c->npart >= n) return LBM_OK;
+  if (c->partials) { cudaFree(c->partials); c->dev_bytes -= 3 * sizeof(double) * c->npart; c->partials = nullptr; }
+  int r = dalloc(c, (void**)&c->partials, 3 * sizeof(double) * (size_t)n, "reduction partials");
+  if (r) { c->npart = 0; return r; }
+  c->npart = n;
+  return LBM_OK;
+}
+
+int ensure_stage(lbm_ctx* c) {
+  if (c->stage) return LBM_OK;
+  return dalloc(c, (void**)&c->stage, sizeof(double) * (size_t)c->N, "state staging");
+}
+
+int parity(const lbm_ctx* c) { return c->inplace ? (int)(c->steps & 1) : 0; }
+
+int check_ready(lbm_ctx* c, bool need_cfg) {
+  if (!c) return fail(LBM_EINVAL, "null context");
+  if (!c->types_set) return fail(LBM_ESTATE, "cell types not set (call lbm_set_types first)");
+  if (need_cfg && !c->configured) return fail(LBM_ESTATE, "parameters not set (call lbm_configure first)");
+  return LBM_OK;
+}
+
+// One step; mac/frc select the kernel variant.  force: 3 doubles or null.
+int launch_step(lbm_ctx* c, bool mac, double* force) {
+  Dev d = dev_of(c);
+  d.force = force;
+  cudaError_t e = c->ops.step(d, c->P, parity(c), c->inplace, mac, force != nullptr, cell_launch(c), c->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "step kernel launch");
+  if (!c->inplace) std::swap(c->pop, c->pop2);
+  c->steps++;
+  return LBM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* lbm_last_error(void) { return g_err.c_str(); }
+
+int lbm_create(const lbm_dims* dims, int storage, int flags, lbm_ctx** out) {
+  if (!dims || !out) return fail(LBM_EINVAL, "null argument");
+  *out = nullptr;
+  if (dims->nx < 1 || dims->ny < 1 || dims->nz < 1) return fail(LBM_EINVAL, "grid dimensions must be >= 1");
+  if (dims->ny > 65535 * 256 || dims->nz > 65535) return fail(LBM_EINVAL, "grid too large for the launch shape");
+  if (storage < LBM_F32 || storage > LBM_F64) return fail(LBM_EINVAL, "unknown storage form");
+  if (flags & ~(LBM_FLAG_WRITE_MACROS | LBM_FLAG_PINGPONG)) return fail(LBM_EINVAL, "unknown flag bits");
+  lbm_ctx* c = new lbm_ctx();
+  c->dims = *dims;
+  c->N = (int64_t)dims->nx * dims->ny * dims->nz;
+  c->storage = storage;
+  c->flags = flags;
+  c->inplace = !(flags & LBM_FLAG_PINGPONG);
+  c->ops = ops_for(storage);
+  const size_t set_bytes = (size_t)c->N * Q * c->ops.elem_bytes;
+  int r = dalloc(c, &c->pop, set_bytes, "populations");
+  if (!r && !c->inplace) r = dalloc(c, &c->pop2, set_bytes, "second population set");
+  if (!r) r = dalloc(c, (void**)&c->tipo, (size_t)c->N, "cell types");
+  if (!r && c->inplace) r = dalloc(c, (void**)&c->link, sizeof(uint32_t) * (size_t)c->N, "link words");
+  if (!r) r = dalloc(c, (void**)&c->red, 3 * sizeof(double), "reduction result");
+  if (!r && (flags & LBM_FLAG_WRITE_MACROS)) r = ensure_macros(c);
+  if (r) { lbm_destroy(c); return r; }
+  cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) { lbm_destroy(c); return cuda_fail(e, "cudaStreamCreate"); }
+  c->own_stream = true;
+  // Rest state: g = 0 everywhere (src/core/lattice.js:32-34).
+  e = cudaMemsetAsync(c->pop, 0, set_bytes, c->stream);
+  if (e == cudaSuccess && c->pop2) e = cudaMemsetAsync(c->pop2, 0, set_bytes, c->stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(c->tipo, 0, (size_t)c->N, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) { lbm_destroy(c); return cuda_fail(e, "initial clear"); }
+  *out = c;
+  return LBM_OK;
+}
+
+int lbm_destroy(lbm_ctx* c) {
+  if (!c) return fail(LBM_EINVAL, "null context");
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  void* ps[] = {c->pop, c->pop2, c->tipo, c->link, c->macros, c->partials, c->red, c->fbuf, c->stage};
+  for (void* p : ps)
+    if (p) cudaFree(p);
+  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return LBM_OK;
+}
+
+int lbm_set_stream(lbm_ctx* c, void* s) {
+  if (!c) return fail(LBM_EINVAL, "null context");
+  CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+  if (c->own_stream) cudaStreamDestroy(c->stream);
+  c->stream = static_cast<cudaStream_t>(s);
+  c->own_stream = false;
+  return LBM_OK;
+}
+
+int lbm_configure(lbm_ctx* c, const lbm_params* p) {
+  if (!c || !p) return fail(LBM_EINVAL, "null argument");
+  if (p->closure != 0 && p->closure != 1) return fail(LBM_EINVAL, "closure must be 0 or 1");
+  Params P;
+  P.omega_plus = p->omega_plus; P.magic = p->magic; P.les_cs = p->les_cs;
+  for (int a = 0; a < 3; ++a) { P.belt[a] = p->belt_u[a]; P.inlet[a] = p->inlet_u[a]; }
+  P.sponge_start = p->sponge_start; P.sponge_len = p->sponge_len; P.bl = p->bl_thickness;
+  P.closure = p->closure;
+  c->P = P;
+  c->configured = true;
+  return LBM_OK;
+}
+
+int lbm_set_types(lbm_ctx* c, const uint32_t* tipo, size_t n) {
+  if (!c || !tipo) return fail(LBM_EINVAL, "null argument");
+  if ((int64_t)n != c->N) {
+    char buf[128];
+    snprintf(buf, sizeof buf, "cell-type field has %zu entries, expected %lld", n, (long long)c->N);
+    return fail(LBM_EINVAL, buf);
+  }
+  std::vector<uint8_t> t8((size_t)n);
+  for (size_t i = 0; i < n; ++i) {
+    if (tipo[i] > 7u) {
+      char buf[128];
+      snprintf(buf, sizeof buf, "cell type %u at index %zu is not a CELULA code (0..7)", tipo[i], i);
+      return fail(LBM_EINVAL, buf);
+    }
+    t8[i] = (uint8_t)tipo[i];
+  }
+  CK(cudaMemcpyAsync(c->tipo, t8.data(), n, cudaMemcpyHostToDevice, c->stream), "types upload");
+  if (c->inplace) {
+    Launch L = cell_launch(c);
+    k_links<<<L.grid, L.block, 0, c->stream>>>(c->tipo, c->link, c->dims.nx, c->dims.ny, c->dims.nz);
+    CK(cudaGetLastError(), "link kernel launch");
+  }
+  CK(cudaStreamSynchronize(c->stream), "types upload sync");
+  c->types_set = true;
+  return LBM_OK;
+}
+
+int lbm_init_equilibrium(lbm_ctx* c) {
+  int r = check_ready(c, true);
+  if (r) return r;
+  c->steps = 0;
+  CK(c->ops.init(dev_of(c), c->P, c->inplace, cell_launch(c), c->stream), "init kernel launch");
+  c->state_set = true;
+  return LBM_OK;
+}
+
+int lbm_set_populations(lbm_ctx* c, const double* g, size_t n) {
+  if (!c || !g) return fail(LBM_EINVAL, "null argument");
+  if ((int64_t)n != Q * c->N) return fail(LBM_EINVAL, "population array must hold 19*N values");
+  int r = ensure_stage(c);
+  if (r) return r;
+  c->steps = 0;
+  for (int k = 0; k < Q; ++k) {
+    CK(cudaMemcpyAsync(c->stage, g + (size_t)k * c->N, sizeof(double) * c->N, cudaMemcpyHostToDevice, c->stream),
+       "population upload");
+    CK(c->ops.put_dir(dev_of(c), c->stage, k, 0, c->inplace, cell_launch(c), c->stream), "population scatter");
+  }
+  CK(cudaStreamSynchronize(c->stream), "population upload sync");
+  c->state_set = true;
+  return LBM_OK;
+}
+
+int lbm_get_populations(lbm_ctx* c, double* g, size_t n) {
+  if (!c || !g) return fail(LBM_EINVAL, "null argument");
+  if ((int64_t)n != Q * c->N) return fail(LBM_EINVAL, "population array must hold 19*N values");
+  int r = ensure_stage(c);
+  if (r) return r;
+  for (int k = 0; k < Q; ++k) {
+    CK(c->ops.get_dir(dev_of(c), c->stage, k, parity(c), c->inplace, cell_launch(c), c->stream), "population gather");
+    CK(cudaMemcpyAsync(g + (size_t)k * c->N, c->stage, sizeof(double) * c->N, cudaMemcpyDeviceToHost, c->stream),
+       "population download");
+    CK(cudaStreamSynchronize(c->stream), "population download sync");
+  }
+  return LBM_OK;
+}
+
+int lbm_step(lbm_ctx* c, int n) {
+  int r = check_ready(c, true);
+  if (r) return r;
+  if (n < 0) return fail(LBM_EINVAL, "negative step count");
+  const bool want_mac = (c->flags & LBM_FLAG_WRITE_MACROS) != 0;
+  if (want_mac && (r = ensure_macros(c))) return r;
+  for (int k = 0; k < n; ++k) {
+    r = launch_step(c, want_mac && k == n - 1, nullptr);
+    if (r) return r;
+  }
+  return LBM_OK;
+}
+
+int lbm_step_forces(lbm_ctx* c, int n, double* out_f) {
+  int r = check_ready(c, true);
+  if (r) return r;
+  if (n < 0 || (n > 0 && !out_f)) return fail(LBM_EINVAL, "bad step count or null output");
+  if (n == 0) return LBM_OK;
+  const bool want_mac = (c->flags & LBM_FLAG_WRITE_MACROS) != 0;
+  if (want_mac && (r = ensure_macros(c))) return r;
+  if (c->fbuf_cap < n) {
+    if (c->fbuf) { cudaFree(c->fbuf); c->dev_bytes -= 3 * sizeof(double) * c->fbuf_cap; c->fbuf = nullptr; c->fbuf_cap = 0; }
+    r = dalloc(c, (void**)&c->fbuf, 3 * sizeof(double) * (size_t)n, "per-step forces");
+    if (r) return r;
+    c->fbuf_cap = n;
+  }
+  CK(cudaMemsetAsync(c->fbuf, 0, 3 * sizeof(double) * (size_t)n, c->stream), "force buffer clear");
+  for (int k = 0; k < n; ++k) {
+    r = launch_step(c, want_mac && k == n - 1, c->fbuf + 3 * (size_t)k);
+    if (r) return r;
+  }
+  CK(cudaMemcpyAsync(out_f, c->fbuf, 3 * sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, c->stream),
+     "force download");
+  CK(cudaStreamSynchronize(c->stream), "force download sync");
+  return LBM_OK;
+}
+
+int lbm_update_macros(lbm_ctx* c) {
+  int r = check_ready(c, false);
+  if (r) return r;
+  if ((r = ensure_macros(c))) return r;
+  CK(c->ops.macros(dev_of(c), parity(c), c->inplace, cell_launch(c), c->stream), "macros kernel launch");
+  return LBM_OK;
+}
+
+int lbm_read_macros(lbm_ctx* c, float* out, size_t n) {
+  if (!c || !out) return fail(LBM_EINVAL, "null argument");
+  if ((int64_t)n != 4 * c->N) return fail(LBM_EINVAL, "macros array must hold 4*N floats");
+  int r = ensure_macros(c);
+  if (r) return r;
+  CK(cudaMemcpyAsync(out, c->macros, sizeof(float4) * (size_t)c->N, cudaMemcpyDeviceToHost, c->stream),
+     "macros download");
+  CK(cudaStreamSynchronize(c->stream), "macros download sync");
+  return LBM_OK;
+}
+
+int lbm_forces(lbm_ctx* c, double f[3]) {
+  int r = check_ready(c, false);
+  if (r) return r;
+  if (!f) return fail(LBM_EINVAL, "null output");
+  Launch L = cell_launch(c);
+  const int64_t nb = (int64_t)L.grid.x * L.grid.y * L.grid.z;
+  if ((r = ensure_partials(c, nb))) return r;
+  CK(c->ops.forces(dev_of(c), parity(c), c->inplace, c->partials, L, c->stream), "force kernel launch");
+  k_reduce3<<<1, 256, 0, c->stream>>>(c->partials, nb, c->red);
+  CK(cudaGetLastError(), "reduce kernel launch");
+  CK(cudaMemcpyAsync(f, c->red, 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "force download");
+  CK(cudaStreamSynchronize(c->stream), "force sync");
+  return LBM_OK;
+}
+
+int lbm_mass(lbm_ctx* c, double* sum) {
+  int r = check_ready(c, false);
+  if (r) return r;
+  if (!sum) return fail(LBM_EINVAL, "null output");
+  Launch L = cell_launch(c);
+  const int64_t nb = (int64_t)L.grid.x * L.grid.y * L.grid.z;
+  if ((r = ensure_partials(c, nb))) return r;
+  CK(c->ops.mass(dev_of(c), parity(c), c->inplace, c->partials, L, c->stream), "mass kernel launch");
+  k_reduce3<<<1, 256, 0, c->stream>>>(c->partials, nb, c->red);
+  CK(cudaGetLastError(), "reduce kernel launch");
+  double out[3];
+  CK(cudaMemcpyAsync(out, c->red, 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "mass download");
+  CK(cudaStreamSynchronize(c->stream), "mass sync");
+  *sum = out[0];
+  return LBM_OK;
+}
+
+int lbm_sync(lbm_ctx* c) {
+  if (!c) return fail(LBM_EINVAL, "null context");
+  CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+  return LBM_OK;
+}
+
+int lbm_get_info(lbm_ctx* c, lbm_info* info) {
+  if (!c || !info) return fail(LBM_EINVAL, "null argument");
+  info->n_cells = c->N;
+  info->device_bytes = c->dev_bytes;
+  info->storage = c->storage;
+  info->flags = c->flags;
+  info->steps = c->steps;
+  info->parity = (int)(c->steps & 1);
+  info->block_x = (int)cell_launch(c).block.x;
+  return LBM_OK;
+}
+
+int lbm_set_block(lbm_ctx* c, int block_x) {
+  if (!c) return fail(LBM_EINVAL, "null context");
+  if (block_x < 0 || block_x > 256 || (block_x % 32) != 0) return fail(LBM_EINVAL, "block_x must be 0 or a multiple of 32 up to 256");
+  c->block_x = block_x;
+  return LBM_OK;
+}
+
+}  // extern "C"

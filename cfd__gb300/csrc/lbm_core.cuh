@@ -1,0 +1,297 @@
+// lbm_core.cuh — D3Q19 tables and the per-cell collide shared by every step
+// kernel of the GB300 solver.
+//
+// The arithmetic restates the reference's generated step body
+// (src/core/emit/ir.js:493-533, blocks :166-478) operation by operation: the
+// files that include this header are compiled with -fmad=false and IEEE
+// division/sqrt, so each fp32 operation rounds exactly where the shader text
+// writes it.  That makes the fp32 path bit-identical to the CPU oracle.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <cuda_bf16.h>
+
+namespace lbm {
+
+constexpr int Q = 19;
+
+// Cell classes (src/core/emit/ir.js:71-80).
+enum : uint32_t {
+  FLUIDO = 0, SOLIDO = 1, ENTRADA = 2, SAIDA = 3, SOLIDO_MOVEL = 4,
+  ESPELHO_Y = 5, ESPELHO_Z = 6, PAREDE = 7
+};
+
+__host__ __device__ constexpr bool is_solid(uint32_t t) {
+  return t == SOLIDO || t == SOLIDO_MOVEL || t == PAREDE;
+}
+
+// Velocity set with opposite pairs adjacent (src/core/lattice.js:57-79).
+__host__ __device__ constexpr int cx(int i) {
+  return (i == 1 || i == 7 || i == 9 || i == 11 || i == 13) ? 1
+       : (i == 2 || i == 8 || i == 10 || i == 12 || i == 14) ? -1 : 0;
+}
+__host__ __device__ constexpr int cy(int i) {
+  return (i == 3 || i == 7 || i == 10 || i == 15 || i == 17) ? 1
+       : (i == 4 || i == 8 || i == 9 || i == 16 || i == 18) ? -1 : 0;
+}
+__host__ __device__ constexpr int cz(int i) {
+  return (i == 5 || i == 11 || i == 14 || i == 15 || i == 18) ? 1
+       : (i == 6 || i == 12 || i == 13 || i == 16 || i == 17) ? -1 : 0;
+}
+__host__ __device__ constexpr int ci(int i, int a) { return a == 0 ? cx(i) : (a == 1 ? cy(i) : cz(i)); }
+// opp(0) = 0, opp(i) = ((i-1)^1)+1 (src/core/lattice.js:89)
+__host__ __device__ constexpr int opp(int i) { return i == 0 ? 0 : (((i - 1) ^ 1) + 1); }
+// Specular reflection across axis `ax` (espelharIdx, src/core/emit/ir.js:86-93).
+__host__ __device__ constexpr int mirror_idx(int i, int ax) {
+  int j = 0;
+  for (int k = 0; k < Q; ++k) {
+    const int a0 = ax == 0 ? -cx(i) : cx(i);
+    const int a1 = ax == 1 ? -cy(i) : cy(i);
+    const int a2 = ax == 2 ? -cz(i) : cz(i);
+    if (cx(k) == a0 && cy(k) == a1 && cz(k) == a2) j = k;
+  }
+  return j;
+}
+
+// Weights as the shader literals (num(), src/core/emit/ir.js:99-106) for fp32,
+// the exact rationals rounded once for fp64.
+template <typename R> struct Lit;
+template <> struct Lit<float> {
+  __host__ __device__ static constexpr float w(int i) {
+    return i == 0 ? 0.333333333f : (i <= 6 ? 0.0555555556f : 0.0277777778f);
+  }
+  // 2 w_i / c_s^2 (src/core/emit/ir.js:185)
+  __host__ __device__ static constexpr float sixw(int i) {
+    return i == 0 ? 0.0f : (i <= 6 ? 0.333333333f : 0.166666667f);
+  }
+  __host__ __device__ static constexpr float bl_exp() { return 0.1428571429f; }
+};
+template <> struct Lit<double> {
+  __host__ __device__ static constexpr double w(int i) {
+    return i == 0 ? 1.0 / 3.0 : (i <= 6 ? 1.0 / 18.0 : 1.0 / 36.0);
+  }
+  __host__ __device__ static constexpr double sixw(int i) { return i == 0 ? 0.0 : 2.0 * w(i) * 3.0; }
+  __host__ __device__ static constexpr double bl_exp() { return 0.1428571429; }
+};
+
+__device__ __forceinline__ float r_sqrt(float v) { return sqrtf(v); }
+__device__ __forceinline__ double r_sqrt(double v) { return sqrt(v); }
+__device__ __forceinline__ float r_pow(float a, float b) { return powf(a, b); }
+__device__ __forceinline__ double r_pow(double a, double b) { return pow(a, b); }
+
+// Kernel-side copy of lbm_params (src/core/emit/wgsl.js:123-135).
+struct Params {
+  float omega_plus, magic, les_cs;
+  float belt[3], inlet[3];
+  float sponge_start, sponge_len, bl;
+  int32_t closure;
+};
+
+// c_i . v with the term order dotC emits (src/core/emit/ir.js:116-126).
+template <typename R>
+__device__ __forceinline__ R dotc(int i, R vx, R vy, R vz) {
+  const int a = cx(i), b = cy(i), c = cz(i);
+  R acc = R(0);
+  bool first = true;
+  if (a != 0) { acc = a > 0 ? vx : -vx; first = false; }
+  if (b != 0) { if (first) { acc = b > 0 ? vy : -vy; first = false; } else acc = b > 0 ? acc + vy : acc - vy; }
+  if (c != 0) { if (first) { acc = c > 0 ? vz : -vz; } else acc = c > 0 ? acc + vz : acc - vz; }
+  return acc;
+}
+
+// Signed sum over the directions with coefficient k(i) != 0, index order,
+// as the emitter joins the terms (src/core/emit/ir.js:201-208, :272-282).
+template <typename R, typename K>
+__device__ __forceinline__ R signed_sum(const R* v, K coef) {
+  R acc = R(0);
+  bool first = true;
+#pragma unroll
+  for (int i = 0; i < Q; ++i) {
+    const int c = coef(i);
+    if (c == 0) continue;
+    if (first) { acc = c > 0 ? v[i] : -v[i]; first = false; }
+    else acc = c > 0 ? acc + v[i] : acc - v[i];
+  }
+  return acc;
+}
+
+// Equilibrium of one direction (src/core/emit/ir.js:216-232).
+template <typename R>
+__device__ __forceinline__ R equilibrium(int i, R delta, R rho, R ux, R uy, R uz, R uu) {
+  if (i == 0) return Lit<R>::w(0) * (delta - R(1.5) * rho * uu);
+  const R cu = dotc<R>(i, ux, uy, uz);
+  return Lit<R>::w(i) * (delta + rho * (R(3.0) * cu + R(4.5) * cu * cu - R(1.5) * uu));
+}
+
+// Pulled moments (src/core/emit/ir.js:192-213).
+template <typename R>
+__device__ __forceinline__ void moments(const R* g, R& delta, R& rho, R& ux, R& uy, R& uz, R& uu) {
+  delta = g[0];
+#pragma unroll
+  for (int i = 1; i < Q; ++i) delta = delta + g[i];
+  rho = R(1.0) + delta;
+  const R mx = signed_sum<R>(g, [](int i) { return cx(i); });
+  const R my = signed_sum<R>(g, [](int i) { return cy(i); });
+  const R mz = signed_sum<R>(g, [](int i) { return cz(i); });
+  ux = mx / rho;
+  uy = my / rho;
+  uz = mz / rho;
+  uu = ux * ux + uy * uy + uz * uz;
+}
+
+// Everything after the pull for one non-solid cell: the boundary branches and
+// the fluid collide with LES, TRT and sponge (src/core/emit/ir.js:505-530).
+// g: pulled populations; out: post-collision populations.  Returns nothing;
+// the caller owns the loads, stores and the macros (u, delta) it already has.
+template <typename R>
+__device__ __forceinline__ void collide(const Params& P, uint32_t ct, int x, int z, const R* g,
+                                        R delta, R rho, R ux, R uy, R uz, R uu, R* out) {
+  if (ct == ESPELHO_Y) {
+#pragma unroll
+    for (int i = 0; i < Q; ++i) out[i] = g[mirror_idx(i, 1)];
+    return;
+  }
+  if (ct == ESPELHO_Z) {
+#pragma unroll
+    for (int i = 0; i < Q; ++i) out[i] = g[mirror_idx(i, 2)];
+    return;
+  }
+  if (ct == ENTRADA) {
+    // blocoEntrada with the boundary-layer factor of the kernel header
+    // (src/core/emit/ir.js:405-422; src/core/emit/wgsl.js:217-220)
+    const R bl = R(P.bl);
+    const R uInletBL = bl > R(1.0) ? bl : R(1.0);
+    const R zc = R(z) + R(0.5);
+    const R blf = zc < bl ? r_pow(zc / uInletBL, Lit<R>::bl_exp()) : R(1.0);
+    const R ex = R(P.inlet[0]) * blf, ey = R(P.inlet[1]) * blf, ez = R(P.inlet[2]) * blf;
+    const R deltaIn = R(0.0), rhoIn = R(1.0);
+    const R uuIn = ex * ex + ey * ey + ez * ez;
+    out[0] = Lit<R>::w(0) * (deltaIn - R(1.5) * rhoIn * uuIn);
+#pragma unroll
+    for (int i = 1; i < Q; ++i) {
+      const R c = dotc<R>(i, ex, ey, ez);
+      out[i] = Lit<R>::w(i) * (deltaIn + rhoIn * (R(3.0) * c + R(4.5) * c * c - R(1.5) * uuIn));
+    }
+    return;
+  }
+  if (ct == SAIDA) {
+    // blocoSaida with the pulled u (src/core/emit/ir.js:432-444, :512-515)
+    out[0] = Lit<R>::w(0) * (R(-1.5) * uu);
+#pragma unroll
+    for (int i = 1; i < Q; ++i) {
+      const R c = dotc<R>(i, ux, uy, uz);
+      out[i] = Lit<R>::w(i) * (R(3.0) * c + R(4.5) * c * c - R(1.5) * uu);
+    }
+    return;
+  }
+  // FLUIDO: equilibrium, Smagorinsky LES (src/core/emit/ir.js:262-301)
+  R n[Q];
+#pragma unroll
+  for (int i = 0; i < Q; ++i) n[i] = g[i] - equilibrium<R>(i, delta, rho, ux, uy, uz, uu);
+  const R pxx = signed_sum<R>(n, [](int i) { return cx(i) * cx(i); });
+  const R pyy = signed_sum<R>(n, [](int i) { return cy(i) * cy(i); });
+  const R pzz = signed_sum<R>(n, [](int i) { return cz(i) * cz(i); });
+  const R pxy = signed_sum<R>(n, [](int i) { return cx(i) * cy(i); });
+  const R pxz = signed_sum<R>(n, [](int i) { return cx(i) * cz(i); });
+  const R pyz = signed_sum<R>(n, [](int i) { return cy(i) * cz(i); });
+  const R pp = pxx * pxx + pyy * pyy + pzz * pzz + R(2.0) * (pxy * pxy + pxz * pxz + pyz * pyz);
+  const R qs = r_sqrt(R(2.0) * pp);
+  const R cs = R(P.les_cs);
+  const R tau0 = R(1.0) / R(P.omega_plus);
+  const R tauT = R(0.5) * (tau0 + r_sqrt(tau0 * tau0 + R(18.0) * cs * cs * qs / rho));
+  const R omegaP = R(1.0) / tauT;
+  const R omegaM = R(1.0) / (R(P.magic) / (R(1.0) / omegaP - R(0.5)) + R(0.5));
+
+  // TRT per opposite pair (src/core/emit/ir.js:304-323); e_i = g_i - n_i is
+  // recomputed from the same operands, so it is the identical value.
+  const R e0 = equilibrium<R>(0, delta, rho, ux, uy, uz, uu);
+  out[0] = g[0] - omegaP * (g[0] - e0);
+#pragma unroll
+  for (int i = 1; i < Q; i += 2) {
+    const int j = i + 1;
+    const R ei = equilibrium<R>(i, delta, rho, ux, uy, uz, uu);
+    const R ej = equilibrium<R>(j, delta, rho, ux, uy, uz, uu);
+    const R p = R(0.5) * ((g[i] + g[j]) - (ei + ej));
+    const R m = R(0.5) * ((g[i] - g[j]) - (ei - ej));
+    out[i] = g[i] - omegaP * p - omegaM * m;
+    out[j] = g[j] - omegaP * p + omegaM * m;
+  }
+
+  // Sponge (src/core/emit/ir.js:458-478): mix(a, b, t) = a (1 - t) + b t.
+  // sig2 = 0 leaves every population unchanged (a*1 + b*0 == a for finite b),
+  // so cells before the sponge skip the blend.
+  const R sx = (R(x) - R(P.sponge_start)) / (R(P.sponge_len) > R(1.0) ? R(P.sponge_len) : R(1.0));
+  R sigma = sx > R(0.0) ? sx : R(0.0);
+  sigma = sigma < R(1.0) ? sigma : R(1.0);
+  const R sig2 = sigma * sigma;
+  if (sig2 != R(0.0)) {
+    const R ix = R(P.inlet[0]), iy = R(P.inlet[1]), iz = R(P.inlet[2]);
+    const R uuInf = ix * ix + iy * iy + iz * iz;
+    const R t0 = Lit<R>::w(0) * (R(-1.5) * uuInf);
+    out[0] = out[0] * (R(1.0) - sig2) + t0 * sig2;
+#pragma unroll
+    for (int i = 1; i < Q; ++i) {
+      const R si = dotc<R>(i, ix, iy, iz);
+      const R ti = Lit<R>::w(i) * (R(3.0) * si + R(4.5) * si * si - R(1.5) * uuInf);
+      out[i] = out[i] * (R(1.0) - sig2) + ti * sig2;
+    }
+  }
+}
+
+// ---------------------------------------------------------------- storage
+// Population storage forms.  Arithmetic is float (or double for the judge).
+struct StF32 {
+  using store_t = float;
+  using real = float;
+  static __device__ __forceinline__ float ld(const float* p) { return *p; }
+  static __device__ __forceinline__ void st(float* p, float v) { *p = v; }
+  static __device__ __forceinline__ float from_double(double v) { return (float)v; }
+};
+struct StF64 {
+  using store_t = double;
+  using real = double;
+  static __device__ __forceinline__ double ld(const double* p) { return *p; }
+  static __device__ __forceinline__ void st(double* p, double v) { *p = v; }
+  static __device__ __forceinline__ double from_double(double v) { return v; }
+};
+// fp16 holding g_i * 2^10: the scale lifts the ~1e-5 free-stream deviations
+// out of the fp16 subnormal range.  Scaling by a power of two is exact.
+struct StF16S {
+  using store_t = uint16_t;
+  using real = float;
+  static __device__ __forceinline__ float ld(const uint16_t* p) {
+    return __half2float(__ushort_as_half(*p)) * (1.0f / 1024.0f);
+  }
+  static __device__ __forceinline__ void st(uint16_t* p, float v) {
+    *p = __half_as_ushort(__float2half_rn(v * 1024.0f));
+  }
+  static __device__ __forceinline__ float from_double(double v) { return (float)v; }
+};
+struct StBF16S {
+  using store_t = uint16_t;
+  using real = float;
+  static __device__ __forceinline__ float ld(const uint16_t* p) {
+    return __bfloat162float(__ushort_as_bfloat16(*p));
+  }
+  static __device__ __forceinline__ void st(uint16_t* p, float v) {
+    *p = __bfloat16_as_ushort(__float2bfloat16_rn(v));
+  }
+  static __device__ __forceinline__ float from_double(double v) { return (float)v; }
+};
+
+// ------------------------------------------------------------- link words
+// Per-cell 32-bit word the in-place kernel reads instead of 18 neighbour
+// types (the reference gathers tipo[] for every direction,
+// src/core/emit/ir.js:176-186):
+//   bits 0..17  bit (k-1): the upstream cell x - c_k is solid (1, 4 or 7)
+//   bits 18..20 the cell's own class
+//   bit 21      slow path: some upstream solid is SOLIDO_MOVEL, or the
+//               upstream solids mix SOLIDO and PAREDE (read tipo[] per link)
+//   bit 22      every upstream solid is SOLIDO (the body): all bounce-back
+//               links count in the force
+constexpr uint32_t LINK_CLASS_SHIFT = 18;
+constexpr uint32_t LINK_SLOW = 1u << 21;
+constexpr uint32_t LINK_BODY = 1u << 22;
+
+}  // namespace lbm

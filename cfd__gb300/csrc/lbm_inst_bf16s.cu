@@ -1,0 +1,6 @@
+// lbm_inst_bf16s.cu — kernel instantiation for the bf16s population storage form.
+#include "lbm_kernels.cuh"
+
+namespace lbm {
+Ops ops_bf16s() { return OpsImpl<StBF16S>::make(); }
+}  // namespace lbm

@@ -1,0 +1,6 @@
+// lbm_inst_f16s.cu — kernel instantiation for the f16s population storage form.
+#include "lbm_kernels.cuh"
+
+namespace lbm {
+Ops ops_f16s() { return OpsImpl<StF16S>::make(); }
+}  // namespace lbm

@@ -1,0 +1,6 @@
+// lbm_inst_f32.cu — kernel instantiation for the f32 population storage form.
+#include "lbm_kernels.cuh"
+
+namespace lbm {
+Ops ops_f32() { return OpsImpl<StF32>::make(); }
+}  // namespace lbm

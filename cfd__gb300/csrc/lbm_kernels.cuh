@@ -1,0 +1,485 @@
+// lbm_kernels.cuh — the step, init, macros, force and mass kernels, templated
+// on the population storage form.  Included by one lbm_inst_<form>.cu per form
+// (compiled in parallel, -fmad=false).
+//
+// Two population layouts:
+//
+//  * IN-PLACE (default).  One population set; each population crosses HBM once
+//    per step (read 19, write 19: 152 B/cell in fp32).  The scheme is the
+//    "esoteric pull" of Lehmann (2022, Computation 10(6):92): for each
+//    opposite pair (i, i+1), i odd, with nb = x + c_i, a cell reads and writes
+//    the same two slots, F[.][x] and F[.][nb], swapping which slot holds which
+//    direction with the step parity.  With e = (steps even):
+//        pulled g_i     = F[e ? i+1 : i][x]      (= post-collision g_i(x - c_i))
+//        pulled g_{i+1} = F[e ? i : i+1][nb]     (= post-collision g_{i+1}(x + c_i))
+//        writes g*_i -> F[e ? i : i+1][nb],  g*_{i+1} -> F[e ? i+1 : i][x]
+//    The reference's fluid-node bounce-back (src/core/emit/ir.js:166-189) needs
+//    the cell's own post-collision g_{opp k} when x - c_k is solid.  That value
+//    sits in the other slot of the same location, which in this step belongs
+//    to the solid cell and is touched by nobody else, so the bounce-back read
+//    is the same load with the slot bit flipped: race-free and exact.
+//
+//  * A/B PING-PONG (flag LBM_FLAG_PINGPONG).  The reference's own scheme
+//    (src/backend/webgpu/solver.js:10-24): natural SoA, pull from the 18
+//    neighbours of src into dst, types gathered per direction.  Kept as the
+//    faithful debug path; both layouts give bit-identical states.
+#pragma once
+#include "lbm_core.cuh"
+
+namespace lbm {
+
+// Device-side view of one context's buffers.
+struct Dev {
+  int nx, ny, nz;
+  int64_t N;
+  void* pop;          // in-place: the set; ping-pong: the current (front) set
+  void* pop2;         // ping-pong only: the back set
+  const uint8_t* tipo;   // cell classes
+  const uint32_t* link;  // link words (in-place layout)
+  float4* macros;        // nullable
+  double* force;         // nullable: 3 doubles accumulated by the fused force
+};
+
+struct Wrap {
+  int xm, xp, ym, yp, zm, zp;
+};
+
+__device__ __forceinline__ Wrap wrap3(int x, int y, int z, int nx, int ny, int nz) {
+  Wrap w;
+  w.xm = x == 0 ? nx - 1 : x - 1;
+  w.xp = x == nx - 1 ? 0 : x + 1;
+  w.ym = y == 0 ? ny - 1 : y - 1;
+  w.yp = y == ny - 1 ? 0 : y + 1;
+  w.zm = z == 0 ? nz - 1 : z - 1;
+  w.zp = z == nz - 1 ? 0 : z + 1;
+  return w;
+}
+
+// Cell index of x + s*c_k (s = +1 downstream, -1 upstream), periodic.
+__device__ __forceinline__ int64_t nbr(int k, int s, int x, int y, int z, const Wrap& w, int nx, int ny) {
+  const int dx = s * cx(k), dy = s * cy(k), dz = s * cz(k);
+  const int xx = dx > 0 ? w.xp : (dx < 0 ? w.xm : x);
+  const int yy = dy > 0 ? w.yp : (dy < 0 ? w.ym : y);
+  const int zz = dz > 0 ? w.zp : (dz < 0 ? w.zm : z);
+  return ((int64_t)zz * ny + yy) * nx + xx;
+}
+
+// Where post-collision population k of cell `cell` lives in the in-place
+// layout at parity p (0: before an even step).  Returns the element offset.
+__device__ __forceinline__ int64_t eso_loc(int k, int p, int64_t cell, int x, int y, int z, const Wrap& w,
+                                           int nx, int ny, int64_t N) {
+  if (k == 0) return cell;
+  if (k & 1) {  // + member of the pair, stored at the downstream neighbour
+    const int64_t nb = nbr(k, +1, x, y, z, w, nx, ny);
+    return (int64_t)(p == 0 ? k + 1 : k) * N + nb;
+  }
+  return (int64_t)(p == 0 ? k - 1 : k) * N + cell;  // - member, stored locally
+}
+
+// Warp-level fp64 sum of three values; lane 0 adds them to dst atomically.
+__device__ __forceinline__ void warp_add3(double a, double b, double c, double* dst) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+    c += __shfl_xor_sync(0xffffffffu, c, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(dst + 0, a);
+    atomicAdd(dst + 1, b);
+    atomicAdd(dst + 2, c);
+  }
+}
+
+// ------------------------------------------------------------------ step
+// In-place step.  Grid: (ceil(nx/bx), ceil(ny/by), nz), block (bx, by).
+// PAR: step parity (0 even).  MAC: write (u, delta).  FRC: accumulate the
+// momentum-exchange force of the state being streamed.
+template <class St, int PAR, bool MAC, bool FRC>
+__global__ void __launch_bounds__(256) k_step_inplace(Dev d, Params P) {
+  using R = typename St::real;
+  using S = typename St::store_t;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  const int nx = d.nx, ny = d.ny;
+  const bool in = x < nx && y < ny;
+  double fx = 0.0, fy = 0.0, fz = 0.0;
+  if (in) {
+    const int64_t N = d.N;
+    const int64_t cell = ((int64_t)z * ny + y) * nx + x;
+    const uint32_t lw = __ldg(d.link + cell);
+    const uint32_t ct = (lw >> LINK_CLASS_SHIFT) & 7u;
+    if (is_solid(ct)) {
+      if (MAC) d.macros[cell] = make_float4(0.f, 0.f, 0.f, 0.f);
+    } else {
+      S* F = static_cast<S*>(d.pop);
+      const Wrap w = wrap3(x, y, z, nx, ny, d.nz);
+      constexpr bool E = (PAR == 0);
+      R g[Q];
+      int64_t nbo[Q];  // neighbour cell of each odd direction
+      g[0] = St::ld(F + cell);
+#pragma unroll
+      for (int i = 1; i < Q; i += 2) {
+        const int64_t nb = nbr(i, +1, x, y, z, w, nx, ny);
+        nbo[i] = nb;
+        const bool bbi = (lw >> (i - 1)) & 1u;   // upstream of +c_i  is x - c_i
+        const bool bbj = (lw >> i) & 1u;         // upstream of c_{i+1} is x + c_i
+        const int si = (E ^ bbi) ? i + 1 : i;
+        const int sj = (E ^ bbj) ? i : i + 1;
+        g[i] = St::ld(F + (int64_t)si * N + cell);
+        g[i + 1] = St::ld(F + (int64_t)sj * N + nb);
+      }
+      // Bounce-back links: moving-wall term and the fused force.
+      const uint32_t bbmask = lw & 0x3ffffu;
+      if (bbmask) {
+        if (lw & LINK_SLOW) {
+#pragma unroll
+          for (int k = 1; k < Q; ++k) {
+            if (!((bbmask >> (k - 1)) & 1u)) continue;
+            const uint32_t t = d.tipo[nbr(k, -1, x, y, z, w, nx, ny)];
+            if (t == SOLIDO_MOVEL) {
+              g[k] = g[k] + Lit<R>::sixw(k) * (dotc<R>(k, R(P.belt[0]), R(P.belt[1]), R(P.belt[2])));
+            }
+            if (FRC && ct == FLUIDO && t == SOLIDO) {
+              const R q = R(2.0) * (g[k] + Lit<R>::w(k));
+              fx -= (double)(cx(k) * q); fy -= (double)(cy(k) * q); fz -= (double)(cz(k) * q);
+            }
+          }
+        } else if (FRC && ct == FLUIDO && (lw & LINK_BODY)) {
+#pragma unroll
+          for (int k = 1; k < Q; ++k) {
+            if (!((bbmask >> (k - 1)) & 1u)) continue;
+            const R q = R(2.0) * (g[k] + Lit<R>::w(k));
+            fx -= (double)(cx(k) * q); fy -= (double)(cy(k) * q); fz -= (double)(cz(k) * q);
+          }
+        }
+      }
+      R delta, rho, ux, uy, uz, uu;
+      moments<R>(g, delta, rho, ux, uy, uz, uu);
+      R o[Q];
+      collide<R>(P, ct, x, z, g, delta, rho, ux, uy, uz, uu, o);
+      St::st(F + cell, o[0]);
+#pragma unroll
+      for (int i = 1; i < Q; i += 2) {
+        const int wi = E ? i : i + 1;       // slot receiving g*_i at the neighbour
+        const int wj = E ? i + 1 : i;       // slot receiving g*_{i+1} locally
+        St::st(F + (int64_t)wi * N + nbo[i], o[i]);
+        St::st(F + (int64_t)wj * N + cell, o[i + 1]);
+      }
+      if (MAC) d.macros[cell] = make_float4((float)ux, (float)uy, (float)uz, (float)delta);
+    }
+  }
+  if (FRC) {
+    const bool any = __any_sync(0xffffffffu, fx != 0.0 || fy != 0.0 || fz != 0.0);
+    if (any) warp_add3(fx, fy, fz, d.force);
+  }
+}
+
+// A/B ping-pong step: the reference's pull verbatim (tipo gathered per link).
+template <class St, bool MAC, bool FRC>
+__global__ void __launch_bounds__(256) k_step_ab(Dev d, Params P) {
+  using R = typename St::real;
+  using S = typename St::store_t;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  const int nx = d.nx, ny = d.ny;
+  double fx = 0.0, fy = 0.0, fz = 0.0;
+  if (x < nx && y < ny) {
+    const int64_t N = d.N;
+    const int64_t cell = ((int64_t)z * ny + y) * nx + x;
+    const uint32_t ct = d.tipo[cell];
+    if (is_solid(ct)) {
+      if (MAC) d.macros[cell] = make_float4(0.f, 0.f, 0.f, 0.f);
+    } else {
+      const S* src = static_cast<const S*>(d.pop);
+      S* dst = static_cast<S*>(d.pop2);
+      const Wrap w = wrap3(x, y, z, nx, ny, d.nz);
+      R g[Q];
+      g[0] = St::ld(src + cell);
+#pragma unroll
+      for (int i = 1; i < Q; ++i) {
+        const int64_t s = nbr(i, -1, x, y, z, w, nx, ny);
+        const uint32_t t = d.tipo[s];
+        if (is_solid(t)) {
+          const R bx = t == SOLIDO_MOVEL ? R(P.belt[0]) : R(0.0);
+          const R by = t == SOLIDO_MOVEL ? R(P.belt[1]) : R(0.0);
+          const R bz = t == SOLIDO_MOVEL ? R(P.belt[2]) : R(0.0);
+          const R gb = St::ld(src + (int64_t)opp(i) * N + cell);
+          g[i] = gb + Lit<R>::sixw(i) * (dotc<R>(i, bx, by, bz));
+          if (FRC && ct == FLUIDO && t == SOLIDO) {
+            const R q = R(2.0) * (gb + Lit<R>::w(i));
+            fx -= (double)(cx(i) * q); fy -= (double)(cy(i) * q); fz -= (double)(cz(i) * q);
+          }
+        } else {
+          g[i] = St::ld(src + (int64_t)i * N + s);
+        }
+      }
+      R delta, rho, ux, uy, uz, uu;
+      moments<R>(g, delta, rho, ux, uy, uz, uu);
+      R o[Q];
+      collide<R>(P, ct, x, z, g, delta, rho, ux, uy, uz, uu, o);
+#pragma unroll
+      for (int i = 0; i < Q; ++i) St::st(dst + (int64_t)i * N + cell, o[i]);
+      if (MAC) d.macros[cell] = make_float4((float)ux, (float)uy, (float)uz, (float)delta);
+    }
+  }
+  if (FRC) {
+    const bool any = __any_sync(0xffffffffu, fx != 0.0 || fy != 0.0 || fz != 0.0);
+    if (any) warp_add3(fx, fy, fz, d.force);
+  }
+}
+
+// ------------------------------------------------------------------ init
+// shaderInit (src/core/emit/wgsl.js:269-302): free-stream equilibrium in every
+// cell; SOLIDO at rest, SOLIDO_MOVEL at the belt velocity.  Writes the
+// parity-0 in-place layout, or the natural layout of `pop` for ping-pong.
+template <class St, bool INPLACE>
+__global__ void k_init(Dev d, Params P) {
+  using R = typename St::real;
+  using S = typename St::store_t;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  if (x >= d.nx || y >= d.ny) return;
+  const int64_t N = d.N;
+  const int64_t cell = ((int64_t)z * d.ny + y) * d.nx + x;
+  const uint32_t ct = d.tipo[cell];
+  R ux = R(P.inlet[0]), uy = R(P.inlet[1]), uz = R(P.inlet[2]);
+  if (ct == SOLIDO) { ux = R(0.0); uy = R(0.0); uz = R(0.0); }
+  if (ct == SOLIDO_MOVEL) { ux = R(P.belt[0]); uy = R(P.belt[1]); uz = R(P.belt[2]); }
+  const R delta = R(0.0), rho = R(1.0);
+  const R uu = ux * ux + uy * uy + uz * uz;
+  S* F = static_cast<S*>(d.pop);
+  const Wrap w = wrap3(x, y, z, d.nx, d.ny, d.nz);
+#pragma unroll
+  for (int k = 0; k < Q; ++k) {
+    const R e = equilibrium<R>(k, delta, rho, ux, uy, uz, uu);
+    const int64_t off = INPLACE ? eso_loc(k, 0, cell, x, y, z, w, d.nx, d.ny, N) : (int64_t)k * N + cell;
+    St::st(F + off, e);
+  }
+}
+
+// ------------------------------------------------- state upload/download
+// One direction k of a natural-layout array <-> storage.
+template <class St, bool INPLACE>
+__global__ void k_put_dir(Dev d, const double* __restrict__ v, int k, int parity) {
+  using S = typename St::store_t;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  if (x >= d.nx || y >= d.ny) return;
+  const int64_t cell = ((int64_t)z * d.ny + y) * d.nx + x;
+  const Wrap w = wrap3(x, y, z, d.nx, d.ny, d.nz);
+  const int64_t off = INPLACE ? eso_loc(k, parity, cell, x, y, z, w, d.nx, d.ny, d.N) : (int64_t)k * d.N + cell;
+  St::st(static_cast<S*>(d.pop) + off, St::from_double(v[cell]));
+}
+
+template <class St, bool INPLACE>
+__global__ void k_get_dir(Dev d, double* __restrict__ v, int k, int parity) {
+  using S = typename St::store_t;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  if (x >= d.nx || y >= d.ny) return;
+  const int64_t cell = ((int64_t)z * d.ny + y) * d.nx + x;
+  const Wrap w = wrap3(x, y, z, d.nx, d.ny, d.nz);
+  const int64_t off = INPLACE ? eso_loc(k, parity, cell, x, y, z, w, d.nx, d.ny, d.N) : (int64_t)k * d.N + cell;
+  v[cell] = (double)St::ld(static_cast<const S*>(d.pop) + off);
+}
+
+// Gather the 19 post-collision populations of one cell from the current state.
+template <class St, bool INPLACE>
+__device__ __forceinline__ void gather_state(const Dev& d, int parity, int64_t cell, int x, int y, int z,
+                                             typename St::real* g) {
+  using S = typename St::store_t;
+  const S* F = static_cast<const S*>(d.pop);
+  const Wrap w = wrap3(x, y, z, d.nx, d.ny, d.nz);
+#pragma unroll
+  for (int k = 0; k < Q; ++k) {
+    const int64_t off = INPLACE ? eso_loc(k, parity, cell, x, y, z, w, d.nx, d.ny, d.N) : (int64_t)k * d.N + cell;
+    g[k] = St::ld(F + off);
+  }
+}
+
+// shaderMacros (src/core/emit/wgsl.js:442-476): moments of the stored state,
+// no streaming.  Solid cells report zero.
+template <class St, bool INPLACE>
+__global__ void k_macros(Dev d, int parity) {
+  using R = typename St::real;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  if (x >= d.nx || y >= d.ny) return;
+  const int64_t cell = ((int64_t)z * d.ny + y) * d.nx + x;
+  if (is_solid(d.tipo[cell])) { d.macros[cell] = make_float4(0.f, 0.f, 0.f, 0.f); return; }
+  R g[Q];
+  gather_state<St, INPLACE>(d, parity, cell, x, y, z, g);
+  R delta = g[0];
+#pragma unroll
+  for (int i = 1; i < Q; ++i) delta = delta + g[i];
+  const R rho = R(1.0) + delta;
+  const R mx = signed_sum<R>(g, [](int i) { return cx(i); });
+  const R my = signed_sum<R>(g, [](int i) { return cy(i); });
+  const R mz = signed_sum<R>(g, [](int i) { return cz(i); });
+  d.macros[cell] = make_float4((float)(mx / rho), (float)(my / rho), (float)(mz / rho), (float)delta);
+}
+
+// Block sum of three doubles into out[3*blockLinear + c] (deterministic order).
+__device__ __forceinline__ void block_partials3(double a, double b, double c, double* out) {
+  __shared__ double sh[3][32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_down_sync(0xffffffffu, a, o);
+    b += __shfl_down_sync(0xffffffffu, b, o);
+    c += __shfl_down_sync(0xffffffffu, c, o);
+  }
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  const int nw = (blockDim.x * blockDim.y + 31) >> 5;
+  if ((tid & 31) == 0) { sh[0][tid >> 5] = a; sh[1][tid >> 5] = b; sh[2][tid >> 5] = c; }
+  __syncthreads();
+  if (tid == 0) {
+    double s0 = 0, s1 = 0, s2 = 0;
+    for (int k = 0; k < nw; ++k) { s0 += sh[0][k]; s1 += sh[1][k]; s2 += sh[2][k]; }
+    const int64_t b_lin = blockIdx.x + (int64_t)gridDim.x * (blockIdx.y + (int64_t)gridDim.y * blockIdx.z);
+    out[3 * b_lin + 0] = s0;
+    out[3 * b_lin + 1] = s1;
+    out[3 * b_lin + 2] = s2;
+  }
+}
+
+// Momentum exchange of the current state (src/core/emit/wgsl.js:356-379):
+// FLUIDO cells, links whose downstream neighbour is SOLIDO, per-link value
+// 2 (g_i + w_i) in the storage's arithmetic, fp64 accumulation.
+template <class St, bool INPLACE>
+__global__ void k_forces(Dev d, int parity, double* partials) {
+  using R = typename St::real;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  double fx = 0, fy = 0, fz = 0;
+  if (x < d.nx && y < d.ny) {
+    const int64_t cell = ((int64_t)z * d.ny + y) * d.nx + x;
+    if (d.tipo[cell] == FLUIDO) {
+      using S = typename St::store_t;
+      const S* F = static_cast<const S*>(d.pop);
+      const Wrap w = wrap3(x, y, z, d.nx, d.ny, d.nz);
+#pragma unroll
+      for (int i = 1; i < Q; ++i) {
+        if (d.tipo[nbr(i, +1, x, y, z, w, d.nx, d.ny)] != SOLIDO) continue;
+        const int64_t off = INPLACE ? eso_loc(i, parity, cell, x, y, z, w, d.nx, d.ny, d.N) : (int64_t)i * d.N + cell;
+        const R q = R(2.0) * (St::ld(F + off) + Lit<R>::w(i));
+        fx += (double)(cx(i) * q); fy += (double)(cy(i) * q); fz += (double)(cz(i) * q);
+      }
+    }
+  }
+  block_partials3(fx, fy, fz, partials);
+}
+
+// Sum of delta over non-solid cells (delta summed in storage arithmetic in
+// index order, as shaderMacros does; fp64 across cells).
+template <class St, bool INPLACE>
+__global__ void k_mass(Dev d, int parity, double* partials) {
+  using R = typename St::real;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  double m = 0;
+  if (x < d.nx && y < d.ny) {
+    const int64_t cell = ((int64_t)z * d.ny + y) * d.nx + x;
+    if (!is_solid(d.tipo[cell])) {
+      R g[Q];
+      gather_state<St, INPLACE>(d, parity, cell, x, y, z, g);
+      R delta = g[0];
+#pragma unroll
+      for (int i = 1; i < Q; ++i) delta = delta + g[i];
+      m = (double)delta;
+    }
+  }
+  block_partials3(m, 0.0, 0.0, partials);
+}
+
+// ---------------------------------------------------------------- launchers
+struct Launch {
+  dim3 grid, block;
+};
+
+struct Ops {
+  cudaError_t (*step)(const Dev&, const Params&, int parity, bool inplace, bool mac, bool frc, Launch, cudaStream_t);
+  cudaError_t (*init)(const Dev&, const Params&, bool inplace, Launch, cudaStream_t);
+  cudaError_t (*put_dir)(const Dev&, const double*, int k, int parity, bool inplace, Launch, cudaStream_t);
+  cudaError_t (*get_dir)(const Dev&, double*, int k, int parity, bool inplace, Launch, cudaStream_t);
+  cudaError_t (*macros)(const Dev&, int parity, bool inplace, Launch, cudaStream_t);
+  cudaError_t (*forces)(const Dev&, int parity, bool inplace, double* partials, Launch, cudaStream_t);
+  cudaError_t (*mass)(const Dev&, int parity, bool inplace, double* partials, Launch, cudaStream_t);
+  int elem_bytes;
+};
+
+template <class St>
+struct OpsImpl {
+  template <int PAR, bool MAC, bool FRC>
+  static void go_inplace(const Dev& d, const Params& P, Launch L, cudaStream_t s) {
+    k_step_inplace<St, PAR, MAC, FRC><<<L.grid, L.block, 0, s>>>(d, P);
+  }
+  static cudaError_t step(const Dev& d, const Params& P, int parity, bool inplace, bool mac, bool frc, Launch L,
+                          cudaStream_t s) {
+    if (inplace) {
+      if (parity == 0) {
+        if (mac) { frc ? go_inplace<0, true, true>(d, P, L, s) : go_inplace<0, true, false>(d, P, L, s); }
+        else { frc ? go_inplace<0, false, true>(d, P, L, s) : go_inplace<0, false, false>(d, P, L, s); }
+      } else {
+        if (mac) { frc ? go_inplace<1, true, true>(d, P, L, s) : go_inplace<1, true, false>(d, P, L, s); }
+        else { frc ? go_inplace<1, false, true>(d, P, L, s) : go_inplace<1, false, false>(d, P, L, s); }
+      }
+    } else {
+      if (mac) { if (frc) k_step_ab<St, true, true><<<L.grid, L.block, 0, s>>>(d, P); else k_step_ab<St, true, false><<<L.grid, L.block, 0, s>>>(d, P); }
+      else { if (frc) k_step_ab<St, false, true><<<L.grid, L.block, 0, s>>>(d, P); else k_step_ab<St, false, false><<<L.grid, L.block, 0, s>>>(d, P); }
+    }
+    return cudaGetLastError();
+  }
+  static cudaError_t init(const Dev& d, const Params& P, bool inplace, Launch L, cudaStream_t s) {
+    if (inplace) k_init<St, true><<<L.grid, L.block, 0, s>>>(d, P);
+    else k_init<St, false><<<L.grid, L.block, 0, s>>>(d, P);
+    return cudaGetLastError();
+  }
+  static cudaError_t put_dir(const Dev& d, const double* v, int k, int parity, bool inplace, Launch L, cudaStream_t s) {
+    if (inplace) k_put_dir<St, true><<<L.grid, L.block, 0, s>>>(d, v, k, parity);
+    else k_put_dir<St, false><<<L.grid, L.block, 0, s>>>(d, v, k, parity);
+    return cudaGetLastError();
+  }
+  static cudaError_t get_dir(const Dev& d, double* v, int k, int parity, bool inplace, Launch L, cudaStream_t s) {
+    if (inplace) k_get_dir<St, true><<<L.grid, L.block, 0, s>>>(d, v, k, parity);
+    else k_get_dir<St, false><<<L.grid, L.block, 0, s>>>(d, v, k, parity);
+    return cudaGetLastError();
+  }
+  static cudaError_t macros(const Dev& d, int parity, bool inplace, Launch L, cudaStream_t s) {
+    if (inplace) k_macros<St, true><<<L.grid, L.block, 0, s>>>(d, parity);
+    else k_macros<St, false><<<L.grid, L.block, 0, s>>>(d, parity);
+    return cudaGetLastError();
+  }
+  static cudaError_t forces(const Dev& d, int parity, bool inplace, double* part, Launch L, cudaStream_t s) {
+    if (inplace) k_forces<St, true><<<L.grid, L.block, 0, s>>>(d, parity, part);
+    else k_forces<St, false><<<L.grid, L.block, 0, s>>>(d, parity, part);
+    return cudaGetLastError();
+  }
+  static cudaError_t mass(const Dev& d, int parity, bool inplace, double* part, Launch L, cudaStream_t s) {
+    if (inplace) k_mass<St, true><<<L.grid, L.block, 0, s>>>(d, parity, part);
+    else k_mass<St, false><<<L.grid, L.block, 0, s>>>(d, parity, part);
+    return cudaGetLastError();
+  }
+  static Ops make() {
+    Ops o;
+    o.step = &step; o.init = &init; o.put_dir = &put_dir; o.get_dir = &get_dir;
+    o.macros = &macros; o.forces = &forces; o.mass = &mass;
+    o.elem_bytes = (int)sizeof(typename St::store_t);
+    return o;
+  }
+};
+
+Ops ops_f32();
+Ops ops_f64();
+Ops ops_f16s();
+Ops ops_bf16s();
+
+}  // namespace lbm

@@ -1,0 +1,182 @@
+/*
+ * lbm.h — C ABI of the GB300 (sm_103a) D3Q19 wind-tunnel solver.
+ *
+ * This is the drop-in boundary: every entry point replaces one member of the
+ * solver class API that the reference's two browser backends share
+ * (src/backend/webgpu/solver.js:36-528, src/backend/webgl2/solver.js:46-573;
+ * the webgl2 file states the API is the same, src/backend/webgl2/solver.js:7-10).
+ * A JavaScript host binds it through an N-API addon; the Python host in
+ * cfd__gb300/solver.py binds it through ctypes.  Plain pointers and sizes only.
+ *
+ * Conventions
+ *   - every call returns int: 0 = LBM_OK, < 0 = an LBM_E* code;
+ *     lbm_last_error() returns the calling thread's last message;
+ *   - a context owns all device memory it allocates; the caller owns host
+ *     buffers passed in;
+ *   - one CUDA stream per context (the legacy default stream unless the caller
+ *     hands one in with lbm_set_stream); enqueue calls are asynchronous,
+ *     lbm_read_*, lbm_get_*, lbm_forces, lbm_mass and lbm_sync synchronise;
+ *   - calls on one context are not thread-safe;
+ *   - no call traps or hangs the GPU: device-side loops are bounded and report
+ *     LBM_ETIMEDOUT.
+ *
+ * Data contract (identical to the reference)
+ *   - population index order, velocities and weights: src/core/lattice.js:57-89
+ *     (opposite pairs adjacent: (0),(1,2),...,(17,18));
+ *   - stored value is the shifted population g_i = f_i - w_i
+ *     (src/core/lattice.js:6-46); rest state = all zeros;
+ *   - linear cell index cell = (z*ny + y)*nx + x (src/core/emit/wgsl.js:15);
+ *   - population arrays crossing this ABI are direction-major SoA,
+ *     g[i*N + cell] (src/core/emit/wgsl.js:13-26), holding the post-collision
+ *     state the next step streams from;
+ *   - cell classes are the CELULA codes (src/core/emit/ir.js:71-80).
+ */
+#ifndef CFD_GB300_LBM_H
+#define CFD_GB300_LBM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LBM_Q 19
+
+/* status codes */
+#define LBM_OK          0
+#define LBM_EINVAL     (-1)   /* bad argument, size mismatch, null handle */
+#define LBM_ENOMEM     (-2)   /* device allocation refused (message gives GB) */
+#define LBM_ECUDA      (-3)   /* CUDA runtime error (message gives the call) */
+#define LBM_ETIMEDOUT  (-4)   /* a bounded device or host loop gave up */
+#define LBM_ESTATE     (-5)   /* call out of order (e.g. step before set_types) */
+#define LBM_ENOTSUP    (-6)   /* feature not available for this storage/layout */
+
+/* cell classes, src/core/emit/ir.js:71-80 */
+#define LBM_FLUIDO        0
+#define LBM_SOLIDO        1
+#define LBM_ENTRADA       2
+#define LBM_SAIDA         3
+#define LBM_SOLIDO_MOVEL  4
+#define LBM_ESPELHO_Y     5
+#define LBM_ESPELHO_Z     6
+#define LBM_PAREDE        7
+
+/* population storage forms */
+#define LBM_F32    0   /* fp32 g_i (152 B/cell/step) */
+#define LBM_F16S   1   /* fp16 of g_i * 2^10, fp32 arithmetic (76 B/cell/step) */
+#define LBM_BF16S  2   /* bf16 of g_i, fp32 arithmetic (76 B/cell/step) */
+#define LBM_F64    3   /* fp64 g_i and fp64 arithmetic: the accuracy judge */
+
+/* lbm_create flags */
+#define LBM_FLAG_WRITE_MACROS  1  /* the last step of each lbm_step writes (u, delta) */
+#define LBM_FLAG_PINGPONG      2  /* two population sets, natural layout, the
+                                     reference's A/B pull exactly
+                                     (src/backend/webgpu/solver.js:10-24);
+                                     default is one in-place set (esoteric pull) */
+
+typedef struct lbm_ctx lbm_ctx;
+
+typedef struct { int32_t nx, ny, nz; } lbm_dims;
+
+/* Fields of the 80-byte Params uniform (src/core/emit/wgsl.js:123-135) as the
+ * reference packs them (src/backend/webgpu/solver.js:285-291).  All fp32, as
+ * the uniform is.  `closure` selects the eddy-viscosity model: 0 = Smagorinsky
+ * (src/core/emit/ir.js:262-301), 1 = the learned MLP set by lbm_set_closure. */
+typedef struct {
+  float omega_plus;      /* P.omegaPlus */
+  float magic;           /* P.magic (TRT Lambda), default 3/16 */
+  float les_cs;          /* P.lesCs, 0 disables LES exactly */
+  float belt_u[3];       /* P.beltU.xyz */
+  float inlet_u[3];      /* P.inletU.xyz */
+  float sponge_start;    /* P.sponge.x */
+  float sponge_len;      /* P.sponge.y */
+  float bl_thickness;    /* P.sponge.z (espessuraCL) */
+  int32_t closure;       /* 0 Smagorinsky, 1 learned closure */
+} lbm_params;
+
+typedef struct {
+  int64_t n_cells;
+  int64_t device_bytes;    /* everything this context allocated */
+  int32_t storage;         /* LBM_F32 ... */
+  int32_t flags;
+  int64_t steps;           /* steps done since init / set_populations */
+  int32_t parity;          /* steps & 1 — the in-place layout's phase */
+  int32_t block_x;         /* chosen launch shape of the step kernel */
+} lbm_info;
+
+/* SolverWebGPU.criar (src/backend/webgpu/solver.js:93-124): allocates; fails
+ * with LBM_ENOMEM and a size message (GB) when the device refuses. */
+int lbm_create(const lbm_dims* dims, int storage, int flags, lbm_ctx** out);
+
+/* SolverWebGPU.destruir (src/backend/webgpu/solver.js:523-527). */
+int lbm_destroy(lbm_ctx* ctx);
+
+/* Optional: run this context's work on the caller's cudaStream_t. */
+int lbm_set_stream(lbm_ctx* ctx, void* cuda_stream);
+
+/* SolverWebGPU.configurar (src/backend/webgpu/solver.js:277-293). */
+int lbm_configure(lbm_ctx* ctx, const lbm_params* p);
+
+/* SolverWebGPU.definirTipos (src/backend/webgpu/solver.js:296-301): LBM_EINVAL
+ * when n != N or a code is > 7. */
+int lbm_set_types(lbm_ctx* ctx, const uint32_t* tipo, size_t n);
+
+/* SolverWebGPU.inicializar (src/backend/webgpu/solver.js:338-349) with the
+ * init kernel shaderInit (src/core/emit/wgsl.js:269-302); resets steps to 0. */
+int lbm_init_equilibrium(lbm_ctx* ctx);
+
+/* SolverWebGPU.definirCampo upload half (src/backend/webgpu/solver.js:363-389):
+ * g is 19*N doubles, SoA, rounded to the storage type on upload.  Resets steps. */
+int lbm_set_populations(lbm_ctx* ctx, const double* g, size_t n);
+
+/* Reads the current state back as 19*N doubles, SoA, natural layout.  No
+ * counterpart in the reference (it never reads populations back); needed for
+ * state parity and checkpointing. */
+int lbm_get_populations(lbm_ctx* ctx, double* g, size_t n);
+
+/* SolverWebGPU.passo (src/backend/webgpu/solver.js:395-415): n steps enqueued
+ * back to back, no sync.  With LBM_FLAG_WRITE_MACROS the last step writes the
+ * pulled (pre-collision) macros (src/core/emit/wgsl.js:244-256). */
+int lbm_step(lbm_ctx* ctx, int n);
+
+/* n steps that also record, for every step, the momentum-exchange force of the
+ * state the step streams from (the value medirForcas would return just before
+ * that step, without the rest offset) as 3 doubles per step into out_f
+ * (3*n doubles, host).  One device->host copy at the end. */
+int lbm_step_forces(lbm_ctx* ctx, int n, double* out_f);
+
+/* SolverWebGPU.atualizarMacros (src/backend/webgpu/solver.js:511-520) with
+ * shaderMacros (src/core/emit/wgsl.js:442-476); solid cells report 0. */
+int lbm_update_macros(lbm_ctx* ctx);
+
+/* SolverWebGPU.lerMacros (src/backend/webgpu/solver.js:427-442): out is 4*N
+ * floats (ux, uy, uz, delta) per cell. */
+int lbm_read_macros(lbm_ctx* ctx, float* out, size_t n);
+
+/* SolverWebGPU.medirForcas device half (src/backend/webgpu/solver.js:486-508,
+ * kernels src/core/emit/wgsl.js:332-435): raw momentum-exchange force on the
+ * SOLIDO cells, fp64 accumulation.  The caller subtracts the rest offset
+ * (calibrarRepouso, src/backend/webgpu/solver.js:480-484). */
+int lbm_forces(lbm_ctx* ctx, double f[3]);
+
+/* Sum of delta over all non-solid cells of the current state, fp64.  The
+ * reference computes it on the host from lerMacros (tests/nucleo.html:209-216). */
+int lbm_mass(lbm_ctx* ctx, double* sum_delta);
+
+/* Wait for all work on the context's stream. */
+int lbm_sync(lbm_ctx* ctx);
+
+int lbm_get_info(lbm_ctx* ctx, lbm_info* info);
+
+/* Thread-local message of the last failing call ("" if none). */
+const char* lbm_last_error(void);
+
+/* Launch-shape override of the step kernel (threads along x per block; 0 =
+ * autotuned).  Used by the autotuner and the benchmark sweep. */
+int lbm_set_block(lbm_ctx* ctx, int block_x);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CFD_GB300_LBM_H */

@@ -1,0 +1,412 @@
+/*
+ * lbm_oracle_impl.h — CPU restatement of the reference's D3Q19 step, init,
+ * macros and momentum-exchange kernels.  TEST INFRASTRUCTURE ONLY: included
+ * twice by lbm_oracle.c (REAL = float, REAL = double).  Nothing in the
+ * product links this.
+ *
+ * Every expression keeps the operand order of the generated shader, so that a
+ * build with -ffp-contract=off evaluates each fp32 operation exactly as
+ * written:
+ *   step body       src/core/emit/ir.js:493-533 (blocks :166-478)
+ *   kernel header   src/core/emit/wgsl.js:184-222 (wrap :159-182)
+ *   macros write    src/core/emit/wgsl.js:244-256
+ *   init            src/core/emit/wgsl.js:269-302
+ *   forces          src/core/emit/wgsl.js:332-396, reduce :407-435
+ *   macros kernel   src/core/emit/wgsl.js:442-476
+ *
+ * Required macros: REAL, SFX (function suffix), the constant tables
+ * W_SFX / SIXW_SFX (weights and 6 w_i as the shader literals), LIT(x).
+ */
+
+#define CAT2(a, b) a##b
+#define CAT(a, b) CAT2(a, b)
+#define FN(name) CAT(name, SFX)
+
+/* Quantisation of stored populations (16-bit forms); identity for plain. */
+static inline REAL FN(orc_q)(REAL v, int storage) {
+#if ORC_IS_FLOAT
+  if (storage == ORC_F16S) return orc_f16_to_f32(orc_f32_to_f16(v * 1024.0f)) * (1.0f / 1024.0f);
+  if (storage == ORC_BF16S) return orc_bf16_to_f32(orc_f32_to_bf16(v));
+#else
+  (void)storage;
+#endif
+  return v;
+}
+
+/* c_i . v in the order dotC (src/core/emit/ir.js:116-126) emits it. */
+static inline REAL FN(orc_dotc)(int i, REAL vx, REAL vy, REAL vz) {
+  const REAL v[3] = {vx, vy, vz};
+  int first = 1;
+  REAL acc = LIT(0.0);
+  ORC_UNROLL
+  for (int a = 0; a < 3; ++a) {
+    const int c = ORC_C[i][a];
+    if (c == 0) continue;
+    if (first) { acc = c > 0 ? v[a] : -v[a]; first = 0; }
+    else acc = c > 0 ? acc + v[a] : acc - v[a];
+  }
+  return acc;   /* 0.0 literal when c_i = 0 */
+}
+
+/* w_i (delta + rho (3 cu + 4.5 cu^2 - 1.5 uu)) ; e0 = w0 (delta - 1.5 rho uu)
+ * src/core/emit/ir.js:216-232 */
+static inline void FN(orc_equilibrium)(REAL delta, REAL rho, REAL ux, REAL uy, REAL uz,
+                                       REAL uu, REAL* e) {
+  e[0] = FN(W_)[0] * (delta - LIT(1.5) * rho * uu);
+  ORC_UNROLL
+  for (int i = 1; i < ORC_Q; ++i) {
+    const REAL cu = FN(orc_dotc)(i, ux, uy, uz);
+    e[i] = FN(W_)[i] * (delta + rho * (LIT(3.0) * cu + LIT(4.5) * cu * cu - LIT(1.5) * uu));
+  }
+}
+
+
+/*
+ * One reference step over every cell, A/B ping-pong, natural SoA layout.
+ * src -> dst; macros (4 per cell) written when non-null.  Solid cells leave
+ * dst untouched (src/core/emit/wgsl.js:201-204).
+ */
+void FN(orc_step)(const orc_params* P, int nx, int ny, int nz, const uint32_t* tipo,
+                  const REAL* src, REAL* dst, float* macros, int storage, int nthreads) {
+  const int64_t N = (int64_t)nx * ny * nz;
+  const REAL omegaPlus = (REAL)P->omega_plus, magic = (REAL)P->magic, lesCs = (REAL)P->les_cs;
+  const REAL spStart = (REAL)P->sponge_start, spLen = (REAL)P->sponge_len;
+  const REAL bl = (REAL)P->bl_thickness;
+  const REAL inx = (REAL)P->inlet_u[0], iny = (REAL)P->inlet_u[1], inz = (REAL)P->inlet_u[2];
+  const REAL bx = (REAL)P->belt_u[0], by = (REAL)P->belt_u[1], bz = (REAL)P->belt_u[2];
+  (void)nthreads;
+#if defined(_OPENMP)
+#pragma omp parallel for schedule(static) num_threads(nthreads > 0 ? nthreads : 1)
+#endif
+  for (int z = 0; z < nz; ++z) {
+    for (int y = 0; y < ny; ++y) {
+      for (int x = 0; x < nx; ++x) {
+        const int64_t cell = ((int64_t)z * ny + y) * nx + x;
+        const uint32_t ct = tipo[cell];
+        if (orc_is_solid(ct)) {
+          if (macros) { macros[4 * cell] = 0; macros[4 * cell + 1] = 0; macros[4 * cell + 2] = 0; macros[4 * cell + 3] = 0; }
+          continue;
+        }
+        /* periodic neighbour coordinates (src/core/emit/wgsl.js:176-180) */
+        const int xs[3] = {x == 0 ? nx - 1 : x - 1, x, x == nx - 1 ? 0 : x + 1};
+        const int ys[3] = {y == 0 ? ny - 1 : y - 1, y, y == ny - 1 ? 0 : y + 1};
+        const int zs[3] = {z == 0 ? nz - 1 : z - 1, z, z == nz - 1 ? 0 : z + 1};
+
+        /* inlet boundary-layer factor (src/core/emit/wgsl.js:217-220) */
+        const REAL uInletBL = bl > LIT(1.0) ? bl : LIT(1.0);
+        const REAL zc = (REAL)z + LIT(0.5);
+        const REAL blf = zc < bl ? ORC_POW(zc / uInletBL, LIT(0.1428571429)) : LIT(1.0);
+        const REAL uex = inx * blf, uey = iny * blf, uez = inz * blf;
+
+        /* blocoPull (src/core/emit/ir.js:166-189) */
+        REAL g[ORC_Q];
+        g[0] = src[cell];
+        ORC_UNROLL
+        for (int i = 1; i < ORC_Q; ++i) {
+          const int sx = xs[1 - ORC_C[i][0]], sy = ys[1 - ORC_C[i][1]], sz = zs[1 - ORC_C[i][2]];
+          const int64_t s = ((int64_t)sz * ny + sy) * nx + sx;
+          const uint32_t t = tipo[s];
+          if (orc_is_solid(t)) {
+            const REAL wx = t == ORC_SOLIDO_MOVEL ? bx : LIT(0.0);
+            const REAL wy = t == ORC_SOLIDO_MOVEL ? by : LIT(0.0);
+            const REAL wz = t == ORC_SOLIDO_MOVEL ? bz : LIT(0.0);
+            g[i] = src[(int64_t)ORC_OPP[i] * N + cell] + FN(SIXW_)[i] * (FN(orc_dotc)(i, wx, wy, wz));
+          } else {
+            g[i] = src[(int64_t)i * N + s];
+          }
+        }
+
+        /* blocoMomentos (src/core/emit/ir.js:192-213) */
+        REAL delta = g[0];
+        ORC_UNROLL
+        for (int i = 1; i < ORC_Q; ++i) delta = delta + g[i];
+        const REAL rho = LIT(1.0) + delta;
+        REAL m[3];
+        ORC_UNROLL
+        for (int a = 0; a < 3; ++a) {
+          int first = 1;
+          REAL acc = LIT(0.0);
+          ORC_UNROLL
+          for (int i = 0; i < ORC_Q; ++i) {
+            const int c = ORC_C[i][a];
+            if (c == 0) continue;
+            if (first) { acc = c > 0 ? g[i] : -g[i]; first = 0; }
+            else acc = c > 0 ? acc + g[i] : acc - g[i];
+          }
+          m[a] = acc;
+        }
+        const REAL ux = m[0] / rho, uy = m[1] / rho, uz = m[2] / rho;
+        const REAL uu = ux * ux + uy * uy + uz * uz;
+
+        REAL* out[ORC_Q];
+        ORC_UNROLL
+        for (int i = 0; i < ORC_Q; ++i) out[i] = dst + (int64_t)i * N + cell;
+
+        if (ct == ORC_ESPELHO_Y || ct == ORC_ESPELHO_Z) {
+          /* blocoEspelho (src/core/emit/ir.js:383-390) */
+          const int ax = ct == ORC_ESPELHO_Y ? 1 : 2;
+          ORC_UNROLL
+          for (int i = 0; i < ORC_Q; ++i) *out[i] = FN(orc_q)(g[ORC_MIRROR[ax][i]], storage);
+        } else if (ct == ORC_ENTRADA) {
+          /* blocoEntrada (src/core/emit/ir.js:405-422) */
+          const REAL deltaIn = LIT(0.0), rhoIn = LIT(1.0);
+          const REAL uuIn = uex * uex + uey * uey + uez * uez;
+          *out[0] = FN(orc_q)(FN(W_)[0] * (deltaIn - LIT(1.5) * rhoIn * uuIn), storage);
+          ORC_UNROLL
+          for (int i = 1; i < ORC_Q; ++i) {
+            const REAL ci = FN(orc_dotc)(i, uex, uey, uez);
+            *out[i] = FN(orc_q)(FN(W_)[i] * (deltaIn + rhoIn * (LIT(3.0) * ci + LIT(4.5) * ci * ci - LIT(1.5) * uuIn)), storage);
+          }
+        } else if (ct == ORC_SAIDA) {
+          /* blocoSaida with the pulled u (src/core/emit/ir.js:432-444, :512-515) */
+          *out[0] = FN(orc_q)(FN(W_)[0] * (LIT(-1.5) * uu), storage);
+          ORC_UNROLL
+          for (int i = 1; i < ORC_Q; ++i) {
+            const REAL cu = FN(orc_dotc)(i, ux, uy, uz);
+            *out[i] = FN(orc_q)(FN(W_)[i] * (LIT(3.0) * cu + LIT(4.5) * cu * cu - LIT(1.5) * uu), storage);
+          }
+        } else {
+          /* FLUIDO: blocoEquilibrio, blocoLES, blocoColisao, blocoEsponja */
+          REAL e[ORC_Q];
+          FN(orc_equilibrium)(delta, rho, ux, uy, uz, uu, e);
+          REAL n[ORC_Q];
+          ORC_UNROLL
+          for (int i = 0; i < ORC_Q; ++i) n[i] = g[i] - e[i];
+          /* Pi_ab = sum c_ia c_ib n_i, terms in index order (src/core/emit/ir.js:269-282) */
+          static const int PA[6] = {0, 1, 2, 0, 0, 1}, PB[6] = {0, 1, 2, 1, 2, 2};
+          REAL pi[6];
+          ORC_UNROLL
+          for (int k = 0; k < 6; ++k) {
+            int first = 1;
+            REAL acc = LIT(0.0);
+            ORC_UNROLL
+            for (int i = 0; i < ORC_Q; ++i) {
+              const int coef = ORC_C[i][PA[k]] * ORC_C[i][PB[k]];
+              if (coef == 0) continue;
+              if (first) { acc = coef > 0 ? n[i] : -n[i]; first = 0; }
+              else acc = coef > 0 ? acc + n[i] : acc - n[i];
+            }
+            pi[k] = acc;
+          }
+          const REAL pp = pi[0] * pi[0] + pi[1] * pi[1] + pi[2] * pi[2] +
+                          LIT(2.0) * (pi[3] * pi[3] + pi[4] * pi[4] + pi[5] * pi[5]);
+          const REAL qs = ORC_SQRT(LIT(2.0) * pp);
+          const REAL tau0 = LIT(1.0) / omegaPlus;
+          const REAL tauT = LIT(0.5) * (tau0 + ORC_SQRT(tau0 * tau0 + LIT(18.0) * lesCs * lesCs * qs / rho));
+          const REAL omegaP = LIT(1.0) / tauT;
+          const REAL omegaM = LIT(1.0) / (magic / (LIT(1.0) / omegaP - LIT(0.5)) + LIT(0.5));
+
+          /* blocoColisao (src/core/emit/ir.js:304-323) */
+          REAL o[ORC_Q];
+          o[0] = g[0] - omegaP * (g[0] - e[0]);
+          ORC_UNROLL
+          for (int i = 1; i < ORC_Q; i += 2) {
+            const int j = i + 1;
+            const REAL p = LIT(0.5) * ((g[i] + g[j]) - (e[i] + e[j]));
+            const REAL mm = LIT(0.5) * ((g[i] - g[j]) - (e[i] - e[j]));
+            o[i] = g[i] - omegaP * p - omegaM * mm;
+            o[j] = g[j] - omegaP * p + omegaM * mm;
+          }
+
+          /* blocoEsponja (src/core/emit/ir.js:458-478); mix(a,b,t) = a(1-t) + bt */
+          const REAL sxs = ((REAL)x - spStart) / (spLen > LIT(1.0) ? spLen : LIT(1.0));
+          REAL sigma = sxs > LIT(0.0) ? sxs : LIT(0.0);
+          sigma = sigma < LIT(1.0) ? sigma : LIT(1.0);
+          const REAL sig2 = sigma * sigma;
+          const REAL uuInf = inx * inx + iny * iny + inz * inz;
+          {
+            const REAL t0 = FN(W_)[0] * (LIT(-1.5) * uuInf);
+            o[0] = o[0] * (LIT(1.0) - sig2) + t0 * sig2;
+          }
+          ORC_UNROLL
+          for (int i = 1; i < ORC_Q; ++i) {
+            const REAL si = FN(orc_dotc)(i, inx, iny, inz);
+            const REAL ti = FN(W_)[i] * (LIT(3.0) * si + LIT(4.5) * si * si - LIT(1.5) * uuInf);
+            o[i] = o[i] * (LIT(1.0) - sig2) + ti * sig2;
+          }
+          ORC_UNROLL
+          for (int i = 0; i < ORC_Q; ++i) *out[i] = FN(orc_q)(o[i], storage);
+        }
+        if (macros) {
+          macros[4 * cell] = (float)ux; macros[4 * cell + 1] = (float)uy;
+          macros[4 * cell + 2] = (float)uz; macros[4 * cell + 3] = (float)delta;
+        }
+      }
+    }
+  }
+}
+
+/* shaderInit (src/core/emit/wgsl.js:269-302): every cell, including solids. */
+void FN(orc_init)(const orc_params* P, int nx, int ny, int nz, const uint32_t* tipo, REAL* dst,
+                  int storage) {
+  const int64_t N = (int64_t)nx * ny * nz;
+  for (int64_t cell = 0; cell < N; ++cell) {
+    const uint32_t ct = tipo[cell];
+    REAL ux = (REAL)P->inlet_u[0], uy = (REAL)P->inlet_u[1], uz = (REAL)P->inlet_u[2];
+    if (ct == ORC_SOLIDO) { ux = LIT(0.0); uy = LIT(0.0); uz = LIT(0.0); }
+    if (ct == ORC_SOLIDO_MOVEL) { ux = (REAL)P->belt_u[0]; uy = (REAL)P->belt_u[1]; uz = (REAL)P->belt_u[2]; }
+    const REAL delta = LIT(0.0), rho = LIT(1.0);
+    const REAL uu = ux * ux + uy * uy + uz * uz;
+    REAL e[ORC_Q];
+    FN(orc_equilibrium)(delta, rho, ux, uy, uz, uu, e);
+    ORC_UNROLL
+    for (int i = 0; i < ORC_Q; ++i) dst[(int64_t)i * N + cell] = FN(orc_q)(e[i], storage);
+  }
+}
+
+/* shaderMacros (src/core/emit/wgsl.js:442-476): moments of the stored state.
+ * zero_solids = 1 writes 0 for SOLIDO/SOLIDO_MOVEL/PAREDE cells. */
+void FN(orc_macros)(int nx, int ny, int nz, const uint32_t* tipo, const REAL* pop, float* macros,
+                    int zero_solids) {
+  const int64_t N = (int64_t)nx * ny * nz;
+  for (int64_t cell = 0; cell < N; ++cell) {
+    if (zero_solids && orc_is_solid(tipo[cell])) {
+      macros[4 * cell] = macros[4 * cell + 1] = macros[4 * cell + 2] = macros[4 * cell + 3] = 0;
+      continue;
+    }
+    REAL g[ORC_Q];
+    ORC_UNROLL
+    for (int i = 0; i < ORC_Q; ++i) g[i] = pop[(int64_t)i * N + cell];
+    REAL delta = g[0];
+    ORC_UNROLL
+    for (int i = 1; i < ORC_Q; ++i) delta = delta + g[i];
+    const REAL rho = LIT(1.0) + delta;
+    REAL m[3];
+    ORC_UNROLL
+    for (int a = 0; a < 3; ++a) {
+      int first = 1;
+      REAL acc = LIT(0.0);
+      ORC_UNROLL
+      for (int i = 0; i < ORC_Q; ++i) {
+        const int c = ORC_C[i][a];
+        if (c == 0) continue;
+        if (first) { acc = c > 0 ? g[i] : -g[i]; first = 0; }
+        else acc = c > 0 ? acc + g[i] : acc - g[i];
+      }
+      m[a] = acc;
+    }
+    macros[4 * cell] = (float)(m[0] / rho);
+    macros[4 * cell + 1] = (float)(m[1] / rho);
+    macros[4 * cell + 2] = (float)(m[2] / rho);
+    macros[4 * cell + 3] = (float)delta;
+  }
+}
+
+/* Per-link momentum exchange of one FLUIDO cell (src/core/emit/wgsl.js:356-379):
+ * q = 2 (g_i + w_i) in REAL, added component-wise as the shader's vec3. */
+static inline void FN(orc_cell_force)(int nx, int ny, int nz, const uint32_t* tipo, const REAL* pop,
+                                      int x, int y, int z, REAL f[3]) {
+  const int64_t N = (int64_t)nx * ny * nz;
+  const int64_t cell = ((int64_t)z * ny + y) * nx + x;
+  f[0] = f[1] = f[2] = LIT(0.0);
+  if (tipo[cell] != ORC_FLUIDO) return;
+  const int xs[3] = {x == 0 ? nx - 1 : x - 1, x, x == nx - 1 ? 0 : x + 1};
+  const int ys[3] = {y == 0 ? ny - 1 : y - 1, y, y == ny - 1 ? 0 : y + 1};
+  const int zs[3] = {z == 0 ? nz - 1 : z - 1, z, z == nz - 1 ? 0 : z + 1};
+  ORC_UNROLL
+  for (int i = 1; i < ORC_Q; ++i) {
+    const int64_t nb = ((int64_t)zs[1 + ORC_C[i][2]] * ny + ys[1 + ORC_C[i][1]]) * nx + xs[1 + ORC_C[i][0]];
+    if (tipo[nb] != ORC_SOLIDO) continue;
+    const REAL q = LIT(2.0) * (pop[(int64_t)i * N + cell] + FN(W_)[i]);
+    ORC_UNROLL
+    for (int a = 0; a < 3; ++a) {
+      const int c = ORC_C[i][a];
+      f[a] = f[a] + (c > 0 ? q : (c < 0 ? -q : LIT(0.0)));
+    }
+  }
+}
+
+/* Force, fp64 accumulation of the per-link REAL values (the GPU's method). */
+void FN(orc_forces_acc64)(int nx, int ny, int nz, const uint32_t* tipo, const REAL* pop, double out[3]) {
+  double s[3] = {0, 0, 0};
+  for (int z = 0; z < nz; ++z)
+    for (int y = 0; y < ny; ++y)
+      for (int x = 0; x < nx; ++x) {
+        const int64_t N = (int64_t)nx * ny * nz;
+        const int64_t cell = ((int64_t)z * ny + y) * nx + x;
+        if (tipo[cell] != ORC_FLUIDO) continue;
+        const int xs[3] = {x == 0 ? nx - 1 : x - 1, x, x == nx - 1 ? 0 : x + 1};
+        const int ys[3] = {y == 0 ? ny - 1 : y - 1, y, y == ny - 1 ? 0 : y + 1};
+        const int zs[3] = {z == 0 ? nz - 1 : z - 1, z, z == nz - 1 ? 0 : z + 1};
+        ORC_UNROLL
+        for (int i = 1; i < ORC_Q; ++i) {
+          const int64_t nb = ((int64_t)zs[1 + ORC_C[i][2]] * ny + ys[1 + ORC_C[i][1]]) * nx + xs[1 + ORC_C[i][0]];
+          if (tipo[nb] != ORC_SOLIDO) continue;
+          const REAL q = LIT(2.0) * (pop[(int64_t)i * N + cell] + FN(W_)[i]);
+          ORC_UNROLL
+          for (int a = 0; a < 3; ++a) s[a] += (double)ORC_C[i][a] * (double)q;
+        }
+      }
+  out[0] = s[0]; out[1] = s[1]; out[2] = s[2];
+}
+
+/* Force with the reference's own REAL reduction order: per-cell vec3 in
+ * direction order, a 64-lane tree per workgroup along x, then one 256-lane
+ * workgroup that strides the partials and trees them
+ * (src/core/emit/wgsl.js:384-393, :419-432). */
+void FN(orc_forces_faithful)(int nx, int ny, int nz, const uint32_t* tipo, const REAL* pop, REAL out[3]) {
+  const int gx = (nx + 63) / 64;
+  const int64_t nparts = (int64_t)gx * ny * nz;
+  REAL* parts = (REAL*)malloc(sizeof(REAL) * 3 * (size_t)nparts);
+  REAL sh[64][3];
+  for (int wz = 0; wz < nz; ++wz)
+    for (int wy = 0; wy < ny; ++wy)
+      for (int wx = 0; wx < gx; ++wx) {
+        for (int lid = 0; lid < 64; ++lid) {
+          const int x = wx * 64 + lid;
+          if (x < nx) FN(orc_cell_force)(nx, ny, nz, tipo, pop, x, wy, wz, sh[lid]);
+          else sh[lid][0] = sh[lid][1] = sh[lid][2] = LIT(0.0);
+        }
+        for (int s = 32; s > 0; s >>= 1)
+          for (int lid = 0; lid < s; ++lid)
+            ORC_UNROLL
+            for (int a = 0; a < 3; ++a) sh[lid][a] = sh[lid][a] + sh[lid + s][a];
+        const int64_t p = wx + (int64_t)gx * (wy + (int64_t)ny * wz);
+        ORC_UNROLL
+        for (int a = 0; a < 3; ++a) parts[3 * p + a] = sh[0][a];
+      }
+  REAL acc[256][3];
+  for (int lid = 0; lid < 256; ++lid) {
+    acc[lid][0] = acc[lid][1] = acc[lid][2] = LIT(0.0);
+    for (int64_t i = lid; i < nparts; i += 256)
+      ORC_UNROLL
+      for (int a = 0; a < 3; ++a) acc[lid][a] = acc[lid][a] + parts[3 * i + a];
+  }
+  for (int s = 128; s > 0; s >>= 1)
+    for (int lid = 0; lid < s; ++lid)
+      ORC_UNROLL
+      for (int a = 0; a < 3; ++a) acc[lid][a] = acc[lid][a] + acc[lid + s][a];
+  out[0] = acc[0][0]; out[1] = acc[0][1]; out[2] = acc[0][2];
+  free(parts);
+}
+
+/* Sum of delta over non-solid cells, fp64 accumulation. */
+double FN(orc_mass)(int nx, int ny, int nz, const uint32_t* tipo, const REAL* pop) {
+  const int64_t N = (int64_t)nx * ny * nz;
+  double s = 0.0;
+  for (int64_t cell = 0; cell < N; ++cell) {
+    if (orc_is_solid(tipo[cell])) continue;
+    REAL d = pop[cell];
+    ORC_UNROLL
+    for (int i = 1; i < ORC_Q; ++i) d = d + pop[(int64_t)i * N + cell];
+    s += (double)d;
+  }
+  return s;
+}
+
+/* n steps with ping-pong; returns 0 when the state ends in a, 1 in b. */
+int FN(orc_run)(const orc_params* P, int nx, int ny, int nz, const uint32_t* tipo, REAL* a, REAL* b,
+                int nsteps, int storage, int nthreads) {
+  REAL* s = a;
+  REAL* d = b;
+  ORC_UNROLL
+  for (int k = 0; k < nsteps; ++k) {
+    FN(orc_step)(P, nx, ny, nz, tipo, s, d, NULL, storage, nthreads);
+    REAL* t = s; s = d; d = t;
+  }
+  return s == a ? 0 : 1;
+}
+
+#undef FN
+#undef CAT
+#undef CAT2

@@ -1,0 +1,166 @@
+"""CUDA step vs the CPU oracle on identical inputs.
+
+fp32: bit-exact (the kernels are built with -fmad=false and IEEE div/sqrt and
+follow the shader's operation order).  The same holds for the fp64 judge and
+for the 16-bit storage forms, whose rounding the oracle reproduces.  The
+spec bar (fp32 populations within 1e-5 relative after 1000 steps) is
+therefore met with margin; tests assert equality.
+Solid cells carry no state in the reference (nothing reads them), so
+population comparisons cover the non-solid cells.
+"""
+import numpy as np
+import pytest
+
+from tests.cases import all_types_tunnel, random_state, sphere_tunnel
+
+pytestmark = pytest.mark.gpu
+
+STORAGES = {"f32": (np.float32, 0), "f64": (np.float64, 0), "f16s": (np.float32, 1), "bf16s": (np.float32, 2)}
+
+
+def _solver(grade, storage="f32", pingpong=False):
+    from cfd__gb300 import SolverCUDA
+    return SolverCUDA(grade, storage=storage, pingpong=pingpong)
+
+
+def _oracle(grade, storage):
+    from oracle import oracle as O
+    dt, q = STORAGES[storage]
+    return O.Lattice((grade["nx"], grade["ny"], grade["nz"]), dtype=dt, storage=q, nthreads=8)
+
+
+def _cfg(esp, **kw):
+    base = dict(omegaPlus=1.85, lesCs=0.12, inletU=[0.05, 0.0, 0.01], beltU=[0.05, 0.0, 0.0], esponja=esp,
+                espessuraCL=0)
+    base.update(kw)
+    return base
+
+
+def _ocfg(c):
+    return dict(omega_plus=c["omegaPlus"], les_cs=c["lesCs"], inlet_u=c["inletU"], belt_u=c["beltU"],
+                sponge_start=c["esponja"]["inicio"], sponge_len=c["esponja"]["comprimento"],
+                bl_thickness=c["espessuraCL"])
+
+
+def _fluid(tipo):
+    t = np.asarray(tipo).reshape(-1)
+    return ~np.isin(t, [1, 4, 7])
+
+
+@pytest.mark.parametrize("storage", ["f32", "f64", "f16s", "bf16s"])
+@pytest.mark.parametrize("pingpong", [False, True])
+def test_step_bit_exact_all_cell_classes(native, storage, pingpong):
+    grade, tipo, esp = all_types_tunnel()
+    cfg = _cfg(esp)
+    g0 = random_state(int(np.prod(list(grade.values()))), seed=11)
+    s = _solver(grade, storage, pingpong)
+    s.definirTipos(tipo)
+    s.configurar(**cfg)
+    s.definirPopulacoes(g0)
+    o = _oracle(grade, storage)
+    o.set_types(tipo)
+    o.configure(**_ocfg(cfg))
+    o.set_populations(g0)
+    fl = _fluid(tipo)
+    for n in (1, 1, 7, 40):
+        s.passo(n)
+        o.step(n, macros=True)
+        gs = s.lerPopulacoes()[:, fl]
+        go = o.populations().reshape(19, -1)[:, fl]
+        assert np.array_equal(gs, go), f"{storage} pingpong={pingpong} after {s.passos}: max diff {np.abs(gs - go).max()}"
+    m = s.lerMacros()
+    assert np.array_equal(m, o.macros), "pulled macros differ"
+    fs = np.array(s.medirForcas())
+    fo = o.forces()
+    np.testing.assert_allclose(fs, fo, rtol=1e-12, atol=1e-15)
+    s.atualizarMacros()
+    assert np.array_equal(s.lerMacros(), o.update_macros(zero_solids=True))
+    np.testing.assert_allclose(s.massa(), o.mass(), rtol=1e-12, atol=1e-13)
+    s.destruir()
+
+
+def test_init_matches_oracle(native):
+    grade, tipo, esp = all_types_tunnel()
+    cfg = _cfg(esp)
+    s = _solver(grade)
+    s.definirTipos(tipo)
+    s.configurar(**cfg)
+    s.inicializar()
+    o = _oracle(grade, "f32")
+    o.set_types(tipo)
+    o.configure(**_ocfg(cfg))
+    o.init()
+    # init writes every cell, solids included (src/core/emit/wgsl.js:285-299)
+    assert np.array_equal(s.lerPopulacoes(), o.populations().reshape(19, -1))
+
+
+def test_config1_sphere_1000_steps_bit_exact(native):
+    """128x64x64, sphere D=16 at (40,32,32), Re 100 (omega 1.908397), Cs 0.1,
+    1000 steps from uniform equilibrium: all populations equal the oracle's."""
+    grade, corpo, tipo, esp = sphere_tunnel(128, 64, 64, r=8, cx=40)
+    nu = 0.05 * 16 / 100
+    cfg = dict(omegaPlus=1 / (3 * nu + 0.5), lesCs=0.1, inletU=[0.05, 0, 0], beltU=[0, 0, 0], esponja=esp,
+               espessuraCL=0)
+    s = _solver(grade)
+    s.definirTipos(tipo)
+    s.configurar(**cfg)
+    s.inicializar()
+    o = _oracle(grade, "f32")
+    o.set_types(tipo)
+    o.configure(**_ocfg(cfg))
+    o.init()
+    s.passo(1000)
+    o.run(1000)
+    fl = _fluid(tipo)
+    gs = s.lerPopulacoes()[:, fl]
+    go = o.populations().reshape(19, -1)[:, fl]
+    rel = np.abs(gs - go).max() / np.abs(go).max()
+    assert rel <= 1e-5            # the stated bar
+    assert np.array_equal(gs, go)  # and in fact bit-exact
+
+
+def test_inplace_equals_pingpong_full_size(native):
+    """Size-independent property at the full config-1 size: the in-place
+    layout and the reference's A/B scheme give the same state bitwise."""
+    grade, corpo, tipo, esp = sphere_tunnel(128, 64, 64, r=8, cx=40, esteira=True, floor_mirror=False)
+    cfg = _cfg(esp, omegaPlus=1.9083969, lesCs=0.1)
+    a = _solver(grade)
+    b = _solver(grade, pingpong=True)
+    for s in (a, b):
+        s.definirTipos(tipo)
+        s.configurar(**cfg)
+        s.inicializar()
+    fa = a.passoComForcas(1000)
+    fb = b.passoComForcas(1000)
+    fl = _fluid(tipo)
+    assert np.array_equal(a.lerPopulacoes()[:, fl], b.lerPopulacoes()[:, fl])
+    np.testing.assert_allclose(fa, fb, rtol=1e-11, atol=1e-13)
+
+
+def test_fused_force_equals_measured_force(native):
+    grade, corpo, tipo, esp = sphere_tunnel(64, 32, 32, r=6, cx=20)
+    s = _solver(grade)
+    s.definirTipos(tipo)
+    s.configurar(**_cfg(esp, beltU=[0, 0, 0]))
+    s.inicializar()
+    for _ in range(5):
+        f_before = np.array(s.medirForcas())
+        fused = s.passoComForcas(1)[0]
+        np.testing.assert_allclose(fused, f_before, rtol=1e-12, atol=1e-14)
+
+
+def test_rest_offset_on_zero_state(native):
+    """calibrarRepouso on the all-zero state equals sum over links of 2 w_i c_i
+    (src/backend/webgpu/solver.js:457-479); zero for a body away from walls."""
+    grade, corpo, tipo, esp = sphere_tunnel(48, 32, 32, r=6, cx=20)
+    s = _solver(grade)
+    s.definirTipos(tipo)
+    s.configurar(**_cfg(esp))
+    off = s.calibrarRepouso()
+    np.testing.assert_allclose(off, [0, 0, 0], atol=1e-12)
+    # a body resting on the floor has a net downward offset
+    t = tipo.reshape(32, 32, 48).copy()
+    t[1:4, 10:20, 10:20] = 1
+    s.definirTipos(t.reshape(-1))
+    off2 = s.calibrarRepouso()
+    assert off2[2] != 0.0
