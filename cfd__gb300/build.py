@@ -25,7 +25,7 @@ LIB = os.path.join(OUT_DIR, "libcfdgb300.so")
 INCLUDE = os.path.join(os.path.dirname(PKG), "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-BASE = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE,
+BASE = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-I", INCLUDE,
                "--expt-relaxed-constexpr"]
 
 # translation unit -> extra flags

@@ -129,14 +129,15 @@ Ops ops_for(int storage) {
 }
 
 Launch cell_launch(const lbm_ctx* c) {
+  // The in-place step is compiled for at most 128 threads per block.
   int bx = c->block_x;
   if (bx <= 0) {
-    bx = 128;
+    bx = 64;
     const int rx = ((c->dims.nx + 31) / 32) * 32;
     if (rx < bx) bx = rx;
   }
   int by = c->block_y > 0 ? c->block_y : 1;
-  while (bx * by > 256) by = std::max(1, by / 2);
+  while (bx * by > 128) by = std::max(1, by / 2);
   Launch L;
   L.block = dim3(bx, by, 1);
   L.grid = dim3((c->dims.nx + bx - 1) / bx, (c->dims.ny + by - 1) / by, c->dims.nz);
@@ -455,7 +456,7 @@ int lbm_get_info(lbm_ctx* c, lbm_info* info) {
 
 int lbm_set_block(lbm_ctx* c, int block_x) {
   if (!c) return fail(LBM_EINVAL, "null context");
-  if (block_x < 0 || block_x > 256 || (block_x % 32) != 0) return fail(LBM_EINVAL, "block_x must be 0 or a multiple of 32 up to 256");
+  if (block_x < 0 || block_x > 128 || (block_x % 32) != 0) return fail(LBM_EINVAL, "block_x must be 0 or a multiple of 32 up to 128");
   c->block_x = block_x;
   return LBM_OK;
 }

@@ -140,21 +140,71 @@ __device__ __forceinline__ void moments(const R* g, R& delta, R& rho, R& ux, R& 
   uu = ux * ux + uy * uy + uz * uz;
 }
 
+// Warp-uniform values derived from Params once per launch on the host (same
+// IEEE operations the per-cell code would do, so results do not change):
+//   tau0 = 1/omega+, tau0^2, 18 Cs^2 (src/core/emit/ir.js:290-293);
+//   with Cs = 0 the LES root is exactly tau0 (sqrt(RN(t^2)) = t in binary
+//   round-to-nearest), so omega+ and omega- are uniform too;
+//   the sponge's free-stream targets (src/core/emit/ir.js:464-476).
+template <typename R>
+struct Uni {
+  R tau0, tau0sq, c18;
+  R omegaP0, omegaM0;
+  R sp_start, sp_len;
+  R sp_t[Q];
+  int les_on;
+};
+
+template <typename R>
+__host__ __device__ inline R dotc_h(int i, R vx, R vy, R vz) {
+  const int a = cx(i), b = cy(i), c = cz(i);
+  R acc = R(0);
+  bool first = true;
+  if (a != 0) { acc = a > 0 ? vx : -vx; first = false; }
+  if (b != 0) { if (first) { acc = b > 0 ? vy : -vy; first = false; } else acc = b > 0 ? acc + vy : acc - vy; }
+  if (c != 0) { if (first) { acc = c > 0 ? vz : -vz; } else acc = c > 0 ? acc + vz : acc - vz; }
+  return acc;
+}
+
+// Host side (built with -ffp-contract=off: no fused multiply-add).
+template <typename R>
+inline Uni<R> make_uni(const Params& P) {
+  Uni<R> u;
+  const R cs = R(P.les_cs);
+  u.tau0 = R(1.0) / R(P.omega_plus);
+  u.tau0sq = u.tau0 * u.tau0;
+  u.c18 = R(18.0) * cs * cs;
+  u.les_on = !(cs == R(0.0));
+  u.omegaP0 = R(1.0) / u.tau0;
+  u.omegaM0 = R(1.0) / (R(P.magic) / (R(1.0) / u.omegaP0 - R(0.5)) + R(0.5));
+  u.sp_start = R(P.sponge_start);
+  u.sp_len = R(P.sponge_len) > R(1.0) ? R(P.sponge_len) : R(1.0);
+  const R ix = R(P.inlet[0]), iy = R(P.inlet[1]), iz = R(P.inlet[2]);
+  const R uuInf = ix * ix + iy * iy + iz * iz;
+  u.sp_t[0] = Lit<R>::w(0) * (R(-1.5) * uuInf);
+  for (int i = 1; i < Q; ++i) {
+    const R si = dotc_h<R>(i, ix, iy, iz);
+    u.sp_t[i] = Lit<R>::w(i) * (R(3.0) * si + R(4.5) * si * si - R(1.5) * uuInf);
+  }
+  return u;
+}
+
 // Everything after the pull for one non-solid cell: the boundary branches and
 // the fluid collide with LES, TRT and sponge (src/core/emit/ir.js:505-530).
-// g: pulled populations; out: post-collision populations.  Returns nothing;
-// the caller owns the loads, stores and the macros (u, delta) it already has.
-template <typename R>
-__device__ __forceinline__ void collide(const Params& P, uint32_t ct, int x, int z, const R* g,
-                                        R delta, R rho, R ux, R uy, R uz, R uu, R* out) {
+// g: pulled populations.  Each post-collision population is handed to
+// emit(i, value) as soon as it exists (i is a compile-time constant after
+// unrolling), so no output array stays live.
+template <typename R, typename Emit>
+__device__ __forceinline__ void collide(const Params& P, const Uni<R>& U, uint32_t ct, int x, int z, const R* g,
+                                        R delta, R rho, R ux, R uy, R uz, R uu, Emit&& emit) {
   if (ct == ESPELHO_Y) {
 #pragma unroll
-    for (int i = 0; i < Q; ++i) out[i] = g[mirror_idx(i, 1)];
+    for (int i = 0; i < Q; ++i) emit(i, g[mirror_idx(i, 1)]);
     return;
   }
   if (ct == ESPELHO_Z) {
 #pragma unroll
-    for (int i = 0; i < Q; ++i) out[i] = g[mirror_idx(i, 2)];
+    for (int i = 0; i < Q; ++i) emit(i, g[mirror_idx(i, 2)]);
     return;
   }
   if (ct == ENTRADA) {
@@ -167,46 +217,61 @@ __device__ __forceinline__ void collide(const Params& P, uint32_t ct, int x, int
     const R ex = R(P.inlet[0]) * blf, ey = R(P.inlet[1]) * blf, ez = R(P.inlet[2]) * blf;
     const R deltaIn = R(0.0), rhoIn = R(1.0);
     const R uuIn = ex * ex + ey * ey + ez * ez;
-    out[0] = Lit<R>::w(0) * (deltaIn - R(1.5) * rhoIn * uuIn);
+    emit(0, Lit<R>::w(0) * (deltaIn - R(1.5) * rhoIn * uuIn));
 #pragma unroll
     for (int i = 1; i < Q; ++i) {
       const R c = dotc<R>(i, ex, ey, ez);
-      out[i] = Lit<R>::w(i) * (deltaIn + rhoIn * (R(3.0) * c + R(4.5) * c * c - R(1.5) * uuIn));
+      emit(i, Lit<R>::w(i) * (deltaIn + rhoIn * (R(3.0) * c + R(4.5) * c * c - R(1.5) * uuIn)));
     }
     return;
   }
   if (ct == SAIDA) {
     // blocoSaida with the pulled u (src/core/emit/ir.js:432-444, :512-515)
-    out[0] = Lit<R>::w(0) * (R(-1.5) * uu);
+    emit(0, Lit<R>::w(0) * (R(-1.5) * uu));
 #pragma unroll
     for (int i = 1; i < Q; ++i) {
       const R c = dotc<R>(i, ux, uy, uz);
-      out[i] = Lit<R>::w(i) * (R(3.0) * c + R(4.5) * c * c - R(1.5) * uu);
+      emit(i, Lit<R>::w(i) * (R(3.0) * c + R(4.5) * c * c - R(1.5) * uu));
     }
     return;
   }
   // FLUIDO: equilibrium, Smagorinsky LES (src/core/emit/ir.js:262-301)
-  R n[Q];
+  R omegaP = U.omegaP0, omegaM = U.omegaM0;
+  if (U.les_on) {
+    R n[Q];
 #pragma unroll
-  for (int i = 0; i < Q; ++i) n[i] = g[i] - equilibrium<R>(i, delta, rho, ux, uy, uz, uu);
-  const R pxx = signed_sum<R>(n, [](int i) { return cx(i) * cx(i); });
-  const R pyy = signed_sum<R>(n, [](int i) { return cy(i) * cy(i); });
-  const R pzz = signed_sum<R>(n, [](int i) { return cz(i) * cz(i); });
-  const R pxy = signed_sum<R>(n, [](int i) { return cx(i) * cy(i); });
-  const R pxz = signed_sum<R>(n, [](int i) { return cx(i) * cz(i); });
-  const R pyz = signed_sum<R>(n, [](int i) { return cy(i) * cz(i); });
-  const R pp = pxx * pxx + pyy * pyy + pzz * pzz + R(2.0) * (pxy * pxy + pxz * pxz + pyz * pyz);
-  const R qs = r_sqrt(R(2.0) * pp);
-  const R cs = R(P.les_cs);
-  const R tau0 = R(1.0) / R(P.omega_plus);
-  const R tauT = R(0.5) * (tau0 + r_sqrt(tau0 * tau0 + R(18.0) * cs * cs * qs / rho));
-  const R omegaP = R(1.0) / tauT;
-  const R omegaM = R(1.0) / (R(P.magic) / (R(1.0) / omegaP - R(0.5)) + R(0.5));
+    for (int i = 0; i < Q; ++i) n[i] = g[i] - equilibrium<R>(i, delta, rho, ux, uy, uz, uu);
+    const R pxx = signed_sum<R>(n, [](int i) { return cx(i) * cx(i); });
+    const R pyy = signed_sum<R>(n, [](int i) { return cy(i) * cy(i); });
+    const R pzz = signed_sum<R>(n, [](int i) { return cz(i) * cz(i); });
+    const R pxy = signed_sum<R>(n, [](int i) { return cx(i) * cy(i); });
+    const R pxz = signed_sum<R>(n, [](int i) { return cx(i) * cz(i); });
+    const R pyz = signed_sum<R>(n, [](int i) { return cy(i) * cz(i); });
+    const R pp = pxx * pxx + pyy * pyy + pzz * pzz + R(2.0) * (pxy * pxy + pxz * pxz + pyz * pyz);
+    const R qs = r_sqrt(R(2.0) * pp);
+    const R tauT = R(0.5) * (U.tau0 + r_sqrt(U.tau0sq + U.c18 * qs / rho));
+    omegaP = R(1.0) / tauT;
+    omegaM = R(1.0) / (R(P.magic) / (R(1.0) / omegaP - R(0.5)) + R(0.5));
+  }
 
-  // TRT per opposite pair (src/core/emit/ir.js:304-323); e_i = g_i - n_i is
-  // recomputed from the same operands, so it is the identical value.
-  const R e0 = equilibrium<R>(0, delta, rho, ux, uy, uz, uu);
-  out[0] = g[0] - omegaP * (g[0] - e0);
+  // Sponge weight (src/core/emit/ir.js:458-463): zero for x <= start, where
+  // the blend a (1 - 0) + b 0 leaves every population unchanged.
+  R sig2 = R(0.0);
+  if (R(x) > U.sp_start) {
+    const R sx = (R(x) - U.sp_start) / U.sp_len;
+    const R sigma = sx < R(1.0) ? sx : R(1.0);
+    sig2 = sigma * sigma;
+  }
+  const bool sponge = sig2 != R(0.0);
+
+  // TRT per opposite pair (src/core/emit/ir.js:304-323), each output blended
+  // with the sponge target, mix(a, b, t) = a (1 - t) + b t.
+  {
+    const R e0 = equilibrium<R>(0, delta, rho, ux, uy, uz, uu);
+    R o = g[0] - omegaP * (g[0] - e0);
+    if (sponge) o = o * (R(1.0) - sig2) + U.sp_t[0] * sig2;
+    emit(0, o);
+  }
 #pragma unroll
   for (int i = 1; i < Q; i += 2) {
     const int j = i + 1;
@@ -214,28 +279,14 @@ __device__ __forceinline__ void collide(const Params& P, uint32_t ct, int x, int
     const R ej = equilibrium<R>(j, delta, rho, ux, uy, uz, uu);
     const R p = R(0.5) * ((g[i] + g[j]) - (ei + ej));
     const R m = R(0.5) * ((g[i] - g[j]) - (ei - ej));
-    out[i] = g[i] - omegaP * p - omegaM * m;
-    out[j] = g[j] - omegaP * p + omegaM * m;
-  }
-
-  // Sponge (src/core/emit/ir.js:458-478): mix(a, b, t) = a (1 - t) + b t.
-  // sig2 = 0 leaves every population unchanged (a*1 + b*0 == a for finite b),
-  // so cells before the sponge skip the blend.
-  const R sx = (R(x) - R(P.sponge_start)) / (R(P.sponge_len) > R(1.0) ? R(P.sponge_len) : R(1.0));
-  R sigma = sx > R(0.0) ? sx : R(0.0);
-  sigma = sigma < R(1.0) ? sigma : R(1.0);
-  const R sig2 = sigma * sigma;
-  if (sig2 != R(0.0)) {
-    const R ix = R(P.inlet[0]), iy = R(P.inlet[1]), iz = R(P.inlet[2]);
-    const R uuInf = ix * ix + iy * iy + iz * iz;
-    const R t0 = Lit<R>::w(0) * (R(-1.5) * uuInf);
-    out[0] = out[0] * (R(1.0) - sig2) + t0 * sig2;
-#pragma unroll
-    for (int i = 1; i < Q; ++i) {
-      const R si = dotc<R>(i, ix, iy, iz);
-      const R ti = Lit<R>::w(i) * (R(3.0) * si + R(4.5) * si * si - R(1.5) * uuInf);
-      out[i] = out[i] * (R(1.0) - sig2) + ti * sig2;
+    R oi = g[i] - omegaP * p - omegaM * m;
+    R oj = g[j] - omegaP * p + omegaM * m;
+    if (sponge) {
+      oi = oi * (R(1.0) - sig2) + U.sp_t[i] * sig2;
+      oj = oj * (R(1.0) - sig2) + U.sp_t[j] * sig2;
     }
+    emit(i, oi);
+    emit(j, oj);
   }
 }
 

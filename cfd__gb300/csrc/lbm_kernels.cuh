@@ -92,13 +92,48 @@ __device__ __forceinline__ void warp_add3(double a, double b, double c, double* 
 }
 
 // ------------------------------------------------------------------ step
+// Offsets are 32-bit when every element index of a population set fits
+// (19 N < 2^31, up to 113 M cells), else 64-bit.
+template <bool W64> struct OffT { using type = int32_t; };
+template <> struct OffT<true> { using type = int64_t; };
+
+// Periodic neighbour displacements of one cell (src/core/emit/wgsl.js:176-180).
+template <typename Off>
+struct Deltas {
+  Off xp, yp, ym, zp, zm;
+  __device__ __forceinline__ Deltas(int x, int y, int z, int nx, int ny, int nz) {
+    const Off nxny = (Off)nx * ny;
+    xp = x == nx - 1 ? (Off)(1 - nx) : (Off)1;
+    yp = y == ny - 1 ? (Off)nx - nxny : (Off)nx;
+    ym = y == 0 ? nxny - (Off)nx : -(Off)nx;
+    zp = z == nz - 1 ? -nxny * (Off)(nz - 1) : nxny;
+    zm = z == 0 ? nxny * (Off)(nz - 1) : -nxny;
+  }
+  // x + c_i for the odd (first) member of each pair
+  __device__ __forceinline__ Off odd(int i) const {
+    switch (i) {
+      case 1: return xp;
+      case 3: return yp;
+      case 5: return zp;
+      case 7: return xp + yp;
+      case 9: return xp + ym;
+      case 11: return xp + zp;
+      case 13: return xp + zm;
+      case 15: return yp + zp;
+      default: return yp + zm;   // 17
+    }
+  }
+};
+
 // In-place step.  Grid: (ceil(nx/bx), ceil(ny/by), nz), block (bx, by).
 // PAR: step parity (0 even).  MAC: write (u, delta).  FRC: accumulate the
 // momentum-exchange force of the state being streamed.
-template <class St, int PAR, bool MAC, bool FRC>
-__global__ void __launch_bounds__(256) k_step_inplace(Dev d, Params P) {
+template <class St, int PAR, bool MAC, bool FRC, bool W64>
+__global__ void __launch_bounds__(128, sizeof(typename St::real) == 8 ? 4 : ((FRC || MAC) ? 6 : 8))
+k_step_inplace(Dev d, Params P, Uni<typename St::real> U) {
   using R = typename St::real;
   using S = typename St::store_t;
+  using Off = typename OffT<W64>::type;
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int z = blockIdx.z;
@@ -106,34 +141,32 @@ __global__ void __launch_bounds__(256) k_step_inplace(Dev d, Params P) {
   const bool in = x < nx && y < ny;
   double fx = 0.0, fy = 0.0, fz = 0.0;
   if (in) {
-    const int64_t N = d.N;
-    const int64_t cell = ((int64_t)z * ny + y) * nx + x;
+    const Off N = (Off)d.N;
+    const Off cell = ((Off)z * ny + y) * nx + x;
     const uint32_t lw = __ldg(d.link + cell);
     const uint32_t ct = (lw >> LINK_CLASS_SHIFT) & 7u;
     if (is_solid(ct)) {
       if (MAC) d.macros[cell] = make_float4(0.f, 0.f, 0.f, 0.f);
     } else {
-      S* F = static_cast<S*>(d.pop);
-      const Wrap w = wrap3(x, y, z, nx, ny, d.nz);
+      S* const Fc = static_cast<S*>(d.pop) + cell;
+      const Deltas<Off> D(x, y, z, nx, ny, d.nz);
       constexpr bool E = (PAR == 0);
       R g[Q];
-      int64_t nbo[Q];  // neighbour cell of each odd direction
-      g[0] = St::ld(F + cell);
+      g[0] = St::ld(Fc);
 #pragma unroll
       for (int i = 1; i < Q; i += 2) {
-        const int64_t nb = nbr(i, +1, x, y, z, w, nx, ny);
-        nbo[i] = nb;
-        const bool bbi = (lw >> (i - 1)) & 1u;   // upstream of +c_i  is x - c_i
-        const bool bbj = (lw >> i) & 1u;         // upstream of c_{i+1} is x + c_i
-        const int si = (E ^ bbi) ? i + 1 : i;
-        const int sj = (E ^ bbj) ? i : i + 1;
-        g[i] = St::ld(F + (int64_t)si * N + cell);
-        g[i + 1] = St::ld(F + (int64_t)sj * N + nb);
+        const bool bbi = (lw >> (i - 1)) & 1u;   // x - c_i is solid
+        const bool bbj = (lw >> i) & 1u;         // x + c_i is solid
+        const Off si = (E ^ bbi) ? (Off)(i + 1) : (Off)i;
+        const Off sj = (E ^ bbj) ? (Off)i : (Off)(i + 1);
+        g[i] = St::ld(Fc + si * N);
+        g[i + 1] = St::ld(Fc + D.odd(i) + sj * N);
       }
       // Bounce-back links: moving-wall term and the fused force.
       const uint32_t bbmask = lw & 0x3ffffu;
       if (bbmask) {
         if (lw & LINK_SLOW) {
+          const Wrap w = wrap3(x, y, z, nx, ny, d.nz);
 #pragma unroll
           for (int k = 1; k < Q; ++k) {
             if (!((bbmask >> (k - 1)) & 1u)) continue;
@@ -157,17 +190,18 @@ __global__ void __launch_bounds__(256) k_step_inplace(Dev d, Params P) {
       }
       R delta, rho, ux, uy, uz, uu;
       moments<R>(g, delta, rho, ux, uy, uz, uu);
-      R o[Q];
-      collide<R>(P, ct, x, z, g, delta, rho, ux, uy, uz, uu, o);
-      St::st(F + cell, o[0]);
-#pragma unroll
-      for (int i = 1; i < Q; i += 2) {
-        const int wi = E ? i : i + 1;       // slot receiving g*_i at the neighbour
-        const int wj = E ? i + 1 : i;       // slot receiving g*_{i+1} locally
-        St::st(F + (int64_t)wi * N + nbo[i], o[i]);
-        St::st(F + (int64_t)wj * N + cell, o[i + 1]);
-      }
       if (MAC) d.macros[cell] = make_float4((float)ux, (float)uy, (float)uz, (float)delta);
+      // g*_i of an odd i goes to the neighbour's slot (E ? i : i+1); g*_{i+1}
+      // stays local in slot (E ? i+1 : i); the rest population stays put.
+      collide<R>(P, U, ct, x, z, g, delta, rho, ux, uy, uz, uu, [&](int i, R v) {
+        if (i == 0) {
+          St::st(Fc, v);
+        } else if (i & 1) {
+          St::st(Fc + D.odd(i) + (Off)(E ? i : i + 1) * N, v);
+        } else {
+          St::st(Fc + (Off)(E ? i : i - 1) * N, v);
+        }
+      });
     }
   }
   if (FRC) {
@@ -178,7 +212,7 @@ __global__ void __launch_bounds__(256) k_step_inplace(Dev d, Params P) {
 
 // A/B ping-pong step: the reference's pull verbatim (tipo gathered per link).
 template <class St, bool MAC, bool FRC>
-__global__ void __launch_bounds__(256) k_step_ab(Dev d, Params P) {
+__global__ void __launch_bounds__(256) k_step_ab(Dev d, Params P, Uni<typename St::real> U) {
   using R = typename St::real;
   using S = typename St::store_t;
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -218,11 +252,9 @@ __global__ void __launch_bounds__(256) k_step_ab(Dev d, Params P) {
       }
       R delta, rho, ux, uy, uz, uu;
       moments<R>(g, delta, rho, ux, uy, uz, uu);
-      R o[Q];
-      collide<R>(P, ct, x, z, g, delta, rho, ux, uy, uz, uu, o);
-#pragma unroll
-      for (int i = 0; i < Q; ++i) St::st(dst + (int64_t)i * N + cell, o[i]);
       if (MAC) d.macros[cell] = make_float4((float)ux, (float)uy, (float)uz, (float)delta);
+      collide<R>(P, U, ct, x, z, g, delta, rho, ux, uy, uz, uu,
+                 [&](int i, R v) { St::st(dst + (int64_t)i * N + cell, v); });
     }
   }
   if (FRC) {
@@ -418,23 +450,28 @@ struct Ops {
 
 template <class St>
 struct OpsImpl {
+  using R = typename St::real;
   template <int PAR, bool MAC, bool FRC>
-  static void go_inplace(const Dev& d, const Params& P, Launch L, cudaStream_t s) {
-    k_step_inplace<St, PAR, MAC, FRC><<<L.grid, L.block, 0, s>>>(d, P);
+  static void go_inplace(const Dev& d, const Params& P, const Uni<R>& U, Launch L, cudaStream_t s) {
+    if ((int64_t)Q * d.N < (int64_t)INT32_MAX)
+      k_step_inplace<St, PAR, MAC, FRC, false><<<L.grid, L.block, 0, s>>>(d, P, U);
+    else
+      k_step_inplace<St, PAR, MAC, FRC, true><<<L.grid, L.block, 0, s>>>(d, P, U);
   }
   static cudaError_t step(const Dev& d, const Params& P, int parity, bool inplace, bool mac, bool frc, Launch L,
                           cudaStream_t s) {
+    const Uni<R> U = make_uni<R>(P);
     if (inplace) {
       if (parity == 0) {
-        if (mac) { frc ? go_inplace<0, true, true>(d, P, L, s) : go_inplace<0, true, false>(d, P, L, s); }
-        else { frc ? go_inplace<0, false, true>(d, P, L, s) : go_inplace<0, false, false>(d, P, L, s); }
+        if (mac) { frc ? go_inplace<0, true, true>(d, P, U, L, s) : go_inplace<0, true, false>(d, P, U, L, s); }
+        else { frc ? go_inplace<0, false, true>(d, P, U, L, s) : go_inplace<0, false, false>(d, P, U, L, s); }
       } else {
-        if (mac) { frc ? go_inplace<1, true, true>(d, P, L, s) : go_inplace<1, true, false>(d, P, L, s); }
-        else { frc ? go_inplace<1, false, true>(d, P, L, s) : go_inplace<1, false, false>(d, P, L, s); }
+        if (mac) { frc ? go_inplace<1, true, true>(d, P, U, L, s) : go_inplace<1, true, false>(d, P, U, L, s); }
+        else { frc ? go_inplace<1, false, true>(d, P, U, L, s) : go_inplace<1, false, false>(d, P, U, L, s); }
       }
     } else {
-      if (mac) { if (frc) k_step_ab<St, true, true><<<L.grid, L.block, 0, s>>>(d, P); else k_step_ab<St, true, false><<<L.grid, L.block, 0, s>>>(d, P); }
-      else { if (frc) k_step_ab<St, false, true><<<L.grid, L.block, 0, s>>>(d, P); else k_step_ab<St, false, false><<<L.grid, L.block, 0, s>>>(d, P); }
+      if (mac) { if (frc) k_step_ab<St, true, true><<<L.grid, L.block, 0, s>>>(d, P, U); else k_step_ab<St, true, false><<<L.grid, L.block, 0, s>>>(d, P, U); }
+      else { if (frc) k_step_ab<St, false, true><<<L.grid, L.block, 0, s>>>(d, P, U); else k_step_ab<St, false, false><<<L.grid, L.block, 0, s>>>(d, P, U); }
     }
     return cudaGetLastError();
   }
