@@ -49,9 +49,10 @@ def _fluid(tipo):
 
 @pytest.mark.parametrize("storage", ["f32", "f64", "f16s", "bf16s"])
 @pytest.mark.parametrize("pingpong", [False, True])
-def test_step_bit_exact_all_cell_classes(native, storage, pingpong):
+@pytest.mark.parametrize("cs", [0.12, 0.0])
+def test_step_bit_exact_all_cell_classes(native, storage, pingpong, cs):
     grade, tipo, esp = all_types_tunnel()
-    cfg = _cfg(esp)
+    cfg = _cfg(esp, lesCs=cs)
     g0 = random_state(int(np.prod(list(grade.values()))), seed=11)
     s = _solver(grade, storage, pingpong)
     s.definirTipos(tipo)
