@@ -13,7 +13,7 @@ import threading
 from . import build as _build
 
 F32, F16S, BF16S, F64 = 0, 1, 2, 3
-FLAG_WRITE_MACROS, FLAG_PINGPONG = 1, 2
+FLAG_WRITE_MACROS, FLAG_PINGPONG, FLAG_STRICT = 1, 2, 4
 
 OK, EINVAL, ENOMEM, ECUDA, ETIMEDOUT, ESTATE, ENOTSUP = 0, -1, -2, -3, -4, -5, -6
 _NAMES = {EINVAL: "EINVAL", ENOMEM: "ENOMEM", ECUDA: "ECUDA", ETIMEDOUT: "ETIMEDOUT",

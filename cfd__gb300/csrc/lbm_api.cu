@@ -201,7 +201,8 @@ int check_ready(lbm_ctx* c, bool need_cfg) {
 int launch_step(lbm_ctx* c, bool mac, double* force) {
   Dev d = dev_of(c);
   d.force = force;
-  cudaError_t e = c->ops.step(d, c->P, parity(c), c->inplace, mac, force != nullptr, cell_launch(c), c->stream);
+  cudaError_t e = c->ops.step(d, c->P, parity(c), c->inplace, mac, force != nullptr, !(c->flags & LBM_FLAG_STRICT),
+                              cell_launch(c), c->stream);
   if (e != cudaSuccess) return cuda_fail(e, "step kernel launch");
   if (!c->inplace) std::swap(c->pop, c->pop2);
   c->steps++;
@@ -220,7 +221,7 @@ int lbm_create(const lbm_dims* dims, int storage, int flags, lbm_ctx** out) {
   if (dims->nx < 1 || dims->ny < 1 || dims->nz < 1) return fail(LBM_EINVAL, "grid dimensions must be >= 1");
   if (dims->ny > 65535 * 256 || dims->nz > 65535) return fail(LBM_EINVAL, "grid too large for the launch shape");
   if (storage < LBM_F32 || storage > LBM_F64) return fail(LBM_EINVAL, "unknown storage form");
-  if (flags & ~(LBM_FLAG_WRITE_MACROS | LBM_FLAG_PINGPONG)) return fail(LBM_EINVAL, "unknown flag bits");
+  if (flags & ~(LBM_FLAG_WRITE_MACROS | LBM_FLAG_PINGPONG | LBM_FLAG_STRICT)) return fail(LBM_EINVAL, "unknown flag bits");
   lbm_ctx* c = new lbm_ctx();
   c->dims = *dims;
   c->N = (int64_t)dims->nx * dims->ny * dims->nz;

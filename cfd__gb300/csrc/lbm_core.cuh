@@ -12,6 +12,8 @@
 #include <cuda_fp16.h>
 #include <cuda_bf16.h>
 
+#include <cmath>
+
 namespace lbm {
 
 constexpr int Q = 19;
@@ -116,17 +118,42 @@ __device__ __forceinline__ R signed_sum(const R* v, K coef) {
   return acc;
 }
 
-// Equilibrium of one direction (src/core/emit/ir.js:216-232).
+// ---------------------------------------------------------- arithmetic modes
+// Two restatements of the shader's arithmetic, both reproduced bit for bit by
+// the CPU oracle:
+//  * STRICT (FAST = false): the generated shader text read literally, one IEEE
+//    operation per written operator, no contraction (src/core/emit/ir.js).
+//  * FAST (FAST = true): the same formulas with fused multiply-adds at fixed
+//    places, u = m * (1/rho) (one reciprocal instead of three divisions) and
+//    omega- = (tau - 1/2) / (Lambda + (tau - 1/2)/2), which is
+//    1 / (Lambda / (1/omega+ - 1/2) + 1/2) with 1/omega+ = tau exactly
+//    (src/core/emit/ir.js:297-299).  Rounding differs from STRICT by ~1 ulp per
+//    operation; the fp64 judge always runs STRICT.
+// Explicit fmaf() stays fused under -fmad=false, so both modes are fixed
+// sequences of IEEE operations.
 template <typename R>
-__device__ __forceinline__ R equilibrium(int i, R delta, R rho, R ux, R uy, R uz, R uu) {
+__device__ __forceinline__ R fma_r(R a, R b, R c) { return fma(a, b, c); }
+template <>
+__device__ __forceinline__ float fma_r<float>(float a, float b, float c) { return fmaf(a, b, c); }
+
+// Equilibrium of one direction (src/core/emit/ir.js:216-232).  uu15 = 1.5 uu
+// is used by FAST only.
+template <typename R, bool FAST>
+__device__ __forceinline__ R equilibrium(int i, R delta, R rho, R ux, R uy, R uz, R uu, R uu15) {
+  if (FAST) {
+    if (i == 0) return Lit<R>::w(0) * fma_r<R>(-rho, uu15, delta);
+    const R cu = dotc<R>(i, ux, uy, uz);
+    const R a = fma_r<R>(cu, fma_r<R>(R(4.5), cu, R(3.0)), -uu15);
+    return Lit<R>::w(i) * fma_r<R>(rho, a, delta);
+  }
   if (i == 0) return Lit<R>::w(0) * (delta - R(1.5) * rho * uu);
   const R cu = dotc<R>(i, ux, uy, uz);
   return Lit<R>::w(i) * (delta + rho * (R(3.0) * cu + R(4.5) * cu * cu - R(1.5) * uu));
 }
 
-// Pulled moments (src/core/emit/ir.js:192-213).
-template <typename R>
-__device__ __forceinline__ void moments(const R* g, R& delta, R& rho, R& ux, R& uy, R& uz, R& uu) {
+// Pulled moments (src/core/emit/ir.js:192-213).  rinv = 1/rho (FAST only).
+template <typename R, bool FAST>
+__device__ __forceinline__ void moments(const R* g, R& delta, R& rho, R& ux, R& uy, R& uz, R& uu, R& rinv) {
   delta = g[0];
 #pragma unroll
   for (int i = 1; i < Q; ++i) delta = delta + g[i];
@@ -134,10 +161,19 @@ __device__ __forceinline__ void moments(const R* g, R& delta, R& rho, R& ux, R& 
   const R mx = signed_sum<R>(g, [](int i) { return cx(i); });
   const R my = signed_sum<R>(g, [](int i) { return cy(i); });
   const R mz = signed_sum<R>(g, [](int i) { return cz(i); });
-  ux = mx / rho;
-  uy = my / rho;
-  uz = mz / rho;
-  uu = ux * ux + uy * uy + uz * uz;
+  if (FAST) {
+    rinv = R(1.0) / rho;
+    ux = mx * rinv;
+    uy = my * rinv;
+    uz = mz * rinv;
+    uu = fma_r<R>(uz, uz, fma_r<R>(uy, uy, ux * ux));
+  } else {
+    rinv = R(0.0);
+    ux = mx / rho;
+    uy = my / rho;
+    uz = mz / rho;
+    uu = ux * ux + uy * uy + uz * uz;
+  }
 }
 
 // Warp-uniform values derived from Params once per launch on the host (same
@@ -149,9 +185,11 @@ __device__ __forceinline__ void moments(const R* g, R& delta, R& rho, R& ux, R& 
 template <typename R>
 struct Uni {
   R tau0, tau0sq, c18;
-  R omegaP0, omegaM0;
+  R omegaP0, omegaM0;      // STRICT, Cs = 0
+  R omegaP0f, omegaM0f;    // FAST, Cs = 0
   R sp_start, sp_len;
-  R sp_t[Q];
+  R sp_t[Q];               // STRICT sponge targets
+  R sp_tf[Q];              // FAST sponge targets
   int les_on;
 };
 
@@ -166,25 +204,36 @@ __host__ __device__ inline R dotc_h(int i, R vx, R vy, R vz) {
   return acc;
 }
 
-// Host side (built with -ffp-contract=off: no fused multiply-add).
+inline float fma_h(float a, float b, float c) { return std::fmaf(a, b, c); }
+inline double fma_h(double a, double b, double c) { return std::fma(a, b, c); }
+
+// Host side (built with -ffp-contract=off; fusion only where fma_h is called).
 template <typename R>
 inline Uni<R> make_uni(const Params& P) {
   Uni<R> u;
   const R cs = R(P.les_cs);
+  const R magic = R(P.magic);
   u.tau0 = R(1.0) / R(P.omega_plus);
   u.tau0sq = u.tau0 * u.tau0;
   u.c18 = R(18.0) * cs * cs;
   u.les_on = !(cs == R(0.0));
   u.omegaP0 = R(1.0) / u.tau0;
-  u.omegaM0 = R(1.0) / (R(P.magic) / (R(1.0) / u.omegaP0 - R(0.5)) + R(0.5));
+  u.omegaM0 = R(1.0) / (magic / (R(1.0) / u.omegaP0 - R(0.5)) + R(0.5));
+  u.omegaP0f = R(1.0) / u.tau0;
+  const R tm = u.tau0 - R(0.5);
+  u.omegaM0f = tm / fma_h(R(0.5), tm, magic);
   u.sp_start = R(P.sponge_start);
   u.sp_len = R(P.sponge_len) > R(1.0) ? R(P.sponge_len) : R(1.0);
   const R ix = R(P.inlet[0]), iy = R(P.inlet[1]), iz = R(P.inlet[2]);
   const R uuInf = ix * ix + iy * iy + iz * iz;
+  const R uuInfF = fma_h(iz, iz, fma_h(iy, iy, ix * ix));
+  const R uu15f = R(1.5) * uuInfF;
   u.sp_t[0] = Lit<R>::w(0) * (R(-1.5) * uuInf);
+  u.sp_tf[0] = Lit<R>::w(0) * (-uu15f);
   for (int i = 1; i < Q; ++i) {
     const R si = dotc_h<R>(i, ix, iy, iz);
     u.sp_t[i] = Lit<R>::w(i) * (R(3.0) * si + R(4.5) * si * si - R(1.5) * uuInf);
+    u.sp_tf[i] = Lit<R>::w(i) * fma_h(si, fma_h(R(4.5), si, R(3.0)), -uu15f);
   }
   return u;
 }
@@ -194,9 +243,9 @@ inline Uni<R> make_uni(const Params& P) {
 // g: pulled populations.  Each post-collision population is handed to
 // emit(i, value) as soon as it exists (i is a compile-time constant after
 // unrolling), so no output array stays live.
-template <typename R, typename Emit>
+template <typename R, bool FAST, typename Emit>
 __device__ __forceinline__ void collide(const Params& P, const Uni<R>& U, uint32_t ct, int x, int z, const R* g,
-                                        R delta, R rho, R ux, R uy, R uz, R uu, Emit&& emit) {
+                                        R delta, R rho, R ux, R uy, R uz, R uu, R rinv, Emit&& emit) {
   if (ct == ESPELHO_Y) {
 #pragma unroll
     for (int i = 0; i < Q; ++i) emit(i, g[mirror_idx(i, 1)]);
@@ -215,6 +264,13 @@ __device__ __forceinline__ void collide(const Params& P, const Uni<R>& U, uint32
     const R zc = R(z) + R(0.5);
     const R blf = zc < bl ? r_pow(zc / uInletBL, Lit<R>::bl_exp()) : R(1.0);
     const R ex = R(P.inlet[0]) * blf, ey = R(P.inlet[1]) * blf, ez = R(P.inlet[2]) * blf;
+    if (FAST) {
+      const R uuIn = fma_r<R>(ez, ez, fma_r<R>(ey, ey, ex * ex));
+      const R uu15 = R(1.5) * uuIn;
+#pragma unroll
+      for (int i = 0; i < Q; ++i) emit(i, equilibrium<R, true>(i, R(0.0), R(1.0), ex, ey, ez, uuIn, uu15));
+      return;
+    }
     const R deltaIn = R(0.0), rhoIn = R(1.0);
     const R uuIn = ex * ex + ey * ey + ez * ez;
     emit(0, Lit<R>::w(0) * (deltaIn - R(1.5) * rhoIn * uuIn));
@@ -225,8 +281,18 @@ __device__ __forceinline__ void collide(const Params& P, const Uni<R>& U, uint32
     }
     return;
   }
+  const R uu15 = R(1.5) * uu;
   if (ct == SAIDA) {
     // blocoSaida with the pulled u (src/core/emit/ir.js:432-444, :512-515)
+    if (FAST) {
+      emit(0, Lit<R>::w(0) * (-uu15));
+#pragma unroll
+      for (int i = 1; i < Q; ++i) {
+        const R c = dotc<R>(i, ux, uy, uz);
+        emit(i, Lit<R>::w(i) * fma_r<R>(c, fma_r<R>(R(4.5), c, R(3.0)), -uu15));
+      }
+      return;
+    }
     emit(0, Lit<R>::w(0) * (R(-1.5) * uu));
 #pragma unroll
     for (int i = 1; i < Q; ++i) {
@@ -236,22 +302,37 @@ __device__ __forceinline__ void collide(const Params& P, const Uni<R>& U, uint32
     return;
   }
   // FLUIDO: equilibrium, Smagorinsky LES (src/core/emit/ir.js:262-301)
-  R omegaP = U.omegaP0, omegaM = U.omegaM0;
+  R e[Q];
+#pragma unroll
+  for (int i = 0; i < Q; ++i) e[i] = equilibrium<R, FAST>(i, delta, rho, ux, uy, uz, uu, uu15);
+  R omegaP = FAST ? U.omegaP0f : U.omegaP0;
+  R omegaM = FAST ? U.omegaM0f : U.omegaM0;
   if (U.les_on) {
     R n[Q];
 #pragma unroll
-    for (int i = 0; i < Q; ++i) n[i] = g[i] - equilibrium<R>(i, delta, rho, ux, uy, uz, uu);
+    for (int i = 0; i < Q; ++i) n[i] = g[i] - e[i];
     const R pxx = signed_sum<R>(n, [](int i) { return cx(i) * cx(i); });
     const R pyy = signed_sum<R>(n, [](int i) { return cy(i) * cy(i); });
     const R pzz = signed_sum<R>(n, [](int i) { return cz(i) * cz(i); });
     const R pxy = signed_sum<R>(n, [](int i) { return cx(i) * cy(i); });
     const R pxz = signed_sum<R>(n, [](int i) { return cx(i) * cz(i); });
     const R pyz = signed_sum<R>(n, [](int i) { return cy(i) * cz(i); });
-    const R pp = pxx * pxx + pyy * pyy + pzz * pzz + R(2.0) * (pxy * pxy + pxz * pxz + pyz * pyz);
-    const R qs = r_sqrt(R(2.0) * pp);
-    const R tauT = R(0.5) * (U.tau0 + r_sqrt(U.tau0sq + U.c18 * qs / rho));
-    omegaP = R(1.0) / tauT;
-    omegaM = R(1.0) / (R(P.magic) / (R(1.0) / omegaP - R(0.5)) + R(0.5));
+    if (FAST) {
+      const R pd = fma_r<R>(pzz, pzz, fma_r<R>(pyy, pyy, pxx * pxx));
+      const R po = fma_r<R>(pyz, pyz, fma_r<R>(pxz, pxz, pxy * pxy));
+      const R pp = fma_r<R>(R(2.0), po, pd);
+      const R qs = r_sqrt(R(2.0) * pp);
+      const R tauT = R(0.5) * (U.tau0 + r_sqrt(fma_r<R>(U.c18 * qs, rinv, U.tau0sq)));
+      omegaP = R(1.0) / tauT;
+      const R tm = tauT - R(0.5);
+      omegaM = tm / fma_r<R>(R(0.5), tm, R(P.magic));
+    } else {
+      const R pp = pxx * pxx + pyy * pyy + pzz * pzz + R(2.0) * (pxy * pxy + pxz * pxz + pyz * pyz);
+      const R qs = r_sqrt(R(2.0) * pp);
+      const R tauT = R(0.5) * (U.tau0 + r_sqrt(U.tau0sq + U.c18 * qs / rho));
+      omegaP = R(1.0) / tauT;
+      omegaM = R(1.0) / (R(P.magic) / (R(1.0) / omegaP - R(0.5)) + R(0.5));
+    }
   }
 
   // Sponge weight (src/core/emit/ir.js:458-463): zero for x <= start, where
@@ -263,30 +344,33 @@ __device__ __forceinline__ void collide(const Params& P, const Uni<R>& U, uint32
     sig2 = sigma * sigma;
   }
   const bool sponge = sig2 != R(0.0);
+  const R oms = R(1.0) - sig2;
+  auto blend = [&](int i, R o) -> R {
+    if (!sponge) return o;
+    return FAST ? fma_r<R>(U.sp_tf[i], sig2, o * oms) : o * oms + U.sp_t[i] * sig2;
+  };
 
   // TRT per opposite pair (src/core/emit/ir.js:304-323), each output blended
   // with the sponge target, mix(a, b, t) = a (1 - t) + b t.
-  {
-    const R e0 = equilibrium<R>(0, delta, rho, ux, uy, uz, uu);
-    R o = g[0] - omegaP * (g[0] - e0);
-    if (sponge) o = o * (R(1.0) - sig2) + U.sp_t[0] * sig2;
-    emit(0, o);
-  }
+  if (FAST) emit(0, blend(0, fma_r<R>(-omegaP, g[0] - e[0], g[0])));
+  else emit(0, blend(0, g[0] - omegaP * (g[0] - e[0])));
 #pragma unroll
   for (int i = 1; i < Q; i += 2) {
     const int j = i + 1;
-    const R ei = equilibrium<R>(i, delta, rho, ux, uy, uz, uu);
-    const R ej = equilibrium<R>(j, delta, rho, ux, uy, uz, uu);
-    const R p = R(0.5) * ((g[i] + g[j]) - (ei + ej));
-    const R m = R(0.5) * ((g[i] - g[j]) - (ei - ej));
-    R oi = g[i] - omegaP * p - omegaM * m;
-    R oj = g[j] - omegaP * p + omegaM * m;
-    if (sponge) {
-      oi = oi * (R(1.0) - sig2) + U.sp_t[i] * sig2;
-      oj = oj * (R(1.0) - sig2) + U.sp_t[j] * sig2;
+    const R p = R(0.5) * ((g[i] + g[j]) - (e[i] + e[j]));
+    const R m = R(0.5) * ((g[i] - g[j]) - (e[i] - e[j]));
+    R oi, oj;
+    if (FAST) {
+      const R gp_i = fma_r<R>(-omegaP, p, g[i]);
+      const R gp_j = fma_r<R>(-omegaP, p, g[j]);
+      oi = fma_r<R>(-omegaM, m, gp_i);
+      oj = fma_r<R>(omegaM, m, gp_j);
+    } else {
+      oi = g[i] - omegaP * p - omegaM * m;
+      oj = g[j] - omegaP * p + omegaM * m;
     }
-    emit(i, oi);
-    emit(j, oj);
+    emit(i, blend(i, oi));
+    emit(j, blend(j, oj));
   }
 }
 

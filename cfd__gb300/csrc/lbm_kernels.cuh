@@ -128,7 +128,7 @@ struct Deltas {
 // In-place step.  Grid: (ceil(nx/bx), ceil(ny/by), nz), block (bx, by).
 // PAR: step parity (0 even).  MAC: write (u, delta).  FRC: accumulate the
 // momentum-exchange force of the state being streamed.
-template <class St, int PAR, bool MAC, bool FRC, bool W64>
+template <class St, int PAR, bool MAC, bool FRC, bool W64, bool FAST>
 __global__ void __launch_bounds__(128, sizeof(typename St::real) == 8 ? 4 : ((FRC || MAC) ? 6 : 8))
 k_step_inplace(Dev d, Params P, Uni<typename St::real> U) {
   using R = typename St::real;
@@ -188,12 +188,12 @@ k_step_inplace(Dev d, Params P, Uni<typename St::real> U) {
           }
         }
       }
-      R delta, rho, ux, uy, uz, uu;
-      moments<R>(g, delta, rho, ux, uy, uz, uu);
+      R delta, rho, ux, uy, uz, uu, rinv;
+      moments<R, FAST>(g, delta, rho, ux, uy, uz, uu, rinv);
       if (MAC) d.macros[cell] = make_float4((float)ux, (float)uy, (float)uz, (float)delta);
       // g*_i of an odd i goes to the neighbour's slot (E ? i : i+1); g*_{i+1}
       // stays local in slot (E ? i+1 : i); the rest population stays put.
-      collide<R>(P, U, ct, x, z, g, delta, rho, ux, uy, uz, uu, [&](int i, R v) {
+      collide<R, FAST>(P, U, ct, x, z, g, delta, rho, ux, uy, uz, uu, rinv, [&](int i, R v) {
         if (i == 0) {
           St::st(Fc, v);
         } else if (i & 1) {
@@ -211,8 +211,8 @@ k_step_inplace(Dev d, Params P, Uni<typename St::real> U) {
 }
 
 // A/B ping-pong step: the reference's pull verbatim (tipo gathered per link).
-template <class St, bool MAC, bool FRC>
-__global__ void __launch_bounds__(256) k_step_ab(Dev d, Params P, Uni<typename St::real> U) {
+template <class St, bool MAC, bool FRC, bool FAST>
+__global__ void __launch_bounds__(128) k_step_ab(Dev d, Params P, Uni<typename St::real> U) {
   using R = typename St::real;
   using S = typename St::store_t;
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -250,11 +250,11 @@ __global__ void __launch_bounds__(256) k_step_ab(Dev d, Params P, Uni<typename S
           g[i] = St::ld(src + (int64_t)i * N + s);
         }
       }
-      R delta, rho, ux, uy, uz, uu;
-      moments<R>(g, delta, rho, ux, uy, uz, uu);
+      R delta, rho, ux, uy, uz, uu, rinv;
+      moments<R, FAST>(g, delta, rho, ux, uy, uz, uu, rinv);
       if (MAC) d.macros[cell] = make_float4((float)ux, (float)uy, (float)uz, (float)delta);
-      collide<R>(P, U, ct, x, z, g, delta, rho, ux, uy, uz, uu,
-                 [&](int i, R v) { St::st(dst + (int64_t)i * N + cell, v); });
+      collide<R, FAST>(P, U, ct, x, z, g, delta, rho, ux, uy, uz, uu, rinv,
+                       [&](int i, R v) { St::st(dst + (int64_t)i * N + cell, v); });
     }
   }
   if (FRC) {
@@ -287,7 +287,7 @@ __global__ void k_init(Dev d, Params P) {
   const Wrap w = wrap3(x, y, z, d.nx, d.ny, d.nz);
 #pragma unroll
   for (int k = 0; k < Q; ++k) {
-    const R e = equilibrium<R>(k, delta, rho, ux, uy, uz, uu);
+    const R e = equilibrium<R, false>(k, delta, rho, ux, uy, uz, uu, R(0.0));  // init is STRICT in both modes
     const int64_t off = INPLACE ? eso_loc(k, 0, cell, x, y, z, w, d.nx, d.ny, N) : (int64_t)k * N + cell;
     St::st(F + off, e);
   }
@@ -438,7 +438,8 @@ struct Launch {
 };
 
 struct Ops {
-  cudaError_t (*step)(const Dev&, const Params&, int parity, bool inplace, bool mac, bool frc, Launch, cudaStream_t);
+  cudaError_t (*step)(const Dev&, const Params&, int parity, bool inplace, bool mac, bool frc, bool fast, Launch,
+                      cudaStream_t);
   cudaError_t (*init)(const Dev&, const Params&, bool inplace, Launch, cudaStream_t);
   cudaError_t (*put_dir)(const Dev&, const double*, int k, int parity, bool inplace, Launch, cudaStream_t);
   cudaError_t (*get_dir)(const Dev&, double*, int k, int parity, bool inplace, Launch, cudaStream_t);
@@ -451,28 +452,36 @@ struct Ops {
 template <class St>
 struct OpsImpl {
   using R = typename St::real;
-  template <int PAR, bool MAC, bool FRC>
+  // The fp64 judge is always STRICT.
+  static constexpr bool kFastOK = sizeof(R) == 4;
+  template <int PAR, bool MAC, bool FRC, bool FAST>
   static void go_inplace(const Dev& d, const Params& P, const Uni<R>& U, Launch L, cudaStream_t s) {
     if ((int64_t)Q * d.N < (int64_t)INT32_MAX)
-      k_step_inplace<St, PAR, MAC, FRC, false><<<L.grid, L.block, 0, s>>>(d, P, U);
+      k_step_inplace<St, PAR, MAC, FRC, false, FAST><<<L.grid, L.block, 0, s>>>(d, P, U);
     else
-      k_step_inplace<St, PAR, MAC, FRC, true><<<L.grid, L.block, 0, s>>>(d, P, U);
+      k_step_inplace<St, PAR, MAC, FRC, true, FAST><<<L.grid, L.block, 0, s>>>(d, P, U);
   }
-  static cudaError_t step(const Dev& d, const Params& P, int parity, bool inplace, bool mac, bool frc, Launch L,
-                          cudaStream_t s) {
-    const Uni<R> U = make_uni<R>(P);
+  template <bool FAST>
+  static void go(const Dev& d, const Params& P, const Uni<R>& U, int parity, bool inplace, bool mac, bool frc,
+                 Launch L, cudaStream_t s) {
     if (inplace) {
       if (parity == 0) {
-        if (mac) { frc ? go_inplace<0, true, true>(d, P, U, L, s) : go_inplace<0, true, false>(d, P, U, L, s); }
-        else { frc ? go_inplace<0, false, true>(d, P, U, L, s) : go_inplace<0, false, false>(d, P, U, L, s); }
+        if (mac) { frc ? go_inplace<0, true, true, FAST>(d, P, U, L, s) : go_inplace<0, true, false, FAST>(d, P, U, L, s); }
+        else { frc ? go_inplace<0, false, true, FAST>(d, P, U, L, s) : go_inplace<0, false, false, FAST>(d, P, U, L, s); }
       } else {
-        if (mac) { frc ? go_inplace<1, true, true>(d, P, U, L, s) : go_inplace<1, true, false>(d, P, U, L, s); }
-        else { frc ? go_inplace<1, false, true>(d, P, U, L, s) : go_inplace<1, false, false>(d, P, U, L, s); }
+        if (mac) { frc ? go_inplace<1, true, true, FAST>(d, P, U, L, s) : go_inplace<1, true, false, FAST>(d, P, U, L, s); }
+        else { frc ? go_inplace<1, false, true, FAST>(d, P, U, L, s) : go_inplace<1, false, false, FAST>(d, P, U, L, s); }
       }
     } else {
-      if (mac) { if (frc) k_step_ab<St, true, true><<<L.grid, L.block, 0, s>>>(d, P, U); else k_step_ab<St, true, false><<<L.grid, L.block, 0, s>>>(d, P, U); }
-      else { if (frc) k_step_ab<St, false, true><<<L.grid, L.block, 0, s>>>(d, P, U); else k_step_ab<St, false, false><<<L.grid, L.block, 0, s>>>(d, P, U); }
+      if (mac) { if (frc) k_step_ab<St, true, true, FAST><<<L.grid, L.block, 0, s>>>(d, P, U); else k_step_ab<St, true, false, FAST><<<L.grid, L.block, 0, s>>>(d, P, U); }
+      else { if (frc) k_step_ab<St, false, true, FAST><<<L.grid, L.block, 0, s>>>(d, P, U); else k_step_ab<St, false, false, FAST><<<L.grid, L.block, 0, s>>>(d, P, U); }
     }
+  }
+  static cudaError_t step(const Dev& d, const Params& P, int parity, bool inplace, bool mac, bool frc, bool fast,
+                          Launch L, cudaStream_t s) {
+    const Uni<R> U = make_uni<R>(P);
+    if (fast && kFastOK) go<kFastOK>(d, P, U, parity, inplace, mac, frc, L, s);
+    else go<false>(d, P, U, parity, inplace, mac, frc, L, s);
     return cudaGetLastError();
   }
   static cudaError_t init(const Dev& d, const Params& P, bool inplace, Launch L, cudaStream_t s) {

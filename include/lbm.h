@@ -74,6 +74,12 @@ extern "C" {
                                      reference's A/B pull exactly
                                      (src/backend/webgpu/solver.js:10-24);
                                      default is one in-place set (esoteric pull) */
+#define LBM_FLAG_STRICT        4  /* the shader's arithmetic read literally: one
+                                     IEEE operation per written operator, no
+                                     fused multiply-add (src/core/emit/ir.js);
+                                     default is the FAST restatement (fixed
+                                     fused multiply-adds, u = m (1/rho)); both
+                                     are reproduced bit for bit by the oracle */
 
 typedef struct lbm_ctx lbm_ctx;
 

@@ -164,6 +164,7 @@ static inline int orc_is_solid(uint32_t t) {
 #define SIXW__f32 SIXW_f
 #define ORC_SQRT sqrtf
 #define ORC_POW powf
+#define ORC_FMA fmaf
 #include "lbm_oracle_impl.h"
 #undef REAL
 #undef SFX
@@ -171,6 +172,7 @@ static inline int orc_is_solid(uint32_t t) {
 #undef LIT
 #undef ORC_SQRT
 #undef ORC_POW
+#undef ORC_FMA
 
 /* ---- fp64 instantiation (the accuracy judge) ---- */
 #define REAL double
@@ -181,6 +183,7 @@ static inline int orc_is_solid(uint32_t t) {
 #define SIXW__f64 SIXW_d
 #define ORC_SQRT sqrt
 #define ORC_POW pow
+#define ORC_FMA fma
 #include "lbm_oracle_impl.h"
 #undef REAL
 #undef SFX
@@ -188,6 +191,7 @@ static inline int orc_is_solid(uint32_t t) {
 #undef LIT
 #undef ORC_SQRT
 #undef ORC_POW
+#undef ORC_FMA
 
 /* ---- exported entry points (ctypes) ---- */
 __attribute__((constructor)) static void orc_ctor(void) { orc_tables(); }

@@ -61,13 +61,29 @@ static inline void FN(orc_equilibrium)(REAL delta, REAL rho, REAL ux, REAL uy, R
 }
 
 
+/* FAST restatement of the equilibrium: w (rho a + delta) with
+ * a = cu (4.5 cu + 3) - 1.5 uu, both by fused multiply-add. */
+static inline void FN(orc_equilibrium_fast)(REAL delta, REAL rho, REAL ux, REAL uy, REAL uz, REAL uu15, REAL* e) {
+  e[0] = FN(W_)[0] * ORC_FMA(-rho, uu15, delta);
+  ORC_UNROLL
+  for (int i = 1; i < ORC_Q; ++i) {
+    const REAL cu = FN(orc_dotc)(i, ux, uy, uz);
+    const REAL a = ORC_FMA(cu, ORC_FMA(LIT(4.5), cu, LIT(3.0)), -uu15);
+    e[i] = FN(W_)[i] * ORC_FMA(rho, a, delta);
+  }
+}
+
 /*
  * One reference step over every cell, A/B ping-pong, natural SoA layout.
  * src -> dst; macros (4 per cell) written when non-null.  Solid cells leave
  * dst untouched (src/core/emit/wgsl.js:201-204).
  */
 void FN(orc_step)(const orc_params* P, int nx, int ny, int nz, const uint32_t* tipo,
-                  const REAL* src, REAL* dst, float* macros, int storage, int nthreads) {
+                  const REAL* src, REAL* dst, float* macros, int storage, int nthreads, int fast_in) {
+  /* FAST restatement: fixed fused multiply-adds (ORC_FMA), u = m (1/rho),
+   * omega- = (tau - 1/2) / (Lambda + (tau - 1/2)/2).  The fp64 judge is
+   * always STRICT. */
+  const int fast = ORC_IS_FLOAT ? fast_in : 0;
   const int64_t N = (int64_t)nx * ny * nz;
   const REAL omegaPlus = (REAL)P->omega_plus, magic = (REAL)P->magic, lesCs = (REAL)P->les_cs;
   const REAL spStart = (REAL)P->sponge_start, spLen = (REAL)P->sponge_len;
@@ -135,8 +151,16 @@ void FN(orc_step)(const orc_params* P, int nx, int ny, int nz, const uint32_t* t
           }
           m[a] = acc;
         }
-        const REAL ux = m[0] / rho, uy = m[1] / rho, uz = m[2] / rho;
-        const REAL uu = ux * ux + uy * uy + uz * uz;
+        REAL ux, uy, uz, uu, rinv = LIT(0.0);
+        if (fast) {
+          rinv = LIT(1.0) / rho;
+          ux = m[0] * rinv; uy = m[1] * rinv; uz = m[2] * rinv;
+          uu = ORC_FMA(uz, uz, ORC_FMA(uy, uy, ux * ux));
+        } else {
+          ux = m[0] / rho; uy = m[1] / rho; uz = m[2] / rho;
+          uu = ux * ux + uy * uy + uz * uz;
+        }
+        const REAL uu15 = LIT(1.5) * uu;
 
         REAL* out[ORC_Q];
         ORC_UNROLL
@@ -147,6 +171,12 @@ void FN(orc_step)(const orc_params* P, int nx, int ny, int nz, const uint32_t* t
           const int ax = ct == ORC_ESPELHO_Y ? 1 : 2;
           ORC_UNROLL
           for (int i = 0; i < ORC_Q; ++i) *out[i] = FN(orc_q)(g[ORC_MIRROR[ax][i]], storage);
+        } else if (ct == ORC_ENTRADA && fast) {
+          const REAL uuIn = ORC_FMA(uez, uez, ORC_FMA(uey, uey, uex * uex));
+          const REAL uuIn15 = LIT(1.5) * uuIn;
+          REAL e[ORC_Q];
+          FN(orc_equilibrium_fast)(LIT(0.0), LIT(1.0), uex, uey, uez, uuIn15, e);
+          for (int i = 0; i < ORC_Q; ++i) *out[i] = FN(orc_q)(e[i], storage);
         } else if (ct == ORC_ENTRADA) {
           /* blocoEntrada (src/core/emit/ir.js:405-422) */
           const REAL deltaIn = LIT(0.0), rhoIn = LIT(1.0);
@@ -156,6 +186,13 @@ void FN(orc_step)(const orc_params* P, int nx, int ny, int nz, const uint32_t* t
           for (int i = 1; i < ORC_Q; ++i) {
             const REAL ci = FN(orc_dotc)(i, uex, uey, uez);
             *out[i] = FN(orc_q)(FN(W_)[i] * (deltaIn + rhoIn * (LIT(3.0) * ci + LIT(4.5) * ci * ci - LIT(1.5) * uuIn)), storage);
+          }
+        } else if (ct == ORC_SAIDA && fast) {
+          *out[0] = FN(orc_q)(FN(W_)[0] * (-uu15), storage);
+          ORC_UNROLL
+          for (int i = 1; i < ORC_Q; ++i) {
+            const REAL cu = FN(orc_dotc)(i, ux, uy, uz);
+            *out[i] = FN(orc_q)(FN(W_)[i] * ORC_FMA(cu, ORC_FMA(LIT(4.5), cu, LIT(3.0)), -uu15), storage);
           }
         } else if (ct == ORC_SAIDA) {
           /* blocoSaida with the pulled u (src/core/emit/ir.js:432-444, :512-515) */
@@ -168,7 +205,8 @@ void FN(orc_step)(const orc_params* P, int nx, int ny, int nz, const uint32_t* t
         } else {
           /* FLUIDO: blocoEquilibrio, blocoLES, blocoColisao, blocoEsponja */
           REAL e[ORC_Q];
-          FN(orc_equilibrium)(delta, rho, ux, uy, uz, uu, e);
+          if (fast) FN(orc_equilibrium_fast)(delta, rho, ux, uy, uz, uu15, e);
+          else FN(orc_equilibrium)(delta, rho, ux, uy, uz, uu, e);
           REAL n[ORC_Q];
           ORC_UNROLL
           for (int i = 0; i < ORC_Q; ++i) n[i] = g[i] - e[i];
@@ -188,24 +226,43 @@ void FN(orc_step)(const orc_params* P, int nx, int ny, int nz, const uint32_t* t
             }
             pi[k] = acc;
           }
-          const REAL pp = pi[0] * pi[0] + pi[1] * pi[1] + pi[2] * pi[2] +
-                          LIT(2.0) * (pi[3] * pi[3] + pi[4] * pi[4] + pi[5] * pi[5]);
-          const REAL qs = ORC_SQRT(LIT(2.0) * pp);
           const REAL tau0 = LIT(1.0) / omegaPlus;
-          const REAL tauT = LIT(0.5) * (tau0 + ORC_SQRT(tau0 * tau0 + LIT(18.0) * lesCs * lesCs * qs / rho));
-          const REAL omegaP = LIT(1.0) / tauT;
-          const REAL omegaM = LIT(1.0) / (magic / (LIT(1.0) / omegaP - LIT(0.5)) + LIT(0.5));
+          REAL omegaP, omegaM;
+          if (fast) {
+            const REAL pd = ORC_FMA(pi[2], pi[2], ORC_FMA(pi[1], pi[1], pi[0] * pi[0]));
+            const REAL po = ORC_FMA(pi[5], pi[5], ORC_FMA(pi[4], pi[4], pi[3] * pi[3]));
+            const REAL pp = ORC_FMA(LIT(2.0), po, pd);
+            const REAL qs = ORC_SQRT(LIT(2.0) * pp);
+            const REAL c18 = LIT(18.0) * lesCs * lesCs;
+            const REAL tauT = LIT(0.5) * (tau0 + ORC_SQRT(ORC_FMA(c18 * qs, rinv, tau0 * tau0)));
+            omegaP = LIT(1.0) / tauT;
+            const REAL tm = tauT - LIT(0.5);
+            omegaM = tm / ORC_FMA(LIT(0.5), tm, magic);
+          } else {
+            const REAL pp = pi[0] * pi[0] + pi[1] * pi[1] + pi[2] * pi[2] +
+                            LIT(2.0) * (pi[3] * pi[3] + pi[4] * pi[4] + pi[5] * pi[5]);
+            const REAL qs = ORC_SQRT(LIT(2.0) * pp);
+            const REAL tauT = LIT(0.5) * (tau0 + ORC_SQRT(tau0 * tau0 + LIT(18.0) * lesCs * lesCs * qs / rho));
+            omegaP = LIT(1.0) / tauT;
+            omegaM = LIT(1.0) / (magic / (LIT(1.0) / omegaP - LIT(0.5)) + LIT(0.5));
+          }
 
           /* blocoColisao (src/core/emit/ir.js:304-323) */
           REAL o[ORC_Q];
-          o[0] = g[0] - omegaP * (g[0] - e[0]);
+          if (fast) o[0] = ORC_FMA(-omegaP, g[0] - e[0], g[0]);
+          else o[0] = g[0] - omegaP * (g[0] - e[0]);
           ORC_UNROLL
           for (int i = 1; i < ORC_Q; i += 2) {
             const int j = i + 1;
             const REAL p = LIT(0.5) * ((g[i] + g[j]) - (e[i] + e[j]));
             const REAL mm = LIT(0.5) * ((g[i] - g[j]) - (e[i] - e[j]));
-            o[i] = g[i] - omegaP * p - omegaM * mm;
-            o[j] = g[j] - omegaP * p + omegaM * mm;
+            if (fast) {
+              o[i] = ORC_FMA(-omegaM, mm, ORC_FMA(-omegaP, p, g[i]));
+              o[j] = ORC_FMA(omegaM, mm, ORC_FMA(-omegaP, p, g[j]));
+            } else {
+              o[i] = g[i] - omegaP * p - omegaM * mm;
+              o[j] = g[j] - omegaP * p + omegaM * mm;
+            }
           }
 
           /* blocoEsponja (src/core/emit/ir.js:458-478); mix(a,b,t) = a(1-t) + bt */
@@ -213,16 +270,33 @@ void FN(orc_step)(const orc_params* P, int nx, int ny, int nz, const uint32_t* t
           REAL sigma = sxs > LIT(0.0) ? sxs : LIT(0.0);
           sigma = sigma < LIT(1.0) ? sigma : LIT(1.0);
           const REAL sig2 = sigma * sigma;
-          const REAL uuInf = inx * inx + iny * iny + inz * inz;
-          {
-            const REAL t0 = FN(W_)[0] * (LIT(-1.5) * uuInf);
-            o[0] = o[0] * (LIT(1.0) - sig2) + t0 * sig2;
-          }
-          ORC_UNROLL
-          for (int i = 1; i < ORC_Q; ++i) {
-            const REAL si = FN(orc_dotc)(i, inx, iny, inz);
-            const REAL ti = FN(W_)[i] * (LIT(3.0) * si + LIT(4.5) * si * si - LIT(1.5) * uuInf);
-            o[i] = o[i] * (LIT(1.0) - sig2) + ti * sig2;
+          if (fast) {
+            const REAL uuInf = ORC_FMA(inz, inz, ORC_FMA(iny, iny, inx * inx));
+            const REAL uuInf15 = LIT(1.5) * uuInf;
+            REAL t[ORC_Q];
+            t[0] = FN(W_)[0] * (-uuInf15);
+            ORC_UNROLL
+            for (int i = 1; i < ORC_Q; ++i) {
+              const REAL si = FN(orc_dotc)(i, inx, iny, inz);
+              t[i] = FN(W_)[i] * ORC_FMA(si, ORC_FMA(LIT(4.5), si, LIT(3.0)), -uuInf15);
+            }
+            if (sig2 != LIT(0.0)) {
+              const REAL oms = LIT(1.0) - sig2;
+              ORC_UNROLL
+              for (int i = 0; i < ORC_Q; ++i) o[i] = ORC_FMA(t[i], sig2, o[i] * oms);
+            }
+          } else {
+            const REAL uuInf = inx * inx + iny * iny + inz * inz;
+            {
+              const REAL t0 = FN(W_)[0] * (LIT(-1.5) * uuInf);
+              o[0] = o[0] * (LIT(1.0) - sig2) + t0 * sig2;
+            }
+            ORC_UNROLL
+            for (int i = 1; i < ORC_Q; ++i) {
+              const REAL si = FN(orc_dotc)(i, inx, iny, inz);
+              const REAL ti = FN(W_)[i] * (LIT(3.0) * si + LIT(4.5) * si * si - LIT(1.5) * uuInf);
+              o[i] = o[i] * (LIT(1.0) - sig2) + ti * sig2;
+            }
           }
           ORC_UNROLL
           for (int i = 0; i < ORC_Q; ++i) *out[i] = FN(orc_q)(o[i], storage);
@@ -396,12 +470,12 @@ double FN(orc_mass)(int nx, int ny, int nz, const uint32_t* tipo, const REAL* po
 
 /* n steps with ping-pong; returns 0 when the state ends in a, 1 in b. */
 int FN(orc_run)(const orc_params* P, int nx, int ny, int nz, const uint32_t* tipo, REAL* a, REAL* b,
-                int nsteps, int storage, int nthreads) {
+                int nsteps, int storage, int nthreads, int fast) {
   REAL* s = a;
   REAL* d = b;
   ORC_UNROLL
   for (int k = 0; k < nsteps; ++k) {
-    FN(orc_step)(P, nx, ny, nz, tipo, s, d, NULL, storage, nthreads);
+    FN(orc_step)(P, nx, ny, nz, tipo, s, d, NULL, storage, nthreads, fast);
     REAL* t = s; s = d; d = t;
   }
   return s == a ? 0 : 1;

@@ -71,14 +71,14 @@ def lib():
             P = C.POINTER
             vp = C.c_void_p
             for sfx in ("f32", "f64"):
-                getattr(L, f"orc_step_{sfx}").argtypes = [P(OrcParams), C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, C.c_int, C.c_int]
+                getattr(L, f"orc_step_{sfx}").argtypes = [P(OrcParams), C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, C.c_int, C.c_int, C.c_int]
                 getattr(L, f"orc_init_{sfx}").argtypes = [P(OrcParams), C.c_int, C.c_int, C.c_int, vp, vp, C.c_int]
                 getattr(L, f"orc_macros_{sfx}").argtypes = [C.c_int, C.c_int, C.c_int, vp, vp, vp, C.c_int]
                 getattr(L, f"orc_forces_acc64_{sfx}").argtypes = [C.c_int, C.c_int, C.c_int, vp, vp, vp]
                 getattr(L, f"orc_forces_faithful_{sfx}").argtypes = [C.c_int, C.c_int, C.c_int, vp, vp, vp]
                 getattr(L, f"orc_mass_{sfx}").argtypes = [C.c_int, C.c_int, C.c_int, vp, vp]
                 getattr(L, f"orc_mass_{sfx}").restype = C.c_double
-                getattr(L, f"orc_run_{sfx}").argtypes = [P(OrcParams), C.c_int, C.c_int, C.c_int, vp, vp, vp, C.c_int, C.c_int, C.c_int]
+                getattr(L, f"orc_run_{sfx}").argtypes = [P(OrcParams), C.c_int, C.c_int, C.c_int, vp, vp, vp, C.c_int, C.c_int, C.c_int, C.c_int]
                 getattr(L, f"orc_run_{sfx}").restype = C.c_int
             L.orc_tables_out.argtypes = [vp] * 6
             L.orc_quantize_f32.argtypes = [vp, C.c_int64, C.c_int]
@@ -132,13 +132,14 @@ def tables():
 class Lattice:
     """A/B ping-pong state on the CPU, natural SoA layout, like the reference."""
 
-    def __init__(self, dims, dtype=np.float32, storage=F32, nthreads=1):
+    def __init__(self, dims, dtype=np.float32, storage=F32, nthreads=1, fast=False):
         self.nx, self.ny, self.nz = dims
         self.N = self.nx * self.ny * self.nz
         self.dtype = np.dtype(dtype)
         self.sfx = "f32" if self.dtype == np.float32 else "f64"
         self.storage = storage
         self.nthreads = nthreads
+        self.fast = 1 if fast else 0
         self.a = np.zeros(19 * self.N, self.dtype)
         self.b = np.zeros(19 * self.N, self.dtype)
         self.tipo = np.zeros(self.N, np.uint32)
@@ -167,13 +168,13 @@ class Lattice:
         for k in range(n):
             m = _ptr(self.macros) if (macros and k == n - 1) else None
             getattr(L, f"orc_step_{self.sfx}")(C.byref(self.p), self.nx, self.ny, self.nz, _ptr(self.tipo),
-                                               _ptr(self.a), _ptr(self.b), m, self.storage, self.nthreads)
+                                               _ptr(self.a), _ptr(self.b), m, self.storage, self.nthreads, self.fast)
             self.a, self.b = self.b, self.a
 
     def run(self, n):
         """n steps in C without returning to Python between steps."""
         which = getattr(lib(), f"orc_run_{self.sfx}")(C.byref(self.p), self.nx, self.ny, self.nz, _ptr(self.tipo),
-                                                     _ptr(self.a), _ptr(self.b), n, self.storage, self.nthreads)
+                                                     _ptr(self.a), _ptr(self.b), n, self.storage, self.nthreads, self.fast)
         if which == 1:
             self.a, self.b = self.b, self.a
 
