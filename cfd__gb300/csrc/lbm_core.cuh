@@ -151,9 +151,10 @@ __device__ __forceinline__ R equilibrium(int i, R delta, R rho, R ux, R uy, R uz
   return Lit<R>::w(i) * (delta + rho * (R(3.0) * cu + R(4.5) * cu * cu - R(1.5) * uu));
 }
 
-// Pulled moments (src/core/emit/ir.js:192-213).  rinv = 1/rho (FAST only).
-template <typename R, bool FAST>
-__device__ __forceinline__ void moments(const R* g, R& delta, R& rho, R& ux, R& uy, R& uz, R& uu, R& rinv) {
+// Pulled moments (src/core/emit/ir.js:192-213), STRICT: the emitter's
+// index-order sums and three divisions.
+template <typename R>
+__device__ __forceinline__ void moments_strict(const R* g, R& delta, R& rho, R& ux, R& uy, R& uz, R& uu) {
   delta = g[0];
 #pragma unroll
   for (int i = 1; i < Q; ++i) delta = delta + g[i];
@@ -161,19 +162,51 @@ __device__ __forceinline__ void moments(const R* g, R& delta, R& rho, R& ux, R& 
   const R mx = signed_sum<R>(g, [](int i) { return cx(i); });
   const R my = signed_sum<R>(g, [](int i) { return cy(i); });
   const R mz = signed_sum<R>(g, [](int i) { return cz(i); });
-  if (FAST) {
-    rinv = R(1.0) / rho;
-    ux = mx * rinv;
-    uy = my * rinv;
-    uz = mz * rinv;
-    uu = fma_r<R>(uz, uz, fma_r<R>(uy, uy, ux * ux));
-  } else {
-    rinv = R(0.0);
-    ux = mx / rho;
-    uy = my / rho;
-    uz = mz / rho;
-    uu = ux * ux + uy * uy + uz * uz;
+  ux = mx / rho;
+  uy = my / rho;
+  uz = mz / rho;
+  uu = ux * ux + uy * uy + uz * uz;
+}
+
+// Signed sum over the nine opposite pairs (k = 0..8, odd member i = 2k+1)
+// with coefficient coef(i) of the odd member, pair order.
+template <typename R, typename K>
+__device__ __forceinline__ R pair_sum(const R* v, K coef) {
+  R acc = R(0);
+  bool first = true;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    const int c = coef(2 * k + 1);
+    if (c == 0) continue;
+    if (first) { acc = c > 0 ? v[k] : -v[k]; first = false; }
+    else acc = c > 0 ? acc + v[k] : acc - v[k];
   }
+  return acc;
+}
+
+// FAST moments from the pair sums s_k = g_i + g_j and differences
+// d_k = g_i - g_j (j = opp i): delta = g0 + sum s, rho u = sum c_i d_k,
+// u = (rho u) (1/rho).  s and d are reused by the pair-form collision.
+template <typename R>
+__device__ __forceinline__ void moments_fast(const R* g, R* sp, R* dp, R& delta, R& rho, R& ux, R& uy, R& uz,
+                                             R& uu, R& rinv) {
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    sp[k] = g[2 * k + 1] + g[2 * k + 2];
+    dp[k] = g[2 * k + 1] - g[2 * k + 2];
+  }
+  delta = g[0];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) delta = delta + sp[k];
+  rho = R(1.0) + delta;
+  const R mx = pair_sum<R>(dp, [](int i) { return cx(i); });
+  const R my = pair_sum<R>(dp, [](int i) { return cy(i); });
+  const R mz = pair_sum<R>(dp, [](int i) { return cz(i); });
+  rinv = R(1.0) / rho;
+  ux = mx * rinv;
+  uy = my * rinv;
+  uz = mz * rinv;
+  uu = fma_r<R>(uz, uz, fma_r<R>(uy, uy, ux * ux));
 }
 
 // Warp-uniform values derived from Params once per launch on the host (same
@@ -245,7 +278,8 @@ inline Uni<R> make_uni(const Params& P) {
 // unrolling), so no output array stays live.
 template <typename R, bool FAST, typename Emit>
 __device__ __forceinline__ void collide(const Params& P, const Uni<R>& U, uint32_t ct, int x, int z, const R* g,
-                                        R delta, R rho, R ux, R uy, R uz, R uu, R rinv, Emit&& emit) {
+                                        const R* sp, const R* dp, R delta, R rho, R ux, R uy, R uz, R uu, R rinv,
+                                        Emit&& emit) {
   if (ct == ESPELHO_Y) {
 #pragma unroll
     for (int i = 0; i < Q; ++i) emit(i, g[mirror_idx(i, 1)]);
@@ -302,22 +336,36 @@ __device__ __forceinline__ void collide(const Params& P, const Uni<R>& U, uint32
     return;
   }
   // FLUIDO: equilibrium, Smagorinsky LES (src/core/emit/ir.js:262-301)
-  R e[Q];
+  R omegaP, omegaM;
+  R e0;
+  R ns[9], nd[9];     // FAST: (g_i + g_j) - (e_i + e_j), (g_i - g_j) - (e_i - e_j)
+  R e[Q];             // STRICT: every e_i
+  if (FAST) {
+    // Pair form of the shifted equilibrium (c_j = -c_i, w_j = w_i):
+    //   e_i + e_j = 2 w (delta + rho (4.5 cu^2 - 1.5 uu)),  e_i - e_j = 6 w rho cu.
+    const R uu15 = R(1.5) * uu;
+    e0 = Lit<R>::w(0) * fma_r<R>(-rho, uu15, delta);
+    const R r6a = (R(6.0) * Lit<R>::w(1)) * rho, r6d = (R(6.0) * Lit<R>::w(7)) * rho;
 #pragma unroll
-  for (int i = 0; i < Q; ++i) e[i] = equilibrium<R, FAST>(i, delta, rho, ux, uy, uz, uu, uu15);
-  R omegaP = FAST ? U.omegaP0f : U.omegaP0;
-  R omegaM = FAST ? U.omegaM0f : U.omegaM0;
-  if (U.les_on) {
-    R n[Q];
-#pragma unroll
-    for (int i = 0; i < Q; ++i) n[i] = g[i] - e[i];
-    const R pxx = signed_sum<R>(n, [](int i) { return cx(i) * cx(i); });
-    const R pyy = signed_sum<R>(n, [](int i) { return cy(i) * cy(i); });
-    const R pzz = signed_sum<R>(n, [](int i) { return cz(i) * cz(i); });
-    const R pxy = signed_sum<R>(n, [](int i) { return cx(i) * cy(i); });
-    const R pxz = signed_sum<R>(n, [](int i) { return cx(i) * cz(i); });
-    const R pyz = signed_sum<R>(n, [](int i) { return cy(i) * cz(i); });
-    if (FAST) {
+    for (int k = 0; k < 9; ++k) {
+      const int i = 2 * k + 1;
+      const R cu = dotc<R>(i, ux, uy, uz);
+      const R a2 = fma_r<R>(R(4.5) * cu, cu, -uu15);
+      const R es = (R(2.0) * Lit<R>::w(i)) * fma_r<R>(rho, a2, delta);
+      const R ed = (i <= 6 ? r6a : r6d) * cu;
+      ns[k] = sp[k] - es;
+      nd[k] = dp[k] - ed;
+    }
+    omegaP = U.omegaP0f;
+    omegaM = U.omegaM0f;
+    if (U.les_on) {
+      // Pi_ab = sum over pairs of c_ia c_ib ((g_i + g_j) - (e_i + e_j))
+      const R pxx = pair_sum<R>(ns, [](int i) { return cx(i) * cx(i); });
+      const R pyy = pair_sum<R>(ns, [](int i) { return cy(i) * cy(i); });
+      const R pzz = pair_sum<R>(ns, [](int i) { return cz(i) * cz(i); });
+      const R pxy = pair_sum<R>(ns, [](int i) { return cx(i) * cy(i); });
+      const R pxz = pair_sum<R>(ns, [](int i) { return cx(i) * cz(i); });
+      const R pyz = pair_sum<R>(ns, [](int i) { return cy(i) * cz(i); });
       const R pd = fma_r<R>(pzz, pzz, fma_r<R>(pyy, pyy, pxx * pxx));
       const R po = fma_r<R>(pyz, pyz, fma_r<R>(pxz, pxz, pxy * pxy));
       const R pp = fma_r<R>(R(2.0), po, pd);
@@ -326,7 +374,23 @@ __device__ __forceinline__ void collide(const Params& P, const Uni<R>& U, uint32
       omegaP = R(1.0) / tauT;
       const R tm = tauT - R(0.5);
       omegaM = tm / fma_r<R>(R(0.5), tm, R(P.magic));
-    } else {
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < Q; ++i) e[i] = equilibrium<R, false>(i, delta, rho, ux, uy, uz, uu, R(0.0));
+    e0 = e[0];
+    omegaP = U.omegaP0;
+    omegaM = U.omegaM0;
+    if (U.les_on) {
+      R n[Q];
+#pragma unroll
+      for (int i = 0; i < Q; ++i) n[i] = g[i] - e[i];
+      const R pxx = signed_sum<R>(n, [](int i) { return cx(i) * cx(i); });
+      const R pyy = signed_sum<R>(n, [](int i) { return cy(i) * cy(i); });
+      const R pzz = signed_sum<R>(n, [](int i) { return cz(i) * cz(i); });
+      const R pxy = signed_sum<R>(n, [](int i) { return cx(i) * cy(i); });
+      const R pxz = signed_sum<R>(n, [](int i) { return cx(i) * cz(i); });
+      const R pyz = signed_sum<R>(n, [](int i) { return cy(i) * cz(i); });
       const R pp = pxx * pxx + pyy * pyy + pzz * pzz + R(2.0) * (pxy * pxy + pxz * pxz + pyz * pyz);
       const R qs = r_sqrt(R(2.0) * pp);
       const R tauT = R(0.5) * (U.tau0 + r_sqrt(U.tau0sq + U.c18 * qs / rho));
@@ -352,25 +416,27 @@ __device__ __forceinline__ void collide(const Params& P, const Uni<R>& U, uint32
 
   // TRT per opposite pair (src/core/emit/ir.js:304-323), each output blended
   // with the sponge target, mix(a, b, t) = a (1 - t) + b t.
-  if (FAST) emit(0, blend(0, fma_r<R>(-omegaP, g[0] - e[0], g[0])));
-  else emit(0, blend(0, g[0] - omegaP * (g[0] - e[0])));
+  if (FAST) {
+    emit(0, blend(0, fma_r<R>(-omegaP, g[0] - e0, g[0])));
+    const R hP = R(0.5) * omegaP, hM = R(0.5) * omegaM;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      const int i = 2 * k + 1, j = i + 1;
+      const R oi = fma_r<R>(-hM, nd[k], fma_r<R>(-hP, ns[k], g[i]));
+      const R oj = fma_r<R>(hM, nd[k], fma_r<R>(-hP, ns[k], g[j]));
+      emit(i, blend(i, oi));
+      emit(j, blend(j, oj));
+    }
+    return;
+  }
+  emit(0, blend(0, g[0] - omegaP * (g[0] - e0)));
 #pragma unroll
   for (int i = 1; i < Q; i += 2) {
     const int j = i + 1;
     const R p = R(0.5) * ((g[i] + g[j]) - (e[i] + e[j]));
     const R m = R(0.5) * ((g[i] - g[j]) - (e[i] - e[j]));
-    R oi, oj;
-    if (FAST) {
-      const R gp_i = fma_r<R>(-omegaP, p, g[i]);
-      const R gp_j = fma_r<R>(-omegaP, p, g[j]);
-      oi = fma_r<R>(-omegaM, m, gp_i);
-      oj = fma_r<R>(omegaM, m, gp_j);
-    } else {
-      oi = g[i] - omegaP * p - omegaM * m;
-      oj = g[j] - omegaP * p + omegaM * m;
-    }
-    emit(i, blend(i, oi));
-    emit(j, blend(j, oj));
+    emit(i, blend(i, g[i] - omegaP * p - omegaM * m));
+    emit(j, blend(j, g[j] - omegaP * p + omegaM * m));
   }
 }
 

@@ -188,12 +188,14 @@ k_step_inplace(Dev d, Params P, Uni<typename St::real> U) {
           }
         }
       }
-      R delta, rho, ux, uy, uz, uu, rinv;
-      moments<R, FAST>(g, delta, rho, ux, uy, uz, uu, rinv);
+      R delta, rho, ux, uy, uz, uu, rinv = R(0.0);
+      R sp[9], dp[9];
+      if (FAST) moments_fast<R>(g, sp, dp, delta, rho, ux, uy, uz, uu, rinv);
+      else moments_strict<R>(g, delta, rho, ux, uy, uz, uu);
       if (MAC) d.macros[cell] = make_float4((float)ux, (float)uy, (float)uz, (float)delta);
       // g*_i of an odd i goes to the neighbour's slot (E ? i : i+1); g*_{i+1}
       // stays local in slot (E ? i+1 : i); the rest population stays put.
-      collide<R, FAST>(P, U, ct, x, z, g, delta, rho, ux, uy, uz, uu, rinv, [&](int i, R v) {
+      collide<R, FAST>(P, U, ct, x, z, g, sp, dp, delta, rho, ux, uy, uz, uu, rinv, [&](int i, R v) {
         if (i == 0) {
           St::st(Fc, v);
         } else if (i & 1) {
@@ -250,10 +252,12 @@ __global__ void __launch_bounds__(128) k_step_ab(Dev d, Params P, Uni<typename S
           g[i] = St::ld(src + (int64_t)i * N + s);
         }
       }
-      R delta, rho, ux, uy, uz, uu, rinv;
-      moments<R, FAST>(g, delta, rho, ux, uy, uz, uu, rinv);
+      R delta, rho, ux, uy, uz, uu, rinv = R(0.0);
+      R sp[9], dp[9];
+      if (FAST) moments_fast<R>(g, sp, dp, delta, rho, ux, uy, uz, uu, rinv);
+      else moments_strict<R>(g, delta, rho, ux, uy, uz, uu);
       if (MAC) d.macros[cell] = make_float4((float)ux, (float)uy, (float)uz, (float)delta);
-      collide<R, FAST>(P, U, ct, x, z, g, delta, rho, ux, uy, uz, uu, rinv,
+      collide<R, FAST>(P, U, ct, x, z, g, sp, dp, delta, rho, ux, uy, uz, uu, rinv,
                        [&](int i, R v) { St::st(dst + (int64_t)i * N + cell, v); });
     }
   }

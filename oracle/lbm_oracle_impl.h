@@ -132,31 +132,53 @@ void FN(orc_step)(const orc_params* P, int nx, int ny, int nz, const uint32_t* t
           }
         }
 
-        /* blocoMomentos (src/core/emit/ir.js:192-213) */
-        REAL delta = g[0];
-        ORC_UNROLL
-        for (int i = 1; i < ORC_Q; ++i) delta = delta + g[i];
-        const REAL rho = LIT(1.0) + delta;
-        REAL m[3];
-        ORC_UNROLL
-        for (int a = 0; a < 3; ++a) {
-          int first = 1;
-          REAL acc = LIT(0.0);
-          ORC_UNROLL
-          for (int i = 0; i < ORC_Q; ++i) {
-            const int c = ORC_C[i][a];
-            if (c == 0) continue;
-            if (first) { acc = c > 0 ? g[i] : -g[i]; first = 0; }
-            else acc = c > 0 ? acc + g[i] : acc - g[i];
-          }
-          m[a] = acc;
-        }
-        REAL ux, uy, uz, uu, rinv = LIT(0.0);
+        /* blocoMomentos (src/core/emit/ir.js:192-213).  FAST: from the pair
+         * sums s_k = g_i + g_j and differences d_k = g_i - g_j (j = opp i). */
+        REAL sp[9], dp[9];
+        REAL delta, rho, ux, uy, uz, uu, rinv = LIT(0.0);
         if (fast) {
+          ORC_UNROLL
+          for (int k = 0; k < 9; ++k) { sp[k] = g[2 * k + 1] + g[2 * k + 2]; dp[k] = g[2 * k + 1] - g[2 * k + 2]; }
+          delta = g[0];
+          ORC_UNROLL
+          for (int k = 0; k < 9; ++k) delta = delta + sp[k];
+          rho = LIT(1.0) + delta;
+          REAL m[3];
+          ORC_UNROLL
+          for (int a = 0; a < 3; ++a) {
+            int first = 1;
+            REAL acc = LIT(0.0);
+            ORC_UNROLL
+            for (int k = 0; k < 9; ++k) {
+              const int c = ORC_C[2 * k + 1][a];
+              if (c == 0) continue;
+              if (first) { acc = c > 0 ? dp[k] : -dp[k]; first = 0; }
+              else acc = c > 0 ? acc + dp[k] : acc - dp[k];
+            }
+            m[a] = acc;
+          }
           rinv = LIT(1.0) / rho;
           ux = m[0] * rinv; uy = m[1] * rinv; uz = m[2] * rinv;
           uu = ORC_FMA(uz, uz, ORC_FMA(uy, uy, ux * ux));
         } else {
+          delta = g[0];
+          ORC_UNROLL
+          for (int i = 1; i < ORC_Q; ++i) delta = delta + g[i];
+          rho = LIT(1.0) + delta;
+          REAL m[3];
+          ORC_UNROLL
+          for (int a = 0; a < 3; ++a) {
+            int first = 1;
+            REAL acc = LIT(0.0);
+            ORC_UNROLL
+            for (int i = 0; i < ORC_Q; ++i) {
+              const int c = ORC_C[i][a];
+              if (c == 0) continue;
+              if (first) { acc = c > 0 ? g[i] : -g[i]; first = 0; }
+              else acc = c > 0 ? acc + g[i] : acc - g[i];
+            }
+            m[a] = acc;
+          }
           ux = m[0] / rho; uy = m[1] / rho; uz = m[2] / rho;
           uu = ux * ux + uy * uy + uz * uz;
         }
@@ -202,6 +224,77 @@ void FN(orc_step)(const orc_params* P, int nx, int ny, int nz, const uint32_t* t
             const REAL cu = FN(orc_dotc)(i, ux, uy, uz);
             *out[i] = FN(orc_q)(FN(W_)[i] * (LIT(3.0) * cu + LIT(4.5) * cu * cu - LIT(1.5) * uu), storage);
           }
+        } else if (fast) {
+          /* FLUIDO, FAST pair form: e_i + e_j = 2w (delta + rho (4.5 cu^2 - 1.5 uu)),
+           * e_i - e_j = 6 w rho cu; Pi from the pair sums; TRT on the pairs. */
+          const REAL e0 = FN(W_)[0] * ORC_FMA(-rho, uu15, delta);
+          const REAL r6a = (LIT(6.0) * FN(W_)[1]) * rho, r6d = (LIT(6.0) * FN(W_)[7]) * rho;
+          REAL ns[9], nd[9];
+          ORC_UNROLL
+          for (int k = 0; k < 9; ++k) {
+            const int i = 2 * k + 1;
+            const REAL cu = FN(orc_dotc)(i, ux, uy, uz);
+            const REAL a2 = ORC_FMA(LIT(4.5) * cu, cu, -uu15);
+            const REAL es = (LIT(2.0) * FN(W_)[i]) * ORC_FMA(rho, a2, delta);
+            const REAL ed = (i <= 6 ? r6a : r6d) * cu;
+            ns[k] = sp[k] - es;
+            nd[k] = dp[k] - ed;
+          }
+          const REAL tau0 = LIT(1.0) / omegaPlus;
+          REAL omegaP, omegaM;
+          {
+            static const int PA[6] = {0, 1, 2, 0, 0, 1}, PB[6] = {0, 1, 2, 1, 2, 2};
+            REAL pi[6];
+            ORC_UNROLL
+            for (int q = 0; q < 6; ++q) {
+              int first = 1;
+              REAL acc = LIT(0.0);
+              ORC_UNROLL
+              for (int k = 0; k < 9; ++k) {
+                const int coef = ORC_C[2 * k + 1][PA[q]] * ORC_C[2 * k + 1][PB[q]];
+                if (coef == 0) continue;
+                if (first) { acc = coef > 0 ? ns[k] : -ns[k]; first = 0; }
+                else acc = coef > 0 ? acc + ns[k] : acc - ns[k];
+              }
+              pi[q] = acc;
+            }
+            const REAL pd = ORC_FMA(pi[2], pi[2], ORC_FMA(pi[1], pi[1], pi[0] * pi[0]));
+            const REAL po = ORC_FMA(pi[5], pi[5], ORC_FMA(pi[4], pi[4], pi[3] * pi[3]));
+            const REAL pp = ORC_FMA(LIT(2.0), po, pd);
+            const REAL qs = ORC_SQRT(LIT(2.0) * pp);
+            const REAL c18 = LIT(18.0) * lesCs * lesCs;
+            const REAL tauT = LIT(0.5) * (tau0 + ORC_SQRT(ORC_FMA(c18 * qs, rinv, tau0 * tau0)));
+            omegaP = LIT(1.0) / tauT;
+            const REAL tm = tauT - LIT(0.5);
+            omegaM = tm / ORC_FMA(LIT(0.5), tm, magic);
+          }
+          REAL o[ORC_Q];
+          o[0] = ORC_FMA(-omegaP, g[0] - e0, g[0]);
+          const REAL hP = LIT(0.5) * omegaP, hM = LIT(0.5) * omegaM;
+          ORC_UNROLL
+          for (int k = 0; k < 9; ++k) {
+            const int i = 2 * k + 1, j = i + 1;
+            o[i] = ORC_FMA(-hM, nd[k], ORC_FMA(-hP, ns[k], g[i]));
+            o[j] = ORC_FMA(hM, nd[k], ORC_FMA(-hP, ns[k], g[j]));
+          }
+          const REAL sxs = ((REAL)x - spStart) / (spLen > LIT(1.0) ? spLen : LIT(1.0));
+          REAL sigma = sxs > LIT(0.0) ? sxs : LIT(0.0);
+          sigma = sigma < LIT(1.0) ? sigma : LIT(1.0);
+          const REAL sig2 = sigma * sigma;
+          if (sig2 != LIT(0.0)) {
+            const REAL uuInf = ORC_FMA(inz, inz, ORC_FMA(iny, iny, inx * inx));
+            const REAL uuInf15 = LIT(1.5) * uuInf;
+            const REAL oms = LIT(1.0) - sig2;
+            ORC_UNROLL
+            for (int i = 0; i < ORC_Q; ++i) {
+              const REAL si = i == 0 ? LIT(0.0) : FN(orc_dotc)(i, inx, iny, inz);
+              const REAL t = i == 0 ? FN(W_)[0] * (-uuInf15)
+                                    : FN(W_)[i] * ORC_FMA(si, ORC_FMA(LIT(4.5), si, LIT(3.0)), -uuInf15);
+              o[i] = ORC_FMA(t, sig2, o[i] * oms);
+            }
+          }
+          ORC_UNROLL
+          for (int i = 0; i < ORC_Q; ++i) *out[i] = FN(orc_q)(o[i], storage);
         } else {
           /* FLUIDO: blocoEquilibrio, blocoLES, blocoColisao, blocoEsponja */
           REAL e[ORC_Q];
