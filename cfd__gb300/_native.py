@@ -48,6 +48,13 @@ class Info(C.Structure):
                 ("flags", C.c_int32), ("steps", C.c_int64), ("parity", C.c_int32), ("block_x", C.c_int32)]
 
 
+class VoxStats(C.Structure):
+    _fields_ = [("n_cells", C.c_int64), ("n_casca", C.c_int64), ("n_dentro", C.c_int64), ("n_solido", C.c_int64),
+                ("triangulo_fora", C.c_int64), ("oco_suspeito", C.c_int32), ("flood_iterations", C.c_int32),
+                ("n_pairs", C.c_int64), ("n_deferred", C.c_int64), ("ms_raster", C.c_float),
+                ("ms_flood", C.c_float), ("ms_total", C.c_float), ("_pad", C.c_float)]
+
+
 _lib = None
 _lock = threading.Lock()
 
@@ -71,6 +78,9 @@ SIGNATURES = {
     "lbm_get_info": (C.c_int, [C.c_void_p, C.POINTER(Info)]),
     "lbm_last_error": (C.c_char_p, []),
     "lbm_set_block": (C.c_int, [C.c_void_p, C.c_int]),
+    "lbm_set_launch": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "vox_voxelize": (C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.POINTER(Dims), C.c_float, C.c_int,
+                               C.c_void_p, C.c_void_p, C.POINTER(VoxStats)]),
 }
 
 

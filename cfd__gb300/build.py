@@ -35,6 +35,7 @@ UNITS = {
     "lbm_inst_f64.cu": ["-fmad=false"],
     "lbm_inst_f16s.cu": ["-fmad=false"],
     "lbm_inst_bf16s.cu": ["-fmad=false"],
+    "vox.cu": ["-fmad=false"],
 }
 
 

@@ -114,6 +114,7 @@ struct lbm_ctx {
   bool configured = false, types_set = false, state_set = false;
   int64_t steps = 0;
   int block_x = 0, block_y = 1;
+  int occ = 8;
   int64_t dev_bytes = 0;
 };
 
@@ -139,6 +140,7 @@ Launch cell_launch(const lbm_ctx* c) {
   int by = c->block_y > 0 ? c->block_y : 1;
   while (bx * by > 128) by = std::max(1, by / 2);
   Launch L;
+  L.occ = c->occ;
   L.block = dim3(bx, by, 1);
   L.grid = dim3((c->dims.nx + bx - 1) / bx, (c->dims.ny + by - 1) / by, c->dims.nz);
   return L;
@@ -214,6 +216,9 @@ int launch_step(lbm_ctx* c, bool mac, double* force) {
 extern "C" {
 
 const char* lbm_last_error(void) { return g_err.c_str(); }
+
+// Shared error channel for the other units of the library (voxelizer).
+int lbm_internal_fail(int code, const char* msg) { return fail(code, msg); }
 
 int lbm_create(const lbm_dims* dims, int storage, int flags, lbm_ctx** out) {
   if (!dims || !out) return fail(LBM_EINVAL, "null argument");
@@ -452,6 +457,15 @@ int lbm_get_info(lbm_ctx* c, lbm_info* info) {
   info->steps = c->steps;
   info->parity = (int)(c->steps & 1);
   info->block_x = (int)cell_launch(c).block.x;
+  return LBM_OK;
+}
+
+int lbm_set_launch(lbm_ctx* c, int block_x, int min_blocks) {
+  if (!c) return fail(LBM_EINVAL, "null context");
+  if (min_blocks != 0 && min_blocks != 6 && min_blocks != 8) return fail(LBM_EINVAL, "min_blocks must be 0, 6 or 8");
+  int r = lbm_set_block(c, block_x);
+  if (r) return r;
+  c->occ = min_blocks == 0 ? 8 : min_blocks;
   return LBM_OK;
 }
 

@@ -128,8 +128,10 @@ struct Deltas {
 // In-place step.  Grid: (ceil(nx/bx), ceil(ny/by), nz), block (bx, by).
 // PAR: step parity (0 even).  MAC: write (u, delta).  FRC: accumulate the
 // momentum-exchange force of the state being streamed.
-template <class St, int PAR, bool MAC, bool FRC, bool W64, bool FAST>
-__global__ void __launch_bounds__(128, sizeof(typename St::real) == 8 ? 4 : ((FRC || MAC) ? 6 : 8))
+// MINB: minimum resident 128-thread blocks per SM the register allocation
+// must allow (8 -> 64 registers, 6 -> 80); the autotuner picks per form.
+template <class St, int PAR, bool MAC, bool FRC, bool W64, bool FAST, int MINB>
+__global__ void __launch_bounds__(128, MINB)
 k_step_inplace(Dev d, Params P, Uni<typename St::real> U) {
   using R = typename St::real;
   using S = typename St::store_t;
@@ -439,6 +441,7 @@ __global__ void k_mass(Dev d, int parity, double* partials) {
 // ---------------------------------------------------------------- launchers
 struct Launch {
   dim3 grid, block;
+  int occ = 8;   // register-cap variant of the plain in-place step (8 or 6)
 };
 
 struct Ops {
@@ -460,10 +463,16 @@ struct OpsImpl {
   static constexpr bool kFastOK = sizeof(R) == 4;
   template <int PAR, bool MAC, bool FRC, bool FAST>
   static void go_inplace(const Dev& d, const Params& P, const Uni<R>& U, Launch L, cudaStream_t s) {
-    if ((int64_t)Q * d.N < (int64_t)INT32_MAX)
-      k_step_inplace<St, PAR, MAC, FRC, false, FAST><<<L.grid, L.block, 0, s>>>(d, P, U);
-    else
-      k_step_inplace<St, PAR, MAC, FRC, true, FAST><<<L.grid, L.block, 0, s>>>(d, P, U);
+    constexpr int kDefault = sizeof(R) == 8 ? 4 : ((FRC || MAC) ? 6 : 8);
+    const bool w64 = (int64_t)Q * d.N >= (int64_t)INT32_MAX;
+    // the plain hot-loop variant also exists with a looser register cap
+    if (!MAC && !FRC && sizeof(R) == 4 && L.occ == 6) {
+      if (w64) k_step_inplace<St, PAR, MAC, FRC, true, FAST, 6><<<L.grid, L.block, 0, s>>>(d, P, U);
+      else k_step_inplace<St, PAR, MAC, FRC, false, FAST, 6><<<L.grid, L.block, 0, s>>>(d, P, U);
+      return;
+    }
+    if (w64) k_step_inplace<St, PAR, MAC, FRC, true, FAST, kDefault><<<L.grid, L.block, 0, s>>>(d, P, U);
+    else k_step_inplace<St, PAR, MAC, FRC, false, FAST, kDefault><<<L.grid, L.block, 0, s>>>(d, P, U);
   }
   template <bool FAST>
   static void go(const Dev& d, const Params& P, const Uni<R>& U, int parity, bool inplace, bool mac, bool frc,

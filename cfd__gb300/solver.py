@@ -226,8 +226,10 @@ class SolverCUDA:
     def definirStream(self, cuda_stream_ptr: int):
         nat.check(self._lib.lbm_set_stream(self._h, C.c_void_p(cuda_stream_ptr)))
 
-    def definirBloco(self, block_x: int):
-        nat.check(self._lib.lbm_set_block(self._h, int(block_x)))
+    def definirBloco(self, block_x: int, min_blocos: int = 0):
+        """Launch shape of the step kernel: threads along x per block and the
+        register-cap variant (min resident blocks per SM: 8 or 6; 0 = default)."""
+        nat.check(self._lib.lbm_set_launch(self._h, int(block_x), int(min_blocos)))
 
     def info(self):
         i = nat.Info()

@@ -182,6 +182,10 @@ const char* lbm_last_error(void);
  * autotuned).  Used by the autotuner and the benchmark sweep. */
 int lbm_set_block(lbm_ctx* ctx, int block_x);
 
+/* Launch shape plus register-cap variant of the plain step kernel:
+ * min_blocks = 8 (64 registers/thread), 6 (80) or 0 (default 8). */
+int lbm_set_launch(lbm_ctx* ctx, int block_x, int min_blocks);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,50 @@
+"""GPU voxelizer vs the CPU restatement of src/geom/voxel.js: classes bit
+for bit, statistics equal, signed distance within fp32 rounding."""
+import numpy as np
+import pytest
+
+from tests import vox_cases as V
+
+pytestmark = pytest.mark.gpu
+
+CASES = {
+    "config2_superellipsoid": V.config2,
+    "cube_example_24": lambda: V.cube_example(),
+    "aligned_cube_ties": lambda: V.aligned_cube({"nx": 40, "ny": 36, "nz": 30}),
+    "sphere": lambda: V.sphere_mesh({"nx": 48, "ny": 48, "nz": 48}, r=12.0),
+    "sphere_hole": lambda: V.sphere_mesh({"nx": 48, "ny": 48, "nz": 48}, r=12.0, hole=(12, 1, 10, 2)),
+    "soup": lambda: V.soup({"nx": 56, "ny": 40, "nz": 44}),
+    "plate": lambda: V.plate({"nx": 40, "ny": 32, "nz": 24}),
+}
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+@pytest.mark.parametrize("seal", [True, False])
+def test_voxelize_bit_exact(native, orc, name, seal):
+    from cfd__gb300.voxel import voxelizar
+    pos, idx, g = CASES[name]()
+    dims = (g["nx"], g["ny"], g["nz"])
+    got = voxelizar(pos, idx, g, banda=1.5, selarFrestas=seal)
+    want_t, want_sdf, want_st = orc.voxelize(pos, idx, dims, banda=1.5, selar=seal)
+    assert np.array_equal(got["tipo"], want_t), f"{name}: {(got['tipo'] != want_t).sum()} voxels differ"
+    st = got["stats"]
+    assert st["nCasca"] == want_st["n_casca"] and st["nDentro"] == want_st["n_dentro"]
+    assert st["trianguloFora"] == want_st["triangulo_fora"]
+    assert st["ocoSuspeito"] == bool(want_st["oco_suspeito"])
+    # the band distance is computed in fp32 on the GPU, fp64 then rounded in the reference
+    np.testing.assert_allclose(got["sdf"], want_sdf, rtol=2e-6, atol=2e-6)
+
+
+def test_aligned_cube_uses_the_fp64_path(native):
+    from cfd__gb300.voxel import voxelizar
+    pos, idx, g = V.aligned_cube({"nx": 40, "ny": 36, "nz": 30})
+    st = voxelizar(pos, idx, g)["stats"]
+    assert st["paresFp64"] > 0
+
+
+def test_bad_index_is_rejected(native):
+    from cfd__gb300 import LbmError
+    from cfd__gb300.voxel import voxelizar
+    pos = np.zeros((3, 3), np.float32)
+    with pytest.raises(LbmError):
+        voxelizar(pos, np.array([[0, 1, 5]], np.uint32), {"nx": 8, "ny": 8, "nz": 8})
