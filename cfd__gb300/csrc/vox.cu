@@ -242,6 +242,7 @@ __global__ void k_raster(const Tri* __restrict__ tris, int ntri, int nx, int ny,
   const int bx = T.box[3] - T.box[0] + 1, by = T.box[4] - T.box[1] + 1, bz = T.box[5] - T.box[2] + 1;
   const long long nvox = (long long)bx * by * bz;
   if (lane == 0) atomicAdd(npairs, (unsigned long long)nvox);
+  if (T.kappa < 0.0f) return;   // ill-conditioned triangle: k_raster_f64 takes all of it
   const float* a = T.v;
   const float* b = T.v + 3;
   const float* c = T.v + 6;
@@ -260,8 +261,8 @@ __global__ void k_raster(const Tri* __restrict__ tris, int ntri, int nx, int ny,
 #pragma unroll
     for (int q = 0; q < 3; ++q) V = fmaxf(V, fmaxf(fabsf(la[q]), fmaxf(fabsf(lb[q]), fabsf(lc[q]))));
     const float Vs = V + 1.0f;
-    bool defer = T.kappa < 0.0f;
-    if (!defer) {
+    bool defer = false;
+    {
       // d2 error: the point-triangle distance conditions like the triangle's
       // shape (kappa); 128 u kappa (6 Vs)^2 covers the branch that divides.
       const float bd2 = 128.0f * kU * T.kappa * 36.0f * Vs * Vs;
@@ -305,6 +306,34 @@ __global__ void k_tiebreak(const Tri* __restrict__ tris, const Deferred* __restr
 __global__ void k_fill_u32(unsigned* __restrict__ p, unsigned v, long long n) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) p[i] = v;
+}
+
+// Ill-conditioned triangles (slivers, near-degenerate): the whole banded box
+// in the reference's fp64 arithmetic, distance band included.
+__global__ void k_raster_f64(const Tri* __restrict__ tris, const int* __restrict__ list, int n, int nx, int ny,
+                             uint8_t* __restrict__ flags, unsigned* __restrict__ dist2) {
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= n) return;
+  const Tri& T = tris[list[warp]];
+  const int bx = T.box[3] - T.box[0] + 1, by = T.box[4] - T.box[1] + 1, bz = T.box[5] - T.box[2] + 1;
+  const long long nvox = (long long)bx * by * bz;
+  const double a[3] = {T.v[0], T.v[1], T.v[2]}, b[3] = {T.v[3], T.v[4], T.v[5]}, c[3] = {T.v[6], T.v[7], T.v[8]};
+  for (long long k = lane; k < nvox; k += 32) {
+    const int x = T.box[0] + (int)(k % bx);
+    const int y = T.box[1] + (int)((k / bx) % by);
+    const int z = T.box[2] + (int)(k / ((long long)bx * by));
+    const long long cell = ((long long)z * ny + y) * nx + x;
+    const double p[3] = {x + 0.5, y + 0.5, z + 0.5};
+    const double d2 = dist2_f64(p, a, b, c);
+    if (d2 >= 0.0) atomicMin(dist2 + cell, __float_as_uint((float)d2));
+    if (d2 <= 0.75) {
+      const double la[3] = {a[0] - p[0], a[1] - p[1], a[2] - p[2]};
+      const double lb[3] = {b[0] - p[0], b[1] - p[1], b[2] - p[2]};
+      const double lc[3] = {c[0] - p[0], c[1] - p[1], c[2] - p[2]};
+      if (tri_box_f64(la, lb, lc)) flags[cell] = 1;
+    }
+  }
 }
 
 // ---- 1-bit rows: word w of row (y, z) holds x = 32 w .. 32 w + 31
@@ -546,7 +575,9 @@ extern "C" int vox_voxelize(const float* pos, size_t nvert, const uint32_t* idx,
     const double A = cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2];
     const double L = (ab[0] * ab[0] + ab[1] * ab[1] + ab[2] * ab[2]) * (ac[0] * ac[0] + ac[1] * ac[1] + ac[2] * ac[2]);
     const double kappa = A > 0 ? L / A : INFINITY;
-    T.kappa = (kappa <= 1e4) ? (float)std::max(1.0, kappa) : -1.0f;   // -1: every pair in fp64
+    // shape factor above 16: the fp32 distance loses too many digits; such
+    // triangles (slivers, near-degenerate) go to the fp64 kernel whole
+    T.kappa = (kappa <= 16.0) ? (float)std::max(1.0, kappa) : -1.0f;
     T.id = (int)t;
     tris.push_back(T);
   }
@@ -593,6 +624,23 @@ extern "C" int vox_voxelize(const float* pos, size_t nvert, const uint32_t* idx,
   k_fill_u32<<<blocks(N, 256), 256, 0, st>>>(d_dist2, 0x7f800000u, N);   // +inf (Float32Array.fill(Infinity))
   VCK(cudaMemsetAsync(d_cnt, 0, 4 * sizeof(unsigned long long), st), "clear");
   const int ntr = (int)tris.size();
+  std::vector<int> f64list;
+  long long f64pairs = 0;
+  for (int t = 0; t < ntr; ++t)
+    if (tris[t].kappa < 0.0f) {
+      f64list.push_back(t);
+      f64pairs += (long long)(tris[t].box[3] - tris[t].box[0] + 1) * (tris[t].box[4] - tris[t].box[1] + 1) *
+                  (tris[t].box[5] - tris[t].box[2] + 1);
+    }
+  int* d_f64 = nullptr;
+  VCK(mem.alloc(&d_f64, sizeof(int) * std::max<size_t>(1, f64list.size())), "fp64 triangle list");
+  if (!f64list.empty()) {
+    VCK(cudaMemcpyAsync(d_f64, f64list.data(), sizeof(int) * f64list.size(), cudaMemcpyHostToDevice, st),
+        "fp64 list upload");
+    k_raster_f64<<<blocks((long long)f64list.size() * 32, 128), 128, 0, st>>>(d_tris, d_f64, (int)f64list.size(),
+                                                                           nx, ny, d_flags, d_dist2);
+    VCK(cudaGetLastError(), "fp64 raster launch");
+  }
   if (ntr > 0) {
     k_raster<<<blocks((long long)ntr * 32, 128), 128, 0, st>>>(d_tris, ntr, nx, ny, d_flags, d_dist2, d_def, d_cnt,
                                                                cap, d_cnt + 1);
@@ -661,7 +709,7 @@ extern "C" int vox_voxelize(const float* pos, size_t nvert, const uint32_t* idx,
     stats->oco_suspeito = ((double)stats->n_dentro < (double)stats->n_casca * 0.25) && stats->n_casca > 500;
     stats->flood_iterations = passes;
     stats->n_pairs = (long long)h_cnt[1];
-    stats->n_deferred = ndef;
+    stats->n_deferred = ndef + f64pairs;
     cudaEventElapsedTime(&stats->ms_raster, ev[0], ev[1]);
     cudaEventElapsedTime(&stats->ms_flood, ev[1], ev[2]);
     cudaEventElapsedTime(&stats->ms_total, ev[0], ev[3]);

@@ -31,8 +31,9 @@ def test_voxelize_bit_exact(native, orc, name, seal):
     assert st["nCasca"] == want_st["n_casca"] and st["nDentro"] == want_st["n_dentro"]
     assert st["trianguloFora"] == want_st["triangulo_fora"]
     assert st["ocoSuspeito"] == bool(want_st["oco_suspeito"])
-    # the band distance is computed in fp32 on the GPU, fp64 then rounded in the reference
-    np.testing.assert_allclose(got["sdf"], want_sdf, rtol=2e-6, atol=2e-6)
+    # the band distance is computed in fp32 on the GPU (fp64 for ill-shaped
+    # triangles), fp64 then rounded to fp32 in the reference
+    np.testing.assert_allclose(got["sdf"], want_sdf, rtol=1e-5, atol=1e-5)
 
 
 def test_aligned_cube_uses_the_fp64_path(native):
