@@ -39,19 +39,24 @@ U_IN, RE, LEN, CS = 0.06, 2000.0, 96.0, 0.12
 BYTES_PER_CELL = {"f32": 152, "f16s": 76, "bf16s": 76, "f64": 304}
 
 
-def workload(body="mesh"):
-    """Cell types and parameters of the 320x160x128 mesh-body tunnel."""
+def workload(body="mesh", cpu_voxelizer=False):
+    """Cell types and parameters of the 320x160x128 mesh-body tunnel.  The
+    reference arm voxelizes with the CPU restatement, ours on the GPU (the
+    two give identical masks)."""
     from cfd__gb300.tunel import montarTipos
 
     nu = U_IN * LEN / RE
     omega = 1.0 / (3.0 * nu + 0.5)
     if body == "mesh":
         from cfd__gb300.geometry import corpo_config2
-        from cfd__gb300.voxel import voxelizar
         pos, idx = corpo_config2(GRID)
-        vox = voxelizar(pos, idx, GRID)
-        corpo = vox["tipo"]
-        desc = "voxelized superellipsoid mesh 48x20x14 cells, 20k triangles, 0.3-cell jitter (GPU voxelizer)"
+        if cpu_voxelizer:
+            from oracle import oracle as O
+            corpo = O.voxelize(pos, idx, (GRID["nx"], GRID["ny"], GRID["nz"]), with_sdf=False)[0]
+        else:
+            from cfd__gb300.voxel import voxelizar
+            corpo = voxelizar(pos, idx, GRID, sdf=False)["tipo"]
+        desc = "voxelized superellipsoid mesh 48x20x14 cells, 20k triangles, 0.3-cell jitter"
     else:
         from cfd__gb300.geometry import mascara_analitica
         corpo = mascara_analitica(GRID, 48, 20, 14, 2.5, 3.0, (0.28 * 320 + 48, 80, 3 + 14))
@@ -209,7 +214,7 @@ def run_reference(args):
     world, rank, local = dist_setup()
     if rank != 0:
         return 0
-    tipo, cfg, desc = workload(body="analytic")
+    tipo, cfg, desc = workload(body=args.body, cpu_voxelizer=True)
     res = []
     for _ in range(args.warmup):
         pass
