@@ -79,6 +79,7 @@ SIGNATURES = {
     "lbm_last_error": (C.c_char_p, []),
     "lbm_set_block": (C.c_int, [C.c_void_p, C.c_int]),
     "lbm_set_launch": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "lbm_forces_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(Dims), C.c_void_p, C.c_void_p]),
     "vox_voxelize": (C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.POINTER(Dims), C.c_float, C.c_int,
                                C.c_void_p, C.c_void_p, C.POINTER(VoxStats)]),
 }

@@ -36,6 +36,7 @@ UNITS = {
     "lbm_inst_f16s.cu": ["-fmad=false"],
     "lbm_inst_bf16s.cu": ["-fmad=false"],
     "vox.cu": ["-fmad=false"],
+    "lbm_noalloc.cu": ["-fmad=false"],
 }
 
 
