@@ -115,6 +115,7 @@ struct lbm_ctx {
   int64_t steps = 0;
   int block_x = 0, block_y = 1;
   int occ = 8;
+  int pipe = 0;
   int64_t dev_bytes = 0;
 };
 
@@ -141,6 +142,7 @@ Launch cell_launch(const lbm_ctx* c) {
   while (bx * by > 128) by = std::max(1, by / 2);
   Launch L;
   L.occ = c->occ;
+  L.pipe = c->pipe;
   L.block = dim3(bx, by, 1);
   L.grid = dim3((c->dims.nx + bx - 1) / bx, (c->dims.ny + by - 1) / by, c->dims.nz);
   return L;
@@ -462,10 +464,15 @@ int lbm_get_info(lbm_ctx* c, lbm_info* info) {
 
 int lbm_set_launch(lbm_ctx* c, int block_x, int min_blocks) {
   if (!c) return fail(LBM_EINVAL, "null context");
-  if (min_blocks != 0 && min_blocks != 6 && min_blocks != 8) return fail(LBM_EINVAL, "min_blocks must be 0, 6 or 8");
+  // min_blocks 4/8/16 with block_x = 64 selects the pipelined step with that
+  // many cells per thread along z
+  if (min_blocks != 0 && min_blocks != 6 && min_blocks != 8 && min_blocks != 104 && min_blocks != 108 &&
+      min_blocks != 116)
+    return fail(LBM_EINVAL, "min_blocks must be 0, 6, 8, or 100 + cells per thread (4, 8, 16) for the pipelined step");
   int r = lbm_set_block(c, block_x);
   if (r) return r;
-  c->occ = min_blocks == 0 ? 8 : min_blocks;
+  if (min_blocks >= 100) { c->pipe = min_blocks - 100; c->occ = 8; }
+  else { c->pipe = 0; c->occ = min_blocks == 0 ? 8 : min_blocks; }
   return LBM_OK;
 }
 

@@ -448,6 +448,8 @@ struct StF32 {
   static __device__ __forceinline__ float ld(const float* p) { return *p; }
   static __device__ __forceinline__ void st(float* p, float v) { *p = v; }
   static __device__ __forceinline__ float from_double(double v) { return (float)v; }
+  // value from the aligned 32-bit word a pipelined copy brought in
+  static __device__ __forceinline__ float from_word(uint32_t w, uint32_t) { return __uint_as_float(w); }
 };
 struct StF64 {
   using store_t = double;
@@ -464,6 +466,9 @@ struct StF16S {
   static __device__ __forceinline__ float ld(const uint16_t* p) {
     return __half2float(__ushort_as_half(*p)) * (1.0f / 1024.0f);
   }
+  static __device__ __forceinline__ float from_word(uint32_t w, uint32_t shift) {
+    return __half2float(__ushort_as_half((unsigned short)(w >> shift))) * (1.0f / 1024.0f);
+  }
   static __device__ __forceinline__ void st(uint16_t* p, float v) {
     *p = __half_as_ushort(__float2half_rn(v * 1024.0f));
   }
@@ -474,6 +479,9 @@ struct StBF16S {
   using real = float;
   static __device__ __forceinline__ float ld(const uint16_t* p) {
     return __bfloat162float(__ushort_as_bfloat16(*p));
+  }
+  static __device__ __forceinline__ float from_word(uint32_t w, uint32_t shift) {
+    return __bfloat162float(__ushort_as_bfloat16((unsigned short)(w >> shift)));
   }
   static __device__ __forceinline__ void st(uint16_t* p, float v) {
     *p = __bfloat16_as_ushort(__float2bfloat16_rn(v));

@@ -438,10 +438,135 @@ __global__ void k_mass(Dev d, int parity, double* partials) {
   block_partials3(m, 0.0, 0.0, partials);
 }
 
+// ------------------------------------------------- pipelined in-place step
+// The same step as k_step_inplace, with load latency hidden by software
+// pipelining: each thread walks KZ cells along z; while it collides cell k,
+// the 19 populations of cell k+1 are already in flight into its own shared
+// memory slots (cp.async, one 4-byte copy per population, so no registers
+// are held by the outstanding loads).  The prefetch takes the normal slots of
+// the parity; a link whose upstream cell is solid (bounce-back, rare) is
+// re-read directly from its bounce-back slot at collide time.  Every
+// (slot, location) a cell touches belongs to that cell alone in this step, so
+// prefetching cell k+1 before cell k's stores is race-free.
+// 16-bit forms copy the aligned 32-bit word holding the element.
+__device__ __forceinline__ void cp_async4(uint32_t saddr, const void* g) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(saddr), "l"(g) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+template <class St, int PAR, bool FAST, int KZ, int BX>
+__global__ void __launch_bounds__(BX, 768 / BX) k_step_pipe(Dev d, Params P, Uni<typename St::real> U) {
+  using R = typename St::real;
+  using S = typename St::store_t;
+  using Off = int32_t;
+  static_assert(sizeof(S) <= 4, "pipelined step: 32-bit or 16-bit storage");
+  __shared__ uint32_t buf[2][Q][BX];
+  const int tid = threadIdx.x;
+  const int x = blockIdx.x * BX + tid;
+  const int y = blockIdx.y;
+  const int z0 = blockIdx.z * KZ;
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  const bool xin = x < nx;
+  const int zend = min(z0 + KZ, nz);
+  const Off N = (Off)d.N;
+  const Off nxny = (Off)nx * ny;
+  S* const F = static_cast<S*>(d.pop);
+  constexpr bool E = (PAR == 0);
+
+  // issue the normal-slot copies of cell (x, y, z) into stage st
+  auto prefetch = [&](int z, int st) {
+    const Off cell = (Off)z * nxny + (Off)y * nx + x;
+    const Deltas<Off> D(x, y, z, nx, ny, nz);
+    const uint32_t base = (uint32_t)__cvta_generic_to_shared(&buf[st][0][tid]);
+    auto copy = [&](int k, Off e) {
+      const S* p = F + e;
+      const char* a = reinterpret_cast<const char*>(p);
+      if (sizeof(S) == 2) a -= (reinterpret_cast<uintptr_t>(a) & 2u);
+      cp_async4(base + (uint32_t)(k * BX * 4), a);
+    };
+    copy(0, cell);
+#pragma unroll
+    for (int i = 1; i < Q; i += 2) {
+      copy(i, cell + (Off)(E ? i + 1 : i) * N);
+      copy(i + 1, cell + D.odd(i) + (Off)(E ? i : i + 1) * N);
+    }
+  };
+  auto word_shift = [&](Off e) -> uint32_t {
+    return sizeof(S) == 2 ? (uint32_t)((reinterpret_cast<uintptr_t>(F + e) & 2u) << 3) : 0u;
+  };
+
+  if (!xin) return;
+  uint32_t lw_next = __ldg(d.link + (Off)z0 * nxny + (Off)y * nx + x);
+  bool pf = !is_solid((lw_next >> LINK_CLASS_SHIFT) & 7u);
+  if (pf) prefetch(z0, 0);
+  cp_async_commit();
+  for (int z = z0; z < zend; ++z) {
+    const int st = (z - z0) & 1;
+    const uint32_t lw = lw_next;
+    const bool have = pf;
+    if (z + 1 < zend) {
+      lw_next = __ldg(d.link + (Off)(z + 1) * nxny + (Off)y * nx + x);
+      pf = !is_solid((lw_next >> LINK_CLASS_SHIFT) & 7u);
+      if (pf) prefetch(z + 1, st ^ 1);
+    }
+    cp_async_commit();
+    cp_async_wait<1>();          // this cell's copies have landed
+    if (!have) continue;         // solid: nothing to do (macros are not written here)
+    const uint32_t ct = (lw >> LINK_CLASS_SHIFT) & 7u;
+    const Off cell = (Off)z * nxny + (Off)y * nx + x;
+    const Deltas<Off> D(x, y, z, nx, ny, nz);
+    R g[Q];
+    g[0] = St::from_word(buf[st][0][tid], word_shift(cell));
+#pragma unroll
+    for (int i = 1; i < Q; i += 2) {
+      const Off ei = cell + (Off)(E ? i + 1 : i) * N;
+      const Off ej = cell + D.odd(i) + (Off)(E ? i : i + 1) * N;
+      g[i] = St::from_word(buf[st][i][tid], word_shift(ei));
+      g[i + 1] = St::from_word(buf[st][i + 1][tid], word_shift(ej));
+    }
+    const uint32_t bbmask = lw & 0x3ffffu;
+    if (bbmask) {
+      // bounce-back links: the other slot of the same location
+#pragma unroll
+      for (int i = 1; i < Q; i += 2) {
+        if ((bbmask >> (i - 1)) & 1u) g[i] = St::ld(F + cell + (Off)(E ? i : i + 1) * N);
+        if ((bbmask >> i) & 1u) g[i + 1] = St::ld(F + cell + D.odd(i) + (Off)(E ? i + 1 : i) * N);
+      }
+      if (lw & LINK_SLOW) {
+        const Wrap w = wrap3(x, y, z, nx, ny, nz);
+#pragma unroll
+        for (int k = 1; k < Q; ++k) {
+          if (!((bbmask >> (k - 1)) & 1u)) continue;
+          if (d.tipo[nbr(k, -1, x, y, z, w, nx, ny)] == SOLIDO_MOVEL)
+            g[k] = g[k] + Lit<R>::sixw(k) * (dotc<R>(k, R(P.belt[0]), R(P.belt[1]), R(P.belt[2])));
+        }
+      }
+    }
+    R delta, rho, ux, uy, uz, uu, rinv = R(0.0);
+    R sp[9], dp[9];
+    if (FAST) moments_fast<R>(g, sp, dp, delta, rho, ux, uy, uz, uu, rinv);
+    else moments_strict<R>(g, delta, rho, ux, uy, uz, uu);
+    S* const Fc = F + cell;
+    collide<R, FAST>(P, U, ct, x, z, g, sp, dp, delta, rho, ux, uy, uz, uu, rinv, [&](int i, R v) {
+      if (i == 0) {
+        St::st(Fc, v);
+      } else if (i & 1) {
+        St::st(Fc + D.odd(i) + (Off)(E ? i : i + 1) * N, v);
+      } else {
+        St::st(Fc + (Off)(E ? i : i - 1) * N, v);
+      }
+    });
+  }
+  cp_async_wait<0>();
+}
+
 // ---------------------------------------------------------------- launchers
 struct Launch {
   dim3 grid, block;
   int occ = 8;   // register-cap variant of the plain in-place step (8 or 6)
+  int pipe = 0;  // > 0: pipelined step, cells per thread along z (4, 8, 16)
 };
 
 struct Ops {
@@ -465,6 +590,15 @@ struct OpsImpl {
   static void go_inplace(const Dev& d, const Params& P, const Uni<R>& U, Launch L, cudaStream_t s) {
     constexpr int kDefault = sizeof(R) == 8 ? 4 : ((FRC || MAC) ? 6 : 8);
     const bool w64 = (int64_t)Q * d.N >= (int64_t)INT32_MAX;
+    if constexpr (!MAC && !FRC && sizeof(typename St::store_t) <= 4) {
+      if (L.pipe > 0 && !w64) {
+        const dim3 grid((d.nx + 63) / 64, d.ny, (d.nz + L.pipe - 1) / L.pipe);
+        if (L.pipe == 4) k_step_pipe<St, PAR, FAST, 4, 64><<<grid, 64, 0, s>>>(d, P, U);
+        else if (L.pipe == 8) k_step_pipe<St, PAR, FAST, 8, 64><<<grid, 64, 0, s>>>(d, P, U);
+        else k_step_pipe<St, PAR, FAST, 16, 64><<<grid, 64, 0, s>>>(d, P, U);
+        return;
+      }
+    }
     // the plain hot-loop variant also exists with a looser register cap
     if (!MAC && !FRC && sizeof(R) == 4 && L.occ == 6) {
       if (w64) k_step_inplace<St, PAR, MAC, FRC, true, FAST, 6><<<L.grid, L.block, 0, s>>>(d, P, U);

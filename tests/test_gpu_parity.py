@@ -173,3 +173,26 @@ def test_rest_offset_on_zero_state(native):
     s.definirTipos(t.reshape(-1))
     off2 = s.calibrarRepouso()
     assert off2[2] != 0.0
+
+
+@pytest.mark.parametrize("storage", ["f32", "f16s", "bf16s"])
+@pytest.mark.parametrize("strict", [False, True])
+@pytest.mark.parametrize("kz", [4, 8, 16])
+def test_pipelined_step_equals_plain_step(native, storage, strict, kz):
+    """The software-pipelined step (cp.async prefetch along z) is the same
+    arithmetic as the plain step: states must be identical."""
+    grade, tipo, esp = all_types_tunnel(nx=70, ny=20, nz=37)
+    cfg = _cfg(esp)
+    g0 = random_state(int(np.prod(list(grade.values()))), seed=3)
+    a = _solver(grade, storage, strict=strict)
+    b = _solver(grade, storage, strict=strict)
+    b.definirBloco(64, 100 + kz)
+    for s in (a, b):
+        s.definirTipos(tipo)
+        s.configurar(**cfg)
+        s.definirPopulacoes(g0)
+    for n in (1, 2, 9):
+        a.passo(n)
+        b.passo(n)
+        fl = _fluid(tipo)
+        assert np.array_equal(a.lerPopulacoes()[:, fl], b.lerPopulacoes()[:, fl]), (storage, strict, kz, a.passos)
