@@ -145,24 +145,32 @@ k_step_inplace(Dev d, Params P, Uni<typename St::real> U) {
   if (in) {
     const Off N = (Off)d.N;
     const Off cell = ((Off)z * ny + y) * nx + x;
+    // The normal-slot loads do not wait for the link word: they are issued
+    // together with it, and the rare bounce-back links are re-read below.
     const uint32_t lw = __ldg(d.link + cell);
+    S* const Fc = static_cast<S*>(d.pop) + cell;
+    const Deltas<Off> D(x, y, z, nx, ny, d.nz);
+    constexpr bool E = (PAR == 0);
+    R g[Q];
+    g[0] = St::ld(Fc);
+#pragma unroll
+    for (int i = 1; i < Q; i += 2) {
+      g[i] = St::ld(Fc + (Off)(E ? i + 1 : i) * N);
+      g[i + 1] = St::ld(Fc + D.odd(i) + (Off)(E ? i : i + 1) * N);
+    }
     const uint32_t ct = (lw >> LINK_CLASS_SHIFT) & 7u;
     if (is_solid(ct)) {
       if (MAC) d.macros[cell] = make_float4(0.f, 0.f, 0.f, 0.f);
     } else {
-      S* const Fc = static_cast<S*>(d.pop) + cell;
-      const Deltas<Off> D(x, y, z, nx, ny, d.nz);
-      constexpr bool E = (PAR == 0);
-      R g[Q];
-      g[0] = St::ld(Fc);
+      {
+        const uint32_t bb = lw & 0x3ffffu;
+        if (bb) {
 #pragma unroll
-      for (int i = 1; i < Q; i += 2) {
-        const bool bbi = (lw >> (i - 1)) & 1u;   // x - c_i is solid
-        const bool bbj = (lw >> i) & 1u;         // x + c_i is solid
-        const Off si = (E ^ bbi) ? (Off)(i + 1) : (Off)i;
-        const Off sj = (E ^ bbj) ? (Off)i : (Off)(i + 1);
-        g[i] = St::ld(Fc + si * N);
-        g[i + 1] = St::ld(Fc + D.odd(i) + sj * N);
+          for (int i = 1; i < Q; i += 2) {
+            if ((bb >> (i - 1)) & 1u) g[i] = St::ld(Fc + (Off)(E ? i : i + 1) * N);
+            if ((bb >> i) & 1u) g[i + 1] = St::ld(Fc + D.odd(i) + (Off)(E ? i + 1 : i) * N);
+          }
+        }
       }
       // Bounce-back links: moving-wall term and the fused force.
       const uint32_t bbmask = lw & 0x3ffffu;
@@ -498,23 +506,22 @@ __global__ void __launch_bounds__(BX, 768 / BX) k_step_pipe(Dev d, Params P, Uni
   };
 
   if (!xin) return;
+  // prefetches never wait on a link word (solid cells' slots are read and
+  // ignored); the link word of the next cell is loaded one cell ahead
   uint32_t lw_next = __ldg(d.link + (Off)z0 * nxny + (Off)y * nx + x);
-  bool pf = !is_solid((lw_next >> LINK_CLASS_SHIFT) & 7u);
-  if (pf) prefetch(z0, 0);
+  prefetch(z0, 0);
   cp_async_commit();
   for (int z = z0; z < zend; ++z) {
     const int st = (z - z0) & 1;
     const uint32_t lw = lw_next;
-    const bool have = pf;
     if (z + 1 < zend) {
       lw_next = __ldg(d.link + (Off)(z + 1) * nxny + (Off)y * nx + x);
-      pf = !is_solid((lw_next >> LINK_CLASS_SHIFT) & 7u);
-      if (pf) prefetch(z + 1, st ^ 1);
+      prefetch(z + 1, st ^ 1);
     }
     cp_async_commit();
     cp_async_wait<1>();          // this cell's copies have landed
-    if (!have) continue;         // solid: nothing to do (macros are not written here)
     const uint32_t ct = (lw >> LINK_CLASS_SHIFT) & 7u;
+    if (is_solid(ct)) continue;  // solid: nothing to do (macros are not written here)
     const Off cell = (Off)z * nxny + (Off)y * nx + x;
     const Deltas<Off> D(x, y, z, nx, ny, nz);
     R g[Q];
