@@ -95,7 +95,7 @@ def precisao(steps=10000, grade=None, forms=("f64", "f32", "f16s", "bf16s"), sam
         tail = cds[len(cds) * 3 // 4:]
         cd = float(np.mean(tail))
         mlups = N * steps / (ms_total / 1e3) / 1e6
-        rec = {"MLUPS": mlups, "roofline_frac": BYTES[form] * N * mlups * 1e6 / 1e9 / _peak(),
+        rec = {"MLUPS": mlups, "roofline_frac": BYTES[form] * mlups * 1e6 / 1e9 / _peak(),
                "cd": cd, "cd_finite": bool(np.isfinite(cds).all())}
         if ref_u is None:
             ref_u, ref_cd = m, cd
