@@ -80,6 +80,17 @@ SIGNATURES = {
     "lbm_set_block": (C.c_int, [C.c_void_p, C.c_int]),
     "lbm_set_launch": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "lbm_forces_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(Dims), C.c_void_p, C.c_void_p]),
+    "lbm_batch_create": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
+    "lbm_batch_destroy": (C.c_int, [C.c_void_p]),
+    "lbm_batch_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "lbm_batch_configure": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(Params)]),
+    "lbm_batch_set_types": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t]),
+    "lbm_batch_init_equilibrium": (C.c_int, [C.c_void_p]),
+    "lbm_batch_step": (C.c_int, [C.c_void_p, C.c_int]),
+    "lbm_batch_get_populations": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_size_t]),
+    "lbm_batch_forces": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "lbm_batch_set_tile": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "lbm_batch_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "vox_voxelize": (C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.POINTER(Dims), C.c_float, C.c_int,
                                C.c_void_p, C.c_void_p, C.POINTER(VoxStats)]),
 }

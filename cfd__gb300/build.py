@@ -37,6 +37,7 @@ UNITS = {
     "lbm_inst_bf16s.cu": ["-fmad=false"],
     "vox.cu": ["-fmad=false"],
     "lbm_noalloc.cu": ["-fmad=false"],
+    "lbm_batch.cu": ["-fmad=false"],
 }
 
 

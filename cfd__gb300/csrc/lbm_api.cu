@@ -90,6 +90,19 @@ __global__ void k_reduce3(const double* __restrict__ part, int64_t n, double* __
 
 }  // namespace
 
+namespace lbm {
+// Link-word builder for other units (batched tunnels).
+cudaError_t launch_links(const uint8_t* tipo, uint32_t* link, int nx, int ny, int nz, cudaStream_t s) {
+  const int bx = nx < 64 ? ((nx + 31) / 32) * 32 : 64;
+  k_links<<<dim3((nx + bx - 1) / bx, ny, nz), dim3(bx, 1, 1), 0, s>>>(tipo, link, nx, ny, nz);
+  return cudaGetLastError();
+}
+cudaError_t launch_reduce3(const double* part, int64_t n, double* out, cudaStream_t s) {
+  k_reduce3<<<1, 256, 0, s>>>(part, n, out);
+  return cudaGetLastError();
+}
+}  // namespace lbm
+
 struct lbm_ctx {
   lbm_dims dims{};
   int64_t N = 0;

@@ -1,0 +1,439 @@
+// lbm_batch.cu — batched tunnels (include/lbm_batch.h).
+//
+// Every tunnel keeps the single-tunnel data layout (its own in-place
+// population set, link words and types).  A device array of descriptors
+// (grid, pointers, parameters, tile shape, first tile) lets one persistent
+// kernel step all tunnels: CTA b walks global tiles b, b + G, b + 2G, ...;
+// each tile is 128 threads covering tx cells along x and 128/tx rows along y
+// of one z-plane of one tunnel, located by a binary search over the
+// tunnels' first-tile prefix.  The per-cell work is step_cell(), the same
+// code as the single-tunnel kernel, so results are bit-identical to lbm_step.
+//
+// Tile width per tunnel (32, 64 or 128) is chosen to leave the fewest idle
+// threads for that tunnel's nx and ny, or set by lbm_batch_set_tile.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/lbm.h"
+#include "../../include/lbm_batch.h"
+#include "lbm_kernels.cuh"
+
+extern "C" int lbm_internal_fail(int code, const char* msg);
+
+namespace lbm {
+cudaError_t launch_links(const uint8_t* tipo, uint32_t* link, int nx, int ny, int nz, cudaStream_t s);
+cudaError_t launch_reduce3(const double* part, int64_t n, double* out, cudaStream_t s);
+}  // namespace lbm
+
+using namespace lbm;
+
+namespace {
+
+struct TunnelDesc {
+  Dev d;
+  Params P;
+  Uni<float> U;
+  int tx, ty, gx, gy;   // tile shape, tiles along x and y
+  long long tile0;      // first global tile of this tunnel
+};
+
+constexpr int kTile = 128;
+
+template <class St, int PAR, bool FAST>
+__global__ void __launch_bounds__(kTile, 8) k_batch_step(const TunnelDesc* __restrict__ T,
+                                                         const long long* __restrict__ first, int ntun,
+                                                         long long ntiles) {
+  for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    int lo = 0, hi = ntun;
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (__ldg(first + mid) <= t) lo = mid;
+      else hi = mid;
+    }
+    const TunnelDesc& D = T[lo];
+    const int tx = D.tx, ty = D.ty, gx = D.gx, gy = D.gy;
+    const long long local = t - D.tile0;
+    const int bxi = (int)(local % gx);
+    const long long rest = local / gx;
+    const int byi = (int)(rest % gy);
+    const int z = (int)(rest / gy);
+    const int x = bxi * tx + (int)(threadIdx.x % tx);
+    const int y = byi * ty + (int)(threadIdx.x / tx);
+    double fx, fy, fz;
+    if (x < D.d.nx && y < D.d.ny) step_cell<St, PAR, false, false, false, FAST>(D.d, D.P, D.U, x, y, z, fx, fy, fz);
+  }
+}
+
+int bfail(int code, const std::string& m) { return lbm_internal_fail(code, m.c_str()); }
+
+#define BCK(call, what)                                                                  \
+  do {                                                                                   \
+    cudaError_t _e = (call);                                                             \
+    if (_e != cudaSuccess) {                                                             \
+      cudaGetLastError();                                                                \
+      return bfail(_e == cudaErrorMemoryAllocation ? LBM_ENOMEM : LBM_ECUDA,             \
+                   std::string(what) + ": " + cudaGetErrorString(_e));                   \
+    }                                                                                    \
+  } while (0)
+
+Ops ops_for_batch(int storage) {
+  switch (storage) {
+    case LBM_F16S: return ops_f16s();
+    case LBM_BF16S: return ops_bf16s();
+    default: return ops_f32();
+  }
+}
+
+}  // namespace
+
+struct lbm_batch {
+  int storage = LBM_F32;
+  bool fast = true;
+  std::vector<lbm_dims> dims;
+  std::vector<TunnelDesc> host;
+  std::vector<int> tile_req;         // requested tile width (0 = cost model)
+  std::vector<bool> configured, typed;
+  std::vector<void*> allocs;
+  TunnelDesc* d_desc = nullptr;
+  long long* d_first = nullptr;
+  long long ntiles = 0;
+  int grid = 0;
+  Ops ops{};
+  double* partials = nullptr;
+  int64_t npart = 0;
+  double* red = nullptr;
+  double* stage = nullptr;
+  int64_t stage_n = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int64_t steps = 0;
+  int64_t cells = 0;
+  int64_t bytes = 0;
+  bool desc_dirty = true;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};   // by start parity
+  int graph_steps = 32;
+  long long graph_ntiles = -1;
+};
+
+namespace {
+
+int balloc(lbm_batch* b, void** p, size_t bytes, const char* what) {
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    char buf[200];
+    snprintf(buf, sizeof buf, "device allocation of %.3f GB for %s failed: %s", bytes / 1e9, what,
+             cudaGetErrorString(e));
+    *p = nullptr;
+    return bfail(LBM_ENOMEM, buf);
+  }
+  b->allocs.push_back(*p);
+  b->bytes += (int64_t)bytes;
+  return LBM_OK;
+}
+
+// Fewest idle threads for (nx, ny); ties go to the wider tile.
+int pick_tile(int nx, int ny) {
+  int best = 128;
+  double best_w = 1e30;
+  for (int tx : {128, 64, 32}) {
+    const int ty = kTile / tx;
+    const double used = (double)nx * ny;
+    const double launched = (double)((nx + tx - 1) / tx) * tx * ((ny + ty - 1) / ty) * ty;
+    const double w = launched / used;
+    if (w < best_w - 1e-12) { best_w = w; best = tx; }
+  }
+  return best;
+}
+
+void drop_graphs(lbm_batch* b) {
+  for (auto& g : b->graph)
+    if (g) { cudaGraphExecDestroy(g); g = nullptr; }
+}
+
+int sync_desc(lbm_batch* b) {
+  if (!b->desc_dirty) return LBM_OK;
+  std::vector<long long> first(b->host.size() + 1, 0);
+  long long t = 0;
+  for (size_t k = 0; k < b->host.size(); ++k) {
+    TunnelDesc& D = b->host[k];
+    const int tx = b->tile_req[k] ? b->tile_req[k] : pick_tile(D.d.nx, D.d.ny);
+    D.tx = tx;
+    D.ty = kTile / tx;
+    D.gx = (D.d.nx + tx - 1) / tx;
+    D.gy = (D.d.ny + D.ty - 1) / D.ty;
+    D.tile0 = t;
+    first[k] = t;
+    t += (long long)D.gx * D.gy * D.d.nz;
+  }
+  first[b->host.size()] = t;
+  if (t != b->ntiles) drop_graphs(b);
+  b->ntiles = t;
+  BCK(cudaMemcpyAsync(b->d_desc, b->host.data(), sizeof(TunnelDesc) * b->host.size(), cudaMemcpyHostToDevice,
+                      b->stream), "descriptor upload");
+  BCK(cudaMemcpyAsync(b->d_first, first.data(), sizeof(long long) * first.size(), cudaMemcpyHostToDevice,
+                      b->stream), "tile prefix upload");
+  BCK(cudaStreamSynchronize(b->stream), "descriptor sync");
+  b->desc_dirty = false;
+  return LBM_OK;
+}
+
+template <class St>
+void launch_batch(lbm_batch* b, int parity) {
+  const int ntun = (int)b->host.size();
+  if (b->fast) {
+    if (parity == 0) k_batch_step<St, 0, true><<<b->grid, kTile, 0, b->stream>>>(b->d_desc, b->d_first, ntun, b->ntiles);
+    else k_batch_step<St, 1, true><<<b->grid, kTile, 0, b->stream>>>(b->d_desc, b->d_first, ntun, b->ntiles);
+  } else {
+    if (parity == 0) k_batch_step<St, 0, false><<<b->grid, kTile, 0, b->stream>>>(b->d_desc, b->d_first, ntun, b->ntiles);
+    else k_batch_step<St, 1, false><<<b->grid, kTile, 0, b->stream>>>(b->d_desc, b->d_first, ntun, b->ntiles);
+  }
+}
+
+void launch_one(lbm_batch* b, int parity) {
+  switch (b->storage) {
+    case LBM_F16S: launch_batch<StF16S>(b, parity); break;
+    case LBM_BF16S: launch_batch<StBF16S>(b, parity); break;
+    default: launch_batch<StF32>(b, parity); break;
+  }
+}
+
+int check_ready(lbm_batch* b) {
+  if (!b) return bfail(LBM_EINVAL, "null batch");
+  for (size_t k = 0; k < b->host.size(); ++k) {
+    if (!b->typed[k]) return bfail(LBM_ESTATE, "tunnel " + std::to_string(k) + ": cell types not set");
+    if (!b->configured[k]) return bfail(LBM_ESTATE, "tunnel " + std::to_string(k) + ": parameters not set");
+  }
+  return LBM_OK;
+}
+
+Launch tunnel_launch(const lbm_dims& d) {
+  Launch L;
+  const int bx = d.nx < 64 ? ((d.nx + 31) / 32) * 32 : 64;
+  L.block = dim3(bx, 1, 1);
+  L.grid = dim3((d.nx + bx - 1) / bx, d.ny, d.nz);
+  return L;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lbm_batch_create(const lbm_dims* dims, int ntunnels, int storage, int flags, lbm_batch** out) {
+  if (!dims || !out || ntunnels < 1) return bfail(LBM_EINVAL, "need at least one tunnel and an output handle");
+  *out = nullptr;
+  if (storage != LBM_F32 && storage != LBM_F16S && storage != LBM_BF16S)
+    return bfail(LBM_ENOTSUP, "batched tunnels support LBM_F32, LBM_F16S and LBM_BF16S");
+  if (flags & ~LBM_FLAG_STRICT) return bfail(LBM_EINVAL, "batched tunnels accept LBM_FLAG_STRICT only");
+  lbm_batch* b = new lbm_batch();
+  b->storage = storage;
+  b->fast = !(flags & LBM_FLAG_STRICT);
+  b->ops = ops_for_batch(storage);
+  b->dims.assign(dims, dims + ntunnels);
+  b->host.resize(ntunnels);
+  b->tile_req.assign(ntunnels, 0);
+  b->configured.assign(ntunnels, false);
+  b->typed.assign(ntunnels, false);
+  int r = LBM_OK;
+  for (int k = 0; k < ntunnels && !r; ++k) {
+    const lbm_dims& d = dims[k];
+    if (d.nx < 1 || d.ny < 1 || d.nz < 1) { r = bfail(LBM_EINVAL, "grid dimensions must be >= 1"); break; }
+    const int64_t N = (int64_t)d.nx * d.ny * d.nz;
+    if ((int64_t)Q * N >= (int64_t)INT32_MAX) { r = bfail(LBM_EINVAL, "a batched tunnel must hold under 113 M cells"); break; }
+    TunnelDesc& D = b->host[k];
+    memset(&D, 0, sizeof D);
+    D.d.nx = d.nx; D.d.ny = d.ny; D.d.nz = d.nz; D.d.N = N;
+    void* p = nullptr;
+    const size_t sb = (size_t)N * Q * b->ops.elem_bytes;
+    if ((r = balloc(b, &p, sb, "populations"))) break;
+    D.d.pop = p;
+    if ((r = balloc(b, &p, (size_t)N, "cell types"))) break;
+    D.d.tipo = static_cast<uint8_t*>(p);
+    if ((r = balloc(b, &p, sizeof(uint32_t) * (size_t)N, "link words"))) break;
+    D.d.link = static_cast<uint32_t*>(p);
+    b->cells += N;
+  }
+  void* p = nullptr;
+  if (!r) r = balloc(b, &p, sizeof(TunnelDesc) * ntunnels, "descriptors");
+  b->d_desc = static_cast<TunnelDesc*>(p);
+  if (!r) r = balloc(b, &p, sizeof(long long) * (ntunnels + 1), "tile prefix");
+  b->d_first = static_cast<long long*>(p);
+  if (!r) r = balloc(b, &p, 3 * sizeof(double), "reduction result");
+  b->red = static_cast<double*>(p);
+  if (r) { lbm_batch_destroy(b); return r; }
+  cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) { lbm_batch_destroy(b); return bfail(LBM_ECUDA, "stream creation failed"); }
+  b->own_stream = true;
+  for (int k = 0; k < ntunnels; ++k) {
+    TunnelDesc& D = b->host[k];
+    cudaMemsetAsync(D.d.pop, 0, (size_t)D.d.N * Q * b->ops.elem_bytes, b->stream);
+    cudaMemsetAsync((void*)D.d.tipo, 0, (size_t)D.d.N, b->stream);
+  }
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  b->grid = std::max(1, sms) * 8;   // persistent: 8 resident 128-thread CTAs per SM
+  e = cudaStreamSynchronize(b->stream);
+  if (e != cudaSuccess) { lbm_batch_destroy(b); return bfail(LBM_ECUDA, "initial clear failed"); }
+  *out = b;
+  return LBM_OK;
+}
+
+int lbm_batch_destroy(lbm_batch* b) {
+  if (!b) return bfail(LBM_EINVAL, "null batch");
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  drop_graphs(b);
+  for (void* p : b->allocs) cudaFree(p);
+  if (b->partials) cudaFree(b->partials);
+  if (b->stage) cudaFree(b->stage);
+  if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+  return LBM_OK;
+}
+
+int lbm_batch_set_stream(lbm_batch* b, void* s) {
+  if (!b) return bfail(LBM_EINVAL, "null batch");
+  BCK(cudaStreamSynchronize(b->stream), "stream sync");
+  if (b->own_stream) cudaStreamDestroy(b->stream);
+  b->stream = static_cast<cudaStream_t>(s);
+  b->own_stream = false;
+  drop_graphs(b);
+  return LBM_OK;
+}
+
+int lbm_batch_configure(lbm_batch* b, int k, const lbm_params* p) {
+  if (!b || !p) return bfail(LBM_EINVAL, "null argument");
+  if (k < 0 || k >= (int)b->host.size()) return bfail(LBM_EINVAL, "tunnel index out of range");
+  Params P;
+  P.omega_plus = p->omega_plus; P.magic = p->magic; P.les_cs = p->les_cs;
+  for (int a = 0; a < 3; ++a) { P.belt[a] = p->belt_u[a]; P.inlet[a] = p->inlet_u[a]; }
+  P.sponge_start = p->sponge_start; P.sponge_len = p->sponge_len; P.bl = p->bl_thickness;
+  P.closure = p->closure;
+  b->host[k].P = P;
+  b->host[k].U = make_uni<float>(P);
+  b->configured[k] = true;
+  b->desc_dirty = true;
+  return LBM_OK;
+}
+
+int lbm_batch_set_types(lbm_batch* b, int k, const uint32_t* tipo, size_t n) {
+  if (!b || !tipo) return bfail(LBM_EINVAL, "null argument");
+  if (k < 0 || k >= (int)b->host.size()) return bfail(LBM_EINVAL, "tunnel index out of range");
+  TunnelDesc& D = b->host[k];
+  if ((int64_t)n != D.d.N) return bfail(LBM_EINVAL, "cell-type field size differs from the tunnel's N");
+  std::vector<uint8_t> t8(n);
+  for (size_t i = 0; i < n; ++i) {
+    if (tipo[i] > 7u) return bfail(LBM_EINVAL, "cell type is not a CELULA code (0..7)");
+    t8[i] = (uint8_t)tipo[i];
+  }
+  BCK(cudaMemcpyAsync((void*)D.d.tipo, t8.data(), n, cudaMemcpyHostToDevice, b->stream), "types upload");
+  BCK(launch_links(D.d.tipo, (uint32_t*)D.d.link, D.d.nx, D.d.ny, D.d.nz, b->stream), "link kernel");
+  BCK(cudaStreamSynchronize(b->stream), "types sync");
+  b->typed[k] = true;
+  return LBM_OK;
+}
+
+int lbm_batch_init_equilibrium(lbm_batch* b) {
+  int r = check_ready(b);
+  if (r) return r;
+  for (size_t k = 0; k < b->host.size(); ++k) {
+    const TunnelDesc& D = b->host[k];
+    BCK(b->ops.init(D.d, D.P, true, tunnel_launch(b->dims[k]), b->stream), "init kernel");
+  }
+  b->steps = 0;
+  return LBM_OK;
+}
+
+int lbm_batch_set_tile(lbm_batch* b, int k, int tile_x) {
+  if (!b) return bfail(LBM_EINVAL, "null batch");
+  if (k < 0 || k >= (int)b->host.size()) return bfail(LBM_EINVAL, "tunnel index out of range");
+  if (tile_x != 0 && tile_x != 32 && tile_x != 64 && tile_x != 128) return bfail(LBM_EINVAL, "tile_x must be 0, 32, 64 or 128");
+  b->tile_req[k] = tile_x;
+  b->desc_dirty = true;
+  return LBM_OK;
+}
+
+int lbm_batch_step(lbm_batch* b, int n) {
+  int r = check_ready(b);
+  if (r) return r;
+  if (n < 0) return bfail(LBM_EINVAL, "negative step count");
+  if ((r = sync_desc(b))) return r;
+  const int G = b->graph_steps;
+  while (n >= G) {
+    const int par = (int)(b->steps & 1);
+    if (!b->graph[par]) {
+      cudaGraph_t g;
+      BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "graph capture begin");
+      for (int s = 0; s < G; ++s) launch_one(b, (par + s) & 1);
+      cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+      if (e != cudaSuccess) return bfail(LBM_ECUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+      e = cudaGraphInstantiate(&b->graph[par], g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) return bfail(LBM_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    }
+    BCK(cudaGraphLaunch(b->graph[par], b->stream), "graph launch");
+    b->steps += G;
+    n -= G;
+  }
+  for (; n > 0; --n) {
+    launch_one(b, (int)(b->steps & 1));
+    BCK(cudaGetLastError(), "batch step launch");
+    b->steps++;
+  }
+  return LBM_OK;
+}
+
+int lbm_batch_get_populations(lbm_batch* b, int k, double* g, size_t n) {
+  if (!b || !g) return bfail(LBM_EINVAL, "null argument");
+  if (k < 0 || k >= (int)b->host.size()) return bfail(LBM_EINVAL, "tunnel index out of range");
+  const TunnelDesc& D = b->host[k];
+  if ((int64_t)n != Q * D.d.N) return bfail(LBM_EINVAL, "population array must hold 19*N_k values");
+  if (b->stage_n < D.d.N) {
+    if (b->stage) cudaFree(b->stage);
+    b->stage = nullptr;
+    BCK(cudaMalloc(&b->stage, sizeof(double) * (size_t)D.d.N), "state staging");
+    b->stage_n = D.d.N;
+  }
+  const Launch L = tunnel_launch(b->dims[k]);
+  for (int q = 0; q < Q; ++q) {
+    BCK(b->ops.get_dir(D.d, b->stage, q, (int)(b->steps & 1), true, L, b->stream), "population gather");
+    BCK(cudaMemcpyAsync(g + (size_t)q * D.d.N, b->stage, sizeof(double) * D.d.N, cudaMemcpyDeviceToHost, b->stream),
+        "population download");
+    BCK(cudaStreamSynchronize(b->stream), "population sync");
+  }
+  return LBM_OK;
+}
+
+int lbm_batch_forces(lbm_batch* b, double* f) {
+  if (!b || !f) return bfail(LBM_EINVAL, "null argument");
+  for (size_t k = 0; k < b->host.size(); ++k) {
+    const TunnelDesc& D = b->host[k];
+    const Launch L = tunnel_launch(b->dims[k]);
+    const int64_t nb = (int64_t)L.grid.x * L.grid.y * L.grid.z;
+    if (b->npart < nb) {
+      if (b->partials) cudaFree(b->partials);
+      b->partials = nullptr;
+      BCK(cudaMalloc(&b->partials, 3 * sizeof(double) * (size_t)nb), "reduction partials");
+      b->npart = nb;
+    }
+    BCK(b->ops.forces(D.d, (int)(b->steps & 1), true, b->partials, L, b->stream), "force kernel");
+    BCK(launch_reduce3(b->partials, nb, b->red, b->stream), "reduce kernel");
+    BCK(cudaMemcpyAsync(f + 3 * k, b->red, 3 * sizeof(double), cudaMemcpyDeviceToHost, b->stream), "force download");
+  }
+  BCK(cudaStreamSynchronize(b->stream), "force sync");
+  return LBM_OK;
+}
+
+int lbm_batch_info(lbm_batch* b, int64_t* total_cells, int64_t* device_bytes) {
+  if (!b) return bfail(LBM_EINVAL, "null batch");
+  if (total_cells) *total_cells = b->cells;
+  if (device_bytes) *device_bytes = b->bytes;
+  return LBM_OK;
+}
+
+}  // extern "C"

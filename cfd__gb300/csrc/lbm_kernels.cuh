@@ -128,21 +128,17 @@ struct Deltas {
 // In-place step.  Grid: (ceil(nx/bx), ceil(ny/by), nz), block (bx, by).
 // PAR: step parity (0 even).  MAC: write (u, delta).  FRC: accumulate the
 // momentum-exchange force of the state being streamed.
-// MINB: minimum resident 128-thread blocks per SM the register allocation
-// must allow (8 -> 64 registers, 6 -> 80); the autotuner picks per form.
-template <class St, int PAR, bool MAC, bool FRC, bool W64, bool FAST, int MINB>
-__global__ void __launch_bounds__(128, MINB)
-k_step_inplace(Dev d, Params P, Uni<typename St::real> U) {
+// One cell of the in-place step (everything the step does for cell x, y, z).
+// Shared by the single-tunnel kernel and the batched kernel, so both run
+// the identical arithmetic.
+template <class St, int PAR, bool MAC, bool FRC, bool W64, bool FAST>
+__device__ __forceinline__ void step_cell(const Dev& d, const Params& P, const Uni<typename St::real>& U, int x, int y,
+                                          int z, double& fx, double& fy, double& fz) {
   using R = typename St::real;
   using S = typename St::store_t;
   using Off = typename OffT<W64>::type;
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = blockIdx.y * blockDim.y + threadIdx.y;
-  const int z = blockIdx.z;
   const int nx = d.nx, ny = d.ny;
-  const bool in = x < nx && y < ny;
-  double fx = 0.0, fy = 0.0, fz = 0.0;
-  if (in) {
+  {
     const Off N = (Off)d.N;
     const Off cell = ((Off)z * ny + y) * nx + x;
     // The normal-slot loads do not wait for the link word: they are issued
@@ -215,7 +211,19 @@ k_step_inplace(Dev d, Params P, Uni<typename St::real> U) {
         }
       });
     }
-  }
+    }
+}
+
+// MINB: minimum resident 128-thread blocks per SM the register allocation
+// must allow (8 -> 64 registers, 6 -> 80); the autotuner picks per form.
+template <class St, int PAR, bool MAC, bool FRC, bool W64, bool FAST, int MINB>
+__global__ void __launch_bounds__(128, MINB)
+k_step_inplace(Dev d, Params P, Uni<typename St::real> U) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  double fx = 0.0, fy = 0.0, fz = 0.0;
+  if (x < d.nx && y < d.ny) step_cell<St, PAR, MAC, FRC, W64, FAST>(d, P, U, x, y, z, fx, fy, fz);
   if (FRC) {
     const bool any = __any_sync(0xffffffffu, fx != 0.0 || fy != 0.0 || fz != 0.0);
     if (any) warp_add3(fx, fy, fz, d.force);

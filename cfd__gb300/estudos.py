@@ -106,15 +106,69 @@ def precisao(steps=10000, grade=None, forms=("f64", "f32", "f16s", "bf16s"), sam
     return out
 
 
+def lote(n_tunnels=64, steps=256, storages=("f32", "f16s"), seed=2026):
+    """Batched workload: n tunnels drawn by sorteio_lote (96x48x48 to
+    256x128x128).  Aggregate MLUPS = sum N_k * steps / time, for the batch
+    (one persistent launch per step, CUDA-graph replay) and for the same
+    tunnels run one after another with the single-tunnel solver."""
+    import torch
+
+    from .lote import LoteCUDA, sorteio_lote
+    from .solver import SolverCUDA
+    tun = sorteio_lote(n_tunnels, seed)
+    cells = sum(t[0]["nx"] * t[0]["ny"] * t[0]["nz"] for t in tun)
+    out = {"tunnels": n_tunnels, "cells": cells, "steps": steps,
+           "omega_flagged": int(sum(t[3]["flag_omega"] for t in tun)), "forms": {}}
+    stream = torch.cuda.Stream()
+    for st in storages:
+        L = LoteCUDA([t[0] for t in tun], storage=st)
+        L.definirStream(stream.cuda_stream)
+        for k, (g, tipo, cfg, info) in enumerate(tun):
+            L.definirTipos(k, tipo)
+            L.configurar(k, **cfg)
+        L.inicializar()
+        L.passo(64)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        L.passo(steps)
+        e1.record(stream)
+        e1.synchronize()
+        ms_batch = e0.elapsed_time(e1)
+        L.destruir()
+        ms_seq = 0.0
+        for g, tipo, cfg, info in tun:
+            s = SolverCUDA(g, storage=st, escrever_macros=False)
+            s.definirStream(stream.cuda_stream)
+            s.definirTipos(tipo)
+            s.configurar(**cfg)
+            s.inicializar()
+            s.passo(8)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            s.passo(steps)
+            e1.record(stream)
+            e1.synchronize()
+            ms_seq += e0.elapsed_time(e1)
+            s.destruir()
+        out["forms"][st] = {"batched_MLUPS": cells * steps / (ms_batch / 1e3) / 1e6,
+                            "sequential_MLUPS": cells * steps / (ms_seq / 1e3) / 1e6,
+                            "speedup": ms_seq / ms_batch}
+    return out
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("study", choices=["precisao"])
+    ap.add_argument("study", choices=["precisao", "lote"])
     ap.add_argument("--steps", type=int, default=10000)
     ap.add_argument("--grid", default="512,256,192")
     a = ap.parse_args(argv)
     nx, ny, nz = (int(v) for v in a.grid.split(","))
     t0 = time.time()
-    r = precisao(a.steps, {"nx": nx, "ny": ny, "nz": nz})
+    if a.study == "lote":
+        r = lote(steps=a.steps)
+    else:
+        r = precisao(a.steps, {"nx": nx, "ny": ny, "nz": nz})
     r["wall_s"] = time.time() - t0
     print(json.dumps(r))
 

@@ -1,0 +1,48 @@
+/*
+ * lbm_batch.h — many wind tunnels of uneven sizes stepped together.
+ *
+ * The reference runs one tunnel per solver object and one compute dispatch
+ * per tunnel step (src/backend/webgpu/solver.js:395-415).  A batch holds T
+ * independent tunnels (each with its own grid, cell types and parameters —
+ * the same data as one lbm_ctx) and advances all of them with ONE persistent
+ * kernel launch per step: a fixed grid of CTAs walks the tiles of every
+ * tunnel.  lbm_batch_step captures the launches into a CUDA graph and
+ * replays it.  Arithmetic is identical to lbm_step (same per-cell code), so
+ * each tunnel's state equals the state a separate lbm_ctx would reach.
+ * Storage forms: LBM_F32, LBM_F16S, LBM_BF16S (in-place layout only).
+ */
+#ifndef CFD_GB300_LBM_BATCH_H
+#define CFD_GB300_LBM_BATCH_H
+
+#include "lbm.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct lbm_batch lbm_batch;
+
+/* T tunnels, dims[k] each; flags: LBM_FLAG_STRICT only. */
+int lbm_batch_create(const lbm_dims* dims, int ntunnels, int storage, int flags, lbm_batch** out);
+int lbm_batch_destroy(lbm_batch* b);
+int lbm_batch_set_stream(lbm_batch* b, void* cuda_stream);
+/* per-tunnel lbm_configure / lbm_set_types */
+int lbm_batch_configure(lbm_batch* b, int k, const lbm_params* p);
+int lbm_batch_set_types(lbm_batch* b, int k, const uint32_t* tipo, size_t n);
+/* shaderInit in every tunnel; step counter to 0 */
+int lbm_batch_init_equilibrium(lbm_batch* b);
+/* n steps of every tunnel (CUDA-graph replay of one persistent launch per step) */
+int lbm_batch_step(lbm_batch* b, int n);
+/* tunnel k's state, 19*N_k doubles, natural layout (as lbm_get_populations) */
+int lbm_batch_get_populations(lbm_batch* b, int k, double* g, size_t n);
+/* raw momentum-exchange force of every tunnel: 3*T doubles (as lbm_forces) */
+int lbm_batch_forces(lbm_batch* b, double* f);
+/* tile width along x of tunnel k (32, 64 or 128 threads; the tile is 128
+ * threads); 0 = the cost model (least idle threads) */
+int lbm_batch_set_tile(lbm_batch* b, int k, int tile_x);
+int lbm_batch_info(lbm_batch* b, int64_t* total_cells, int64_t* device_bytes);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CFD_GB300_LBM_BATCH_H */

@@ -1,0 +1,44 @@
+"""Batched tunnels: every tunnel of a batch equals a separate solver, bit for
+bit, through the graph-replayed persistent launch."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _tunnels():
+    from cfd__gb300.lote import sorteio_lote
+    # five uneven tunnels (small grids from the same generator as the 64-tunnel workload)
+    return sorteio_lote(n=5, seed=11, nx_min=32, nx_max=80)
+
+
+@pytest.mark.parametrize("storage", ["f32", "f16s"])
+@pytest.mark.parametrize("tile", [0, 32])
+def test_batch_equals_separate_solvers(native, storage, tile):
+    from cfd__gb300 import SolverCUDA
+    from cfd__gb300.lote import LoteCUDA
+    tun = _tunnels()
+    lote = LoteCUDA([t[0] for t in tun], storage=storage)
+    solos = []
+    for k, (g, tipo, cfg, info) in enumerate(tun):
+        lote.definirTipos(k, tipo)
+        lote.configurar(k, **cfg)
+        if tile:
+            lote.definirLadrilho(k, tile)
+        s = SolverCUDA(g, storage=storage)
+        s.definirTipos(tipo)
+        s.configurar(**cfg)
+        s.inicializar()
+        solos.append(s)
+    lote.inicializar()
+    for n in (3, 40):          # direct launches, then a 32-step graph replay + 8 direct
+        lote.passo(n)
+        for s in solos:
+            s.passo(n)
+    f = lote.medirForcas()
+    for k, (g, tipo, cfg, info) in enumerate(tun):
+        fl = ~np.isin(tipo, [1, 4, 7])
+        a = lote.lerPopulacoes(k)[:, fl]
+        b = solos[k].lerPopulacoes()[:, fl]
+        assert np.array_equal(a, b), (k, storage, tile)
+        np.testing.assert_allclose(f[k], solos[k].medirForcas(), rtol=1e-12, atol=1e-15)
