@@ -91,6 +91,7 @@ SIGNATURES = {
     "lbm_batch_forces": (C.c_int, [C.c_void_p, C.c_void_p]),
     "lbm_batch_set_tile": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "lbm_batch_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "lbm_batch_set_mode": (C.c_int, [C.c_void_p, C.c_int]),
     "vox_voxelize": (C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.POINTER(Dims), C.c_float, C.c_int,
                                C.c_void_p, C.c_void_p, C.POINTER(VoxStats)]),
 }

@@ -11,6 +11,9 @@
 //
 // Tile width per tunnel (32, 64 or 128) is chosen to leave the fewest idle
 // threads for that tunnel's nx and ny, or set by lbm_batch_set_tile.
+// The descriptors of up to 64 tunnels travel by value in the launch's
+// parameter space (read through the constant cache, as single-tunnel
+// parameters are); larger batches take one launch per 64 tunnels per step.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -43,25 +46,46 @@ struct TunnelDesc {
 };
 
 constexpr int kTile = 128;
+static_assert(sizeof(TunnelDesc) % 4 == 0, "descriptor copied as 32-bit words");
+constexpr int kPerLaunch = 64;   // tunnels whose descriptors ride in one launch's parameters
+
+// One launch's share of the batch, passed by value: the descriptors sit in
+// the kernel parameter space (constant bank), like a single tunnel's Params.
+struct BatchArgs {
+  int ntun;
+  int ntiles;
+  int first[kPerLaunch + 1];   // first tile of each tunnel (prefix), local to this launch
+  TunnelDesc t[kPerLaunch];
+};
+static_assert(sizeof(BatchArgs) < 32000, "kernel parameter space");
 
 template <class St, int PAR, bool FAST>
-__global__ void __launch_bounds__(kTile, 8) k_batch_step(const TunnelDesc* __restrict__ T,
-                                                         const long long* __restrict__ first, int ntun,
-                                                         long long ntiles) {
-  for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    int lo = 0, hi = ntun;
+__global__ void __launch_bounds__(kTile, 8) k_batch_step(const __grid_constant__ BatchArgs A) {
+  // The current tunnel's descriptor, staged in shared memory when a CTA
+  // moves to a tile of another tunnel.
+  __shared__ TunnelDesc D;
+  int cur = -1;
+  for (int t = blockIdx.x; t < A.ntiles; t += gridDim.x) {
+    int lo = 0, hi = A.ntun;
     while (hi - lo > 1) {
       const int mid = (lo + hi) >> 1;
-      if (__ldg(first + mid) <= t) lo = mid;
+      if (A.first[mid] <= t) lo = mid;
       else hi = mid;
     }
-    const TunnelDesc& D = T[lo];
+    if (lo != cur) {
+      __syncthreads();
+      const uint32_t* src = reinterpret_cast<const uint32_t*>(&A.t[lo]);
+      uint32_t* dst = reinterpret_cast<uint32_t*>(&D);
+      for (int w = threadIdx.x; w < (int)(sizeof(TunnelDesc) / 4); w += kTile) dst[w] = src[w];
+      __syncthreads();
+      cur = lo;
+    }
     const int tx = D.tx, ty = D.ty, gx = D.gx, gy = D.gy;
-    const long long local = t - D.tile0;
-    const int bxi = (int)(local % gx);
-    const long long rest = local / gx;
-    const int byi = (int)(rest % gy);
-    const int z = (int)(rest / gy);
+    const int local = t - A.first[lo];
+    const int bxi = local % gx;
+    const int rest = local / gx;
+    const int byi = rest % gy;
+    const int z = rest / gy;
     const int x = bxi * tx + (int)(threadIdx.x % tx);
     const int y = byi * ty + (int)(threadIdx.x / tx);
     double fx, fy, fz;
@@ -99,8 +123,7 @@ struct lbm_batch {
   std::vector<int> tile_req;         // requested tile width (0 = cost model)
   std::vector<bool> configured, typed;
   std::vector<void*> allocs;
-  TunnelDesc* d_desc = nullptr;
-  long long* d_first = nullptr;
+  std::vector<BatchArgs> args;       // one per launch of a step (64 tunnels each)
   long long ntiles = 0;
   int grid = 0;
   Ops ops{};
@@ -117,7 +140,10 @@ struct lbm_batch {
   bool desc_dirty = true;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};   // by start parity
   int graph_steps = 32;
-  long long graph_ntiles = -1;
+  int mode = 0;                      // 0: graph of per-tunnel chains, 1: persistent single launch
+  std::vector<cudaStream_t> lanes;   // capture-time streams, one per tunnel (mode 0)
+  cudaEvent_t fork = nullptr;
+  std::vector<cudaEvent_t> joins;
 };
 
 namespace {
@@ -158,40 +184,50 @@ void drop_graphs(lbm_batch* b) {
 
 int sync_desc(lbm_batch* b) {
   if (!b->desc_dirty) return LBM_OK;
-  std::vector<long long> first(b->host.size() + 1, 0);
-  long long t = 0;
-  for (size_t k = 0; k < b->host.size(); ++k) {
-    TunnelDesc& D = b->host[k];
-    const int tx = b->tile_req[k] ? b->tile_req[k] : pick_tile(D.d.nx, D.d.ny);
-    D.tx = tx;
-    D.ty = kTile / tx;
-    D.gx = (D.d.nx + tx - 1) / tx;
-    D.gy = (D.d.ny + D.ty - 1) / D.ty;
-    D.tile0 = t;
-    first[k] = t;
-    t += (long long)D.gx * D.gy * D.d.nz;
+  // Launch arguments change: graphs hold them by value, so drop them.
+  drop_graphs(b);
+  b->args.clear();
+  long long total = 0;
+  for (size_t k0 = 0; k0 < b->host.size(); k0 += kPerLaunch) {
+    BatchArgs A;
+    memset(&A, 0, sizeof A);
+    const size_t k1 = std::min(b->host.size(), k0 + kPerLaunch);
+    long long t = 0;
+    for (size_t k = k0; k < k1; ++k) {
+      TunnelDesc& D = b->host[k];
+      const int tx = b->tile_req[k] ? b->tile_req[k] : pick_tile(D.d.nx, D.d.ny);
+      D.tx = tx;
+      D.ty = kTile / tx;
+      D.gx = (D.d.nx + tx - 1) / tx;
+      D.gy = (D.d.ny + D.ty - 1) / D.ty;
+      D.tile0 = t;
+      A.first[k - k0] = (int)t;
+      A.t[k - k0] = D;
+      t += (long long)D.gx * D.gy * D.d.nz;
+    }
+    if (t >= INT32_MAX) return bfail(LBM_EINVAL, "too many tiles in one launch (keep a batch under 2^31 tiles)");
+    A.ntun = (int)(k1 - k0);
+    A.first[A.ntun] = (int)t;
+    A.ntiles = (int)t;
+    b->args.push_back(A);
+    total += t;
   }
-  first[b->host.size()] = t;
-  if (t != b->ntiles) drop_graphs(b);
-  b->ntiles = t;
-  BCK(cudaMemcpyAsync(b->d_desc, b->host.data(), sizeof(TunnelDesc) * b->host.size(), cudaMemcpyHostToDevice,
-                      b->stream), "descriptor upload");
-  BCK(cudaMemcpyAsync(b->d_first, first.data(), sizeof(long long) * first.size(), cudaMemcpyHostToDevice,
-                      b->stream), "tile prefix upload");
-  BCK(cudaStreamSynchronize(b->stream), "descriptor sync");
+  b->ntiles = total;
   b->desc_dirty = false;
   return LBM_OK;
 }
 
 template <class St>
 void launch_batch(lbm_batch* b, int parity) {
-  const int ntun = (int)b->host.size();
-  if (b->fast) {
-    if (parity == 0) k_batch_step<St, 0, true><<<b->grid, kTile, 0, b->stream>>>(b->d_desc, b->d_first, ntun, b->ntiles);
-    else k_batch_step<St, 1, true><<<b->grid, kTile, 0, b->stream>>>(b->d_desc, b->d_first, ntun, b->ntiles);
-  } else {
-    if (parity == 0) k_batch_step<St, 0, false><<<b->grid, kTile, 0, b->stream>>>(b->d_desc, b->d_first, ntun, b->ntiles);
-    else k_batch_step<St, 1, false><<<b->grid, kTile, 0, b->stream>>>(b->d_desc, b->d_first, ntun, b->ntiles);
+  for (const BatchArgs& A : b->args) {
+    const int grid = std::min(b->grid, std::max(1, A.ntiles));
+    if (b->fast) {
+      if (parity == 0) k_batch_step<St, 0, true><<<grid, kTile, 0, b->stream>>>(A);
+      else k_batch_step<St, 1, true><<<grid, kTile, 0, b->stream>>>(A);
+    } else {
+      if (parity == 0) k_batch_step<St, 0, false><<<grid, kTile, 0, b->stream>>>(A);
+      else k_batch_step<St, 1, false><<<grid, kTile, 0, b->stream>>>(A);
+    }
   }
 }
 
@@ -201,6 +237,28 @@ void launch_one(lbm_batch* b, int parity) {
     case LBM_BF16S: launch_batch<StBF16S>(b, parity); break;
     default: launch_batch<StF32>(b, parity); break;
   }
+}
+
+Launch tunnel_launch(const lbm_dims& d);
+
+// Mode 0: tunnel k's steps go to lane k; lanes fork from and join back into
+// the batch stream, so a captured graph holds T independent chains that the
+// GPU runs concurrently, each launch with its own constant-bank parameters.
+cudaError_t launch_chains(lbm_batch* b, int parity, int nsteps) {
+  cudaError_t e = cudaEventRecord(b->fork, b->stream);
+  if (e != cudaSuccess) return e;
+  for (size_t k = 0; k < b->host.size(); ++k) {
+    cudaStream_t L = b->lanes[k];
+    if ((e = cudaStreamWaitEvent(L, b->fork, 0)) != cudaSuccess) return e;
+    const TunnelDesc& D = b->host[k];
+    for (int s = 0; s < nsteps; ++s) {
+      e = b->ops.step(D.d, D.P, (parity + s) & 1, true, false, false, b->fast, tunnel_launch(b->dims[k]), L);
+      if (e != cudaSuccess) return e;
+    }
+    if ((e = cudaEventRecord(b->joins[k], L)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(b->stream, b->joins[k], 0)) != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 int check_ready(lbm_batch* b) {
@@ -214,6 +272,8 @@ int check_ready(lbm_batch* b) {
 
 Launch tunnel_launch(const lbm_dims& d) {
   Launch L;
+  L.occ = 8;
+  L.pipe = 0;
   const int bx = d.nx < 64 ? ((d.nx + 31) / 32) * 32 : 64;
   L.block = dim3(bx, 1, 1);
   L.grid = dim3((d.nx + bx - 1) / bx, d.ny, d.nz);
@@ -259,10 +319,6 @@ int lbm_batch_create(const lbm_dims* dims, int ntunnels, int storage, int flags,
     b->cells += N;
   }
   void* p = nullptr;
-  if (!r) r = balloc(b, &p, sizeof(TunnelDesc) * ntunnels, "descriptors");
-  b->d_desc = static_cast<TunnelDesc*>(p);
-  if (!r) r = balloc(b, &p, sizeof(long long) * (ntunnels + 1), "tile prefix");
-  b->d_first = static_cast<long long*>(p);
   if (!r) r = balloc(b, &p, 3 * sizeof(double), "reduction result");
   b->red = static_cast<double*>(p);
   if (r) { lbm_batch_destroy(b); return r; }
@@ -288,6 +344,9 @@ int lbm_batch_destroy(lbm_batch* b) {
   if (!b) return bfail(LBM_EINVAL, "null batch");
   if (b->stream) cudaStreamSynchronize(b->stream);
   drop_graphs(b);
+  for (cudaStream_t L : b->lanes) cudaStreamDestroy(L);
+  for (cudaEvent_t e : b->joins) cudaEventDestroy(e);
+  if (b->fork) cudaEventDestroy(b->fork);
   for (void* p : b->allocs) cudaFree(p);
   if (b->partials) cudaFree(b->partials);
   if (b->stage) cudaFree(b->stage);
@@ -364,13 +423,25 @@ int lbm_batch_step(lbm_batch* b, int n) {
   if (n < 0) return bfail(LBM_EINVAL, "negative step count");
   if ((r = sync_desc(b))) return r;
   const int G = b->graph_steps;
+  if (b->mode == 0 && b->lanes.empty()) {
+    b->lanes.resize(b->host.size());
+    b->joins.resize(b->host.size());
+    for (size_t k = 0; k < b->host.size(); ++k) {
+      BCK(cudaStreamCreateWithFlags(&b->lanes[k], cudaStreamNonBlocking), "lane stream");
+      BCK(cudaEventCreateWithFlags(&b->joins[k], cudaEventDisableTiming), "lane event");
+    }
+    BCK(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming), "fork event");
+  }
   while (n >= G) {
     const int par = (int)(b->steps & 1);
     if (!b->graph[par]) {
       cudaGraph_t g;
       BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "graph capture begin");
-      for (int s = 0; s < G; ++s) launch_one(b, (par + s) & 1);
+      cudaError_t ce = cudaSuccess;
+      if (b->mode == 0) ce = launch_chains(b, par, G);
+      else for (int s = 0; s < G; ++s) launch_one(b, (par + s) & 1);
       cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+      if (ce != cudaSuccess) e = ce;
       if (e != cudaSuccess) return bfail(LBM_ECUDA, std::string("graph capture: ") + cudaGetErrorString(e));
       e = cudaGraphInstantiate(&b->graph[par], g, 0);
       cudaGraphDestroy(g);
@@ -379,6 +450,11 @@ int lbm_batch_step(lbm_batch* b, int n) {
     BCK(cudaGraphLaunch(b->graph[par], b->stream), "graph launch");
     b->steps += G;
     n -= G;
+  }
+  if (n > 0 && b->mode == 0) {
+    BCK(launch_chains(b, (int)(b->steps & 1), n), "batch step launch");
+    b->steps += n;
+    n = 0;
   }
   for (; n > 0; --n) {
     launch_one(b, (int)(b->steps & 1));
@@ -426,6 +502,16 @@ int lbm_batch_forces(lbm_batch* b, double* f) {
     BCK(cudaMemcpyAsync(f + 3 * k, b->red, 3 * sizeof(double), cudaMemcpyDeviceToHost, b->stream), "force download");
   }
   BCK(cudaStreamSynchronize(b->stream), "force sync");
+  return LBM_OK;
+}
+
+int lbm_batch_set_mode(lbm_batch* b, int mode) {
+  if (!b) return bfail(LBM_EINVAL, "null batch");
+  if (mode != 0 && mode != 1) return bfail(LBM_EINVAL, "mode must be 0 (graph of tunnel chains) or 1 (persistent launch)");
+  BCK(cudaStreamSynchronize(b->stream), "stream sync");
+  if (mode != b->mode) drop_graphs(b);
+  b->desc_dirty = true;
+  b->mode = mode;
   return LBM_OK;
 }
 

@@ -121,21 +121,25 @@ def lote(n_tunnels=64, steps=256, storages=("f32", "f16s"), seed=2026):
            "omega_flagged": int(sum(t[3]["flag_omega"] for t in tun)), "forms": {}}
     stream = torch.cuda.Stream()
     for st in storages:
-        L = LoteCUDA([t[0] for t in tun], storage=st)
-        L.definirStream(stream.cuda_stream)
-        for k, (g, tipo, cfg, info) in enumerate(tun):
-            L.definirTipos(k, tipo)
-            L.configurar(k, **cfg)
-        L.inicializar()
-        L.passo(64)
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        L.passo(steps)
-        e1.record(stream)
-        e1.synchronize()
-        ms_batch = e0.elapsed_time(e1)
-        L.destruir()
+        ms_modes = {}
+        for modo in (0, 1):
+            L = LoteCUDA([t[0] for t in tun], storage=st)
+            L.definirStream(stream.cuda_stream)
+            L.definirModo(modo)
+            for k, (g, tipo, cfg, info) in enumerate(tun):
+                L.definirTipos(k, tipo)
+                L.configurar(k, **cfg)
+            L.inicializar()
+            L.passo(64)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            L.passo(steps)
+            e1.record(stream)
+            e1.synchronize()
+            ms_modes[modo] = e0.elapsed_time(e1)
+            L.destruir()
+        ms_batch = ms_modes[0]
         ms_seq = 0.0
         for g, tipo, cfg, info in tun:
             s = SolverCUDA(g, storage=st, escrever_macros=False)
@@ -152,6 +156,7 @@ def lote(n_tunnels=64, steps=256, storages=("f32", "f16s"), seed=2026):
             ms_seq += e0.elapsed_time(e1)
             s.destruir()
         out["forms"][st] = {"batched_MLUPS": cells * steps / (ms_batch / 1e3) / 1e6,
+                            "persistent_launch_MLUPS": cells * steps / (ms_modes[1] / 1e3) / 1e6,
                             "sequential_MLUPS": cells * steps / (ms_seq / 1e3) / 1e6,
                             "speedup": ms_seq / ms_batch}
     return out

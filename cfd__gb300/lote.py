@@ -68,6 +68,10 @@ class LoteCUDA:
     def definirLadrilho(self, k, tile_x):
         nat.check(self._lib.lbm_batch_set_tile(self._h, int(k), int(tile_x)))
 
+    def definirModo(self, modo):
+        """0: graph of per-tunnel chains (default); 1: one persistent launch per step."""
+        nat.check(self._lib.lbm_batch_set_mode(self._h, int(modo)))
+
     def definirStream(self, ptr):
         nat.check(self._lib.lbm_batch_set_stream(self._h, C.c_void_p(ptr)))
 

@@ -4,10 +4,11 @@
  * The reference runs one tunnel per solver object and one compute dispatch
  * per tunnel step (src/backend/webgpu/solver.js:395-415).  A batch holds T
  * independent tunnels (each with its own grid, cell types and parameters —
- * the same data as one lbm_ctx) and advances all of them with ONE persistent
- * kernel launch per step: a fixed grid of CTAs walks the tiles of every
- * tunnel.  lbm_batch_step captures the launches into a CUDA graph and
- * replays it.  Arithmetic is identical to lbm_step (same per-cell code), so
+ * the same data as one lbm_ctx) and advances all of them together.
+ * lbm_batch_step captures 32 steps of every tunnel into a CUDA graph and
+ * replays it: by default one independent chain of single-tunnel launches per
+ * tunnel (the GPU overlaps the chains), or (lbm_batch_set_mode 1) one
+ * persistent launch per step whose CTAs walk the tiles of every tunnel.  Arithmetic is identical to lbm_step (same per-cell code), so
  * each tunnel's state equals the state a separate lbm_ctx would reach.
  * Storage forms: LBM_F32, LBM_F16S, LBM_BF16S (in-place layout only).
  */
@@ -40,6 +41,11 @@ int lbm_batch_forces(lbm_batch* b, double* f);
 /* tile width along x of tunnel k (32, 64 or 128 threads; the tile is 128
  * threads); 0 = the cost model (least idle threads) */
 int lbm_batch_set_tile(lbm_batch* b, int k, int tile_x);
+/* 0 (default): each step of each tunnel is its own launch of the
+ * single-tunnel kernel; the captured graph holds one chain per tunnel and
+ * the GPU runs the chains concurrently.  1: one persistent launch per step
+ * walks the tiles of all tunnels (descriptors in the launch parameters). */
+int lbm_batch_set_mode(lbm_batch* b, int mode);
 int lbm_batch_info(lbm_batch* b, int64_t* total_cells, int64_t* device_bytes);
 
 #ifdef __cplusplus

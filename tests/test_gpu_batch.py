@@ -14,11 +14,13 @@ def _tunnels():
 
 @pytest.mark.parametrize("storage", ["f32", "f16s"])
 @pytest.mark.parametrize("tile", [0, 32])
-def test_batch_equals_separate_solvers(native, storage, tile):
+@pytest.mark.parametrize("mode", [0, 1])
+def test_batch_equals_separate_solvers(native, storage, tile, mode):
     from cfd__gb300 import SolverCUDA
     from cfd__gb300.lote import LoteCUDA
     tun = _tunnels()
     lote = LoteCUDA([t[0] for t in tun], storage=storage)
+    lote.definirModo(mode)
     solos = []
     for k, (g, tipo, cfg, info) in enumerate(tun):
         lote.definirTipos(k, tipo)
