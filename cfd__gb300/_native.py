@@ -55,6 +55,24 @@ class VoxStats(C.Structure):
                 ("ms_flood", C.c_float), ("ms_total", C.c_float), ("_pad", C.c_float)]
 
 
+CLOSURE_IN, CLOSURE_H = 6, 32
+CLOSURE_NPARAM = CLOSURE_H * CLOSURE_IN + CLOSURE_H + CLOSURE_H * CLOSURE_H + CLOSURE_H + CLOSURE_H + 1
+
+
+class ClosureWeights(C.Structure):
+    _fields_ = [("w1", C.c_float * (CLOSURE_H * CLOSURE_IN)), ("b1", C.c_float * CLOSURE_H),
+                ("w2", C.c_float * (CLOSURE_H * CLOSURE_H)), ("b2", C.c_float * CLOSURE_H),
+                ("w3", C.c_float * CLOSURE_H), ("b3", C.c_float),
+                ("mean", C.c_float * CLOSURE_IN), ("std", C.c_float * CLOSURE_IN),
+                ("nu_scale", C.c_float), ("nu_max", C.c_float)]
+
+
+class ClosureCfg(C.Structure):
+    _fields_ = [("steps", C.c_int32), ("batch", C.c_int32), ("lr", C.c_float), ("beta1", C.c_float),
+                ("beta2", C.c_float), ("eps", C.c_float), ("seed", C.c_uint64), ("init", C.c_int32),
+                ("_pad", C.c_int32)]
+
+
 _lib = None
 _lock = threading.Lock()
 
@@ -92,6 +110,14 @@ SIGNATURES = {
     "lbm_batch_set_tile": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "lbm_batch_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "lbm_batch_set_mode": (C.c_int, [C.c_void_p, C.c_int]),
+    "closure_train": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.POINTER(ClosureCfg),
+                                C.POINTER(ClosureWeights), C.c_void_p]),
+    "closure_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.POINTER(ClosureWeights),
+                               C.POINTER(C.c_float), C.c_void_p]),
+    "closure_eval": (C.c_int, [C.POINTER(ClosureWeights), C.c_void_p, C.c_size_t, C.c_void_p]),
+    "closure_samples": (C.c_int, [C.c_void_p, C.c_float, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_size_t]),
+    "lbm_set_closure": (C.c_int, [C.c_void_p, C.POINTER(ClosureWeights)]),
+    "lbm_closure_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "vox_voxelize": (C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.POINTER(Dims), C.c_float, C.c_int,
                                C.c_void_p, C.c_void_p, C.POINTER(VoxStats)]),
 }

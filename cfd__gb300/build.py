@@ -38,6 +38,7 @@ UNITS = {
     "vox.cu": ["-fmad=false"],
     "lbm_noalloc.cu": ["-fmad=false"],
     "lbm_batch.cu": ["-fmad=false"],
+    "closure.cu": ["-fmad=false"],
 }
 
 

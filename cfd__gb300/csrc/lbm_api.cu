@@ -13,6 +13,7 @@
 #include <vector>
 
 #include "../../include/lbm.h"
+#include "../../include/lbm_closure.h"
 #include "lbm_kernels.cuh"
 
 using namespace lbm;
@@ -130,7 +131,18 @@ struct lbm_ctx {
   int occ = 8;
   int pipe = 0;
   int64_t dev_bytes = 0;
+  // learned closure
+  lbm::MlpFrag* clo = nullptr;            // fragments of the network (device)
+  unsigned long long* clo_fb = nullptr;   // fallback counter (device)
+  int64_t clo_steps = 0;                  // closure steps since the last stats call
+  int64_t n_fluido = 0;                   // FLUIDO cells of the current types
 };
+
+namespace lbm {
+void closure_pack(const closure_weights* w, MlpFrag* F);
+cudaError_t closure_samples_launch(const float4* mac, const uint8_t* tipo, int nx, int ny, int nz, float tau0c,
+                                   int x0, int x1, float* feats_dev, float* target_dev, cudaStream_t s);
+}
 
 namespace {
 
@@ -218,6 +230,17 @@ int check_ready(lbm_ctx* c, bool need_cfg) {
 int launch_step(lbm_ctx* c, bool mac, double* force) {
   Dev d = dev_of(c);
   d.force = force;
+  if (c->P.closure == 1) {
+    if (!c->clo) return fail(LBM_ESTATE, "closure = 1 but no network set (call lbm_set_closure first)");
+    if (!c->inplace || (c->flags & LBM_FLAG_STRICT) || !c->ops.step_closure)
+      return fail(LBM_ENOTSUP, "the learned closure runs in the in-place FAST step with fp32 arithmetic only");
+    cudaError_t e = c->ops.step_closure(d, c->P, parity(c), mac, force != nullptr, c->clo, c->clo_fb,
+                                        cell_launch(c), c->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "closure step kernel launch");
+    c->steps++;
+    c->clo_steps++;
+    return LBM_OK;
+  }
   cudaError_t e = c->ops.step(d, c->P, parity(c), c->inplace, mac, force != nullptr, !(c->flags & LBM_FLAG_STRICT),
                               cell_launch(c), c->stream);
   if (e != cudaSuccess) return cuda_fail(e, "step kernel launch");
@@ -273,7 +296,7 @@ int lbm_create(const lbm_dims* dims, int storage, int flags, lbm_ctx** out) {
 int lbm_destroy(lbm_ctx* c) {
   if (!c) return fail(LBM_EINVAL, "null context");
   if (c->stream) cudaStreamSynchronize(c->stream);
-  void* ps[] = {c->pop, c->pop2, c->tipo, c->link, c->macros, c->partials, c->red, c->fbuf, c->stage};
+  void* ps[] = {c->pop, c->pop2, c->tipo, c->link, c->macros, c->partials, c->red, c->fbuf, c->stage, c->clo, c->clo_fb};
   for (void* p : ps)
     if (p) cudaFree(p);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -319,6 +342,9 @@ int lbm_set_types(lbm_ctx* c, const uint32_t* tipo, size_t n) {
     }
     t8[i] = (uint8_t)tipo[i];
   }
+  int64_t nf = 0;
+  for (size_t i = 0; i < n; ++i) nf += t8[i] == LBM_FLUIDO;
+  c->n_fluido = nf;
   CK(cudaMemcpyAsync(c->tipo, t8.data(), n, cudaMemcpyHostToDevice, c->stream), "types upload");
   if (c->inplace) {
     Launch L = cell_launch(c);
@@ -460,6 +486,66 @@ int lbm_mass(lbm_ctx* c, double* sum) {
 int lbm_sync(lbm_ctx* c) {
   if (!c) return fail(LBM_EINVAL, "null context");
   CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+  return LBM_OK;
+}
+
+int lbm_set_closure(lbm_ctx* c, const closure_weights* w) {
+  if (!c || !w) return fail(LBM_EINVAL, "null argument");
+  if (!c->ops.step_closure || !c->inplace || (c->flags & LBM_FLAG_STRICT))
+    return fail(LBM_ENOTSUP, "the learned closure runs in the in-place FAST step with fp32 arithmetic only");
+  lbm::MlpFrag F;
+  lbm::closure_pack(w, &F);
+  if (!c->clo) {
+    int r = dalloc(c, (void**)&c->clo, sizeof(lbm::MlpFrag), "closure network");
+    if (r) return r;
+    r = dalloc(c, (void**)&c->clo_fb, sizeof(unsigned long long), "closure counter");
+    if (r) return r;
+    CK(cudaMemsetAsync(c->clo_fb, 0, sizeof(unsigned long long), c->stream), "closure counter clear");
+  }
+  CK(cudaMemcpyAsync(c->clo, &F, sizeof F, cudaMemcpyHostToDevice, c->stream), "closure upload");
+  CK(cudaStreamSynchronize(c->stream), "closure upload sync");
+  return LBM_OK;
+}
+
+int closure_samples(lbm_ctx* c, float tau0_coarse, int x0, int x1, float* feats, float* target, size_t rows) {
+  if (!c || !feats || !target) return fail(LBM_EINVAL, "null argument");
+  int r = check_ready(c, false);
+  if (r) return r;
+  const int cx_ = c->dims.nx / 2, cy_ = c->dims.ny / 2, cz_ = c->dims.nz / 2;
+  if (cx_ < 3 || cy_ < 3 || cz_ < 3) return fail(LBM_EINVAL, "fine grid too small for a 2x coarse grid");
+  if (x0 < 0 || x1 > cx_ || x0 >= x1) return fail(LBM_EINVAL, "bad coarse x range");
+  const size_t nr = (size_t)(x1 - x0) * cy_ * cz_;
+  if (rows != nr) return fail(LBM_EINVAL, "rows must be (x1 - x0) * (ny/2) * (nz/2)");
+  if (!(tau0_coarse > 0.5f)) return fail(LBM_EINVAL, "tau0_coarse must exceed 1/2");
+  if ((r = lbm_update_macros(c))) return r;
+  float *df = nullptr, *dt = nullptr;
+  if ((r = dalloc(c, (void**)&df, sizeof(float) * 6 * nr, "sample features"))) return r;
+  if ((r = dalloc(c, (void**)&dt, sizeof(float) * nr, "sample targets"))) {
+    cudaFree(df); c->dev_bytes -= sizeof(float) * 6 * nr;
+    return r;
+  }
+  cudaError_t e = lbm::closure_samples_launch(c->macros, c->tipo, c->dims.nx, c->dims.ny, c->dims.nz, tau0_coarse,
+                                              x0, x1, df, dt, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpy(feats, df, sizeof(float) * 6 * nr, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(target, dt, sizeof(float) * nr, cudaMemcpyDeviceToHost);
+  cudaFree(df);
+  cudaFree(dt);
+  c->dev_bytes -= sizeof(float) * 7 * nr;
+  if (e != cudaSuccess) return cuda_fail(e, "closure samples");
+  return LBM_OK;
+}
+
+int lbm_closure_stats(lbm_ctx* c, int64_t* fallback_cells, int64_t* fluid_cells) {
+  if (!c || !fallback_cells || !fluid_cells) return fail(LBM_EINVAL, "null argument");
+  unsigned long long fb = 0;
+  if (c->clo_fb) {
+    CK(cudaMemcpyAsync(&fb, c->clo_fb, sizeof fb, cudaMemcpyDeviceToHost, c->stream), "closure counter download");
+    CK(cudaMemsetAsync(c->clo_fb, 0, sizeof fb, c->stream), "closure counter clear");
+    CK(cudaStreamSynchronize(c->stream), "closure counter sync");
+  }
+  *fallback_cells = (int64_t)fb;
+  *fluid_cells = c->n_fluido * c->clo_steps;
+  c->clo_steps = 0;
   return LBM_OK;
 }
 

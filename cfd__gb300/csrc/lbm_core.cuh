@@ -271,6 +271,91 @@ inline Uni<R> make_uni(const Params& P) {
   return u;
 }
 
+// ---- FAST fluid path in three pieces (the learned closure runs its network
+// between the first and the last) ----
+
+// Pair form of the shifted equilibrium (c_j = -c_i, w_j = w_i):
+//   e_i + e_j = 2 w (delta + rho (4.5 cu^2 - 1.5 uu)),  e_i - e_j = 6 w rho cu;
+// ns = (g_i + g_j) - (e_i + e_j), nd = (g_i - g_j) - (e_i - e_j).
+template <typename R>
+__device__ __forceinline__ void fluid_neq_fast(const R* sp, const R* dp, R delta, R rho, R ux, R uy, R uz, R uu,
+                                               R& e0, R* ns, R* nd) {
+  const R uu15 = R(1.5) * uu;
+  e0 = Lit<R>::w(0) * fma_r<R>(-rho, uu15, delta);
+  const R r6a = (R(6.0) * Lit<R>::w(1)) * rho, r6d = (R(6.0) * Lit<R>::w(7)) * rho;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    const int i = 2 * k + 1;
+    const R cu = dotc<R>(i, ux, uy, uz);
+    const R a2 = fma_r<R>(R(4.5) * cu, cu, -uu15);
+    const R es = (R(2.0) * Lit<R>::w(i)) * fma_r<R>(rho, a2, delta);
+    const R ed = (i <= 6 ? r6a : r6d) * cu;
+    ns[k] = sp[k] - es;
+    nd[k] = dp[k] - ed;
+  }
+}
+
+// Pi_ab = sum over pairs of c_ia c_ib ns (src/core/emit/ir.js:269-282, pair form)
+template <typename R>
+struct PiT {
+  R xx, yy, zz, xy, xz, yz;
+};
+template <typename R>
+__device__ __forceinline__ PiT<R> pi_fast(const R* ns) {
+  PiT<R> p;
+  p.xx = pair_sum<R>(ns, [](int i) { return cx(i) * cx(i); });
+  p.yy = pair_sum<R>(ns, [](int i) { return cy(i) * cy(i); });
+  p.zz = pair_sum<R>(ns, [](int i) { return cz(i) * cz(i); });
+  p.xy = pair_sum<R>(ns, [](int i) { return cx(i) * cy(i); });
+  p.xz = pair_sum<R>(ns, [](int i) { return cx(i) * cz(i); });
+  p.yz = pair_sum<R>(ns, [](int i) { return cy(i) * cz(i); });
+  return p;
+}
+
+// Smagorinsky relaxation rates (src/core/emit/ir.js:284-299), FAST form.
+template <typename R>
+__device__ __forceinline__ void smag_rates_fast(const Params& P, const Uni<R>& U, const R* ns, R rinv, R& omegaP,
+                                                R& omegaM) {
+  omegaP = U.omegaP0f;
+  omegaM = U.omegaM0f;
+  if (U.les_on) {
+    const PiT<R> q = pi_fast<R>(ns);
+    const R pd = fma_r<R>(q.zz, q.zz, fma_r<R>(q.yy, q.yy, q.xx * q.xx));
+    const R po = fma_r<R>(q.yz, q.yz, fma_r<R>(q.xz, q.xz, q.xy * q.xy));
+    const R pp = fma_r<R>(R(2.0), po, pd);
+    const R qs = r_sqrt(R(2.0) * pp);
+    const R tauT = R(0.5) * (U.tau0 + r_sqrt(fma_r<R>(U.c18 * qs, rinv, U.tau0sq)));
+    omegaP = R(1.0) / tauT;
+    const R tm = tauT - R(0.5);
+    omegaM = tm / fma_r<R>(R(0.5), tm, R(P.magic));
+  }
+}
+
+// TRT per pair and the sponge blend (src/core/emit/ir.js:304-323, :458-478).
+template <typename R, typename Emit>
+__device__ __forceinline__ void trt_emit_fast(const Uni<R>& U, int x, const R* g, R e0, const R* ns, const R* nd,
+                                              R omegaP, R omegaM, Emit&& emit) {
+  R sig2 = R(0.0);
+  if (R(x) > U.sp_start) {
+    const R sx = (R(x) - U.sp_start) / U.sp_len;
+    const R sigma = sx < R(1.0) ? sx : R(1.0);
+    sig2 = sigma * sigma;
+  }
+  const bool sponge = sig2 != R(0.0);
+  const R oms = R(1.0) - sig2;
+  auto blend = [&](int i, R o) -> R { return sponge ? fma_r<R>(U.sp_tf[i], sig2, o * oms) : o; };
+  emit(0, blend(0, fma_r<R>(-omegaP, g[0] - e0, g[0])));
+  const R hP = R(0.5) * omegaP, hM = R(0.5) * omegaM;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    const int i = 2 * k + 1, j = i + 1;
+    const R oi = fma_r<R>(-hM, nd[k], fma_r<R>(-hP, ns[k], g[i]));
+    const R oj = fma_r<R>(hM, nd[k], fma_r<R>(-hP, ns[k], g[j]));
+    emit(i, blend(i, oi));
+    emit(j, blend(j, oj));
+  }
+}
+
 // Everything after the pull for one non-solid cell: the boundary branches and
 // the fluid collide with LES, TRT and sponge (src/core/emit/ir.js:505-530).
 // g: pulled populations.  Each post-collision population is handed to
@@ -336,69 +421,33 @@ __device__ __forceinline__ void collide(const Params& P, const Uni<R>& U, uint32
     return;
   }
   // FLUIDO: equilibrium, Smagorinsky LES (src/core/emit/ir.js:262-301)
-  R omegaP, omegaM;
-  R e0;
-  R ns[9], nd[9];     // FAST: (g_i + g_j) - (e_i + e_j), (g_i - g_j) - (e_i - e_j)
-  R e[Q];             // STRICT: every e_i
   if (FAST) {
-    // Pair form of the shifted equilibrium (c_j = -c_i, w_j = w_i):
-    //   e_i + e_j = 2 w (delta + rho (4.5 cu^2 - 1.5 uu)),  e_i - e_j = 6 w rho cu.
-    const R uu15 = R(1.5) * uu;
-    e0 = Lit<R>::w(0) * fma_r<R>(-rho, uu15, delta);
-    const R r6a = (R(6.0) * Lit<R>::w(1)) * rho, r6d = (R(6.0) * Lit<R>::w(7)) * rho;
-#pragma unroll
-    for (int k = 0; k < 9; ++k) {
-      const int i = 2 * k + 1;
-      const R cu = dotc<R>(i, ux, uy, uz);
-      const R a2 = fma_r<R>(R(4.5) * cu, cu, -uu15);
-      const R es = (R(2.0) * Lit<R>::w(i)) * fma_r<R>(rho, a2, delta);
-      const R ed = (i <= 6 ? r6a : r6d) * cu;
-      ns[k] = sp[k] - es;
-      nd[k] = dp[k] - ed;
-    }
-    omegaP = U.omegaP0f;
-    omegaM = U.omegaM0f;
-    if (U.les_on) {
-      // Pi_ab = sum over pairs of c_ia c_ib ((g_i + g_j) - (e_i + e_j))
-      const R pxx = pair_sum<R>(ns, [](int i) { return cx(i) * cx(i); });
-      const R pyy = pair_sum<R>(ns, [](int i) { return cy(i) * cy(i); });
-      const R pzz = pair_sum<R>(ns, [](int i) { return cz(i) * cz(i); });
-      const R pxy = pair_sum<R>(ns, [](int i) { return cx(i) * cy(i); });
-      const R pxz = pair_sum<R>(ns, [](int i) { return cx(i) * cz(i); });
-      const R pyz = pair_sum<R>(ns, [](int i) { return cy(i) * cz(i); });
-      const R pd = fma_r<R>(pzz, pzz, fma_r<R>(pyy, pyy, pxx * pxx));
-      const R po = fma_r<R>(pyz, pyz, fma_r<R>(pxz, pxz, pxy * pxy));
-      const R pp = fma_r<R>(R(2.0), po, pd);
-      const R qs = r_sqrt(R(2.0) * pp);
-      const R tauT = R(0.5) * (U.tau0 + r_sqrt(fma_r<R>(U.c18 * qs, rinv, U.tau0sq)));
-      omegaP = R(1.0) / tauT;
-      const R tm = tauT - R(0.5);
-      omegaM = tm / fma_r<R>(R(0.5), tm, R(P.magic));
-    }
-  } else {
-#pragma unroll
-    for (int i = 0; i < Q; ++i) e[i] = equilibrium<R, false>(i, delta, rho, ux, uy, uz, uu, R(0.0));
-    e0 = e[0];
-    omegaP = U.omegaP0;
-    omegaM = U.omegaM0;
-    if (U.les_on) {
-      R n[Q];
-#pragma unroll
-      for (int i = 0; i < Q; ++i) n[i] = g[i] - e[i];
-      const R pxx = signed_sum<R>(n, [](int i) { return cx(i) * cx(i); });
-      const R pyy = signed_sum<R>(n, [](int i) { return cy(i) * cy(i); });
-      const R pzz = signed_sum<R>(n, [](int i) { return cz(i) * cz(i); });
-      const R pxy = signed_sum<R>(n, [](int i) { return cx(i) * cy(i); });
-      const R pxz = signed_sum<R>(n, [](int i) { return cx(i) * cz(i); });
-      const R pyz = signed_sum<R>(n, [](int i) { return cy(i) * cz(i); });
-      const R pp = pxx * pxx + pyy * pyy + pzz * pzz + R(2.0) * (pxy * pxy + pxz * pxz + pyz * pyz);
-      const R qs = r_sqrt(R(2.0) * pp);
-      const R tauT = R(0.5) * (U.tau0 + r_sqrt(U.tau0sq + U.c18 * qs / rho));
-      omegaP = R(1.0) / tauT;
-      omegaM = R(1.0) / (R(P.magic) / (R(1.0) / omegaP - R(0.5)) + R(0.5));
-    }
+    R e0, ns[9], nd[9], omegaP, omegaM;
+    fluid_neq_fast<R>(sp, dp, delta, rho, ux, uy, uz, uu, e0, ns, nd);
+    smag_rates_fast<R>(P, U, ns, rinv, omegaP, omegaM);
+    trt_emit_fast<R>(U, x, g, e0, ns, nd, omegaP, omegaM, emit);
+    return;
   }
-
+  R e[Q];
+#pragma unroll
+  for (int i = 0; i < Q; ++i) e[i] = equilibrium<R, false>(i, delta, rho, ux, uy, uz, uu, R(0.0));
+  R omegaP = U.omegaP0, omegaM = U.omegaM0;
+  if (U.les_on) {
+    R n[Q];
+#pragma unroll
+    for (int i = 0; i < Q; ++i) n[i] = g[i] - e[i];
+    const R pxx = signed_sum<R>(n, [](int i) { return cx(i) * cx(i); });
+    const R pyy = signed_sum<R>(n, [](int i) { return cy(i) * cy(i); });
+    const R pzz = signed_sum<R>(n, [](int i) { return cz(i) * cz(i); });
+    const R pxy = signed_sum<R>(n, [](int i) { return cx(i) * cy(i); });
+    const R pxz = signed_sum<R>(n, [](int i) { return cx(i) * cz(i); });
+    const R pyz = signed_sum<R>(n, [](int i) { return cy(i) * cz(i); });
+    const R pp = pxx * pxx + pyy * pyy + pzz * pzz + R(2.0) * (pxy * pxy + pxz * pxz + pyz * pyz);
+    const R qs = r_sqrt(R(2.0) * pp);
+    const R tauT = R(0.5) * (U.tau0 + r_sqrt(U.tau0sq + U.c18 * qs / rho));
+    omegaP = R(1.0) / tauT;
+    omegaM = R(1.0) / (R(P.magic) / (R(1.0) / omegaP - R(0.5)) + R(0.5));
+  }
   // Sponge weight (src/core/emit/ir.js:458-463): zero for x <= start, where
   // the blend a (1 - 0) + b 0 leaves every population unchanged.
   R sig2 = R(0.0);
@@ -409,27 +458,9 @@ __device__ __forceinline__ void collide(const Params& P, const Uni<R>& U, uint32
   }
   const bool sponge = sig2 != R(0.0);
   const R oms = R(1.0) - sig2;
-  auto blend = [&](int i, R o) -> R {
-    if (!sponge) return o;
-    return FAST ? fma_r<R>(U.sp_tf[i], sig2, o * oms) : o * oms + U.sp_t[i] * sig2;
-  };
-
-  // TRT per opposite pair (src/core/emit/ir.js:304-323), each output blended
-  // with the sponge target, mix(a, b, t) = a (1 - t) + b t.
-  if (FAST) {
-    emit(0, blend(0, fma_r<R>(-omegaP, g[0] - e0, g[0])));
-    const R hP = R(0.5) * omegaP, hM = R(0.5) * omegaM;
-#pragma unroll
-    for (int k = 0; k < 9; ++k) {
-      const int i = 2 * k + 1, j = i + 1;
-      const R oi = fma_r<R>(-hM, nd[k], fma_r<R>(-hP, ns[k], g[i]));
-      const R oj = fma_r<R>(hM, nd[k], fma_r<R>(-hP, ns[k], g[j]));
-      emit(i, blend(i, oi));
-      emit(j, blend(j, oj));
-    }
-    return;
-  }
-  emit(0, blend(0, g[0] - omegaP * (g[0] - e0)));
+  auto blend = [&](int i, R o) -> R { return sponge ? o * oms + U.sp_t[i] * sig2 : o; };
+  // TRT per opposite pair (src/core/emit/ir.js:304-323), mix(a, b, t) = a (1 - t) + b t
+  emit(0, blend(0, g[0] - omegaP * (g[0] - e[0])));
 #pragma unroll
   for (int i = 1; i < Q; i += 2) {
     const int j = i + 1;

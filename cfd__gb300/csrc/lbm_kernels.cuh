@@ -24,6 +24,7 @@
 //    neighbours of src into dst, types gathered per direction.  Kept as the
 //    faithful debug path; both layouts give bit-identical states.
 #pragma once
+#include "closure_mlp.cuh"
 #include "lbm_core.cuh"
 
 namespace lbm {
@@ -224,6 +225,151 @@ k_step_inplace(Dev d, Params P, Uni<typename St::real> U) {
   const int z = blockIdx.z;
   double fx = 0.0, fy = 0.0, fz = 0.0;
   if (x < d.nx && y < d.ny) step_cell<St, PAR, MAC, FRC, W64, FAST>(d, P, U, x, y, z, fx, fy, fz);
+  if (FRC) {
+    const bool any = __any_sync(0xffffffffu, fx != 0.0 || fy != 0.0 || fz != 0.0);
+    if (any) warp_add3(fx, fy, fz, d.force);
+  }
+}
+
+// In-place step with the learned eddy-viscosity closure (fp32 arithmetic,
+// FAST form).  The same pull, bounce-back and fused force as step_cell; for
+// FLUIDO cells the six features of the pulled non-equilibrium stress feed
+// the warp's tensor-core MLP (every lane takes part, with zero features when
+// it has no fluid cell), which gives nu_t and tau = tau0 + 3 nu_t, omega-
+// keeping Lambda fixed.  A fluid cell whose network output is not usable
+// relaxes with the Smagorinsky rates (src/core/emit/ir.js:284-299) and is
+// counted in *nfb.  Every other class goes through collide() unchanged.
+template <class St, int PAR, bool MAC, bool FRC, bool W64>
+__global__ void __launch_bounds__(128, 6)
+k_step_closure(Dev d, Params P, Uni<float> U, const MlpFrag* __restrict__ F, unsigned long long* __restrict__ nfb,
+               float omega0) {
+  using R = float;
+  using S = typename St::store_t;
+  using Off = typename OffT<W64>::type;
+  static_assert(sizeof(typename St::real) == 4, "closure step is fp32 arithmetic");
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  const int nx = d.nx, ny = d.ny;
+  const bool inr = x < nx && y < ny;
+  const Off N = (Off)d.N;
+  const Off cell = ((Off)z * ny + y) * nx + x;
+  S* const Fc = static_cast<S*>(d.pop) + cell;
+  const Deltas<Off> D(x, y, z, nx, ny, d.nz);
+  constexpr bool E = (PAR == 0);
+  double fx = 0.0, fy = 0.0, fz = 0.0;
+  auto emit = [&](int i, R v) {
+    if (i == 0) {
+      St::st(Fc, v);
+    } else if (i & 1) {
+      St::st(Fc + D.odd(i) + (Off)(E ? i : i + 1) * N, v);
+    } else {
+      St::st(Fc + (Off)(E ? i : i - 1) * N, v);
+    }
+  };
+  // A fluid cell's pulled g and moments wait for the network in shared
+  // memory (column per thread), so that the registers of the pull and of the
+  // network are not live at the same time; the pair sums and the
+  // non-equilibrium parts are recomputed after it (same operations, same
+  // values).
+  constexpr int kStash = Q + 7;
+  __shared__ float stash[kStash][128];
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+  R g[Q];
+  R delta = R(0.0), rho = R(1.0), ux = R(0.0), uy = R(0.0), uz = R(0.0), uu = R(0.0), rinv = R(1.0);
+  float feat[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  bool fluid = false;
+  if (inr) {
+    const uint32_t lw = __ldg(d.link + cell);
+    g[0] = St::ld(Fc);
+#pragma unroll
+    for (int i = 1; i < Q; i += 2) {
+      g[i] = St::ld(Fc + (Off)(E ? i + 1 : i) * N);
+      g[i + 1] = St::ld(Fc + D.odd(i) + (Off)(E ? i : i + 1) * N);
+    }
+    const uint32_t ct = (lw >> LINK_CLASS_SHIFT) & 7u;
+    if (is_solid(ct)) {
+      if (MAC) d.macros[cell] = make_float4(0.f, 0.f, 0.f, 0.f);
+    } else {
+      const uint32_t bb = lw & 0x3ffffu;
+      if (bb) {
+#pragma unroll
+        for (int i = 1; i < Q; i += 2) {
+          if ((bb >> (i - 1)) & 1u) g[i] = St::ld(Fc + (Off)(E ? i : i + 1) * N);
+          if ((bb >> i) & 1u) g[i + 1] = St::ld(Fc + D.odd(i) + (Off)(E ? i + 1 : i) * N);
+        }
+        if (lw & LINK_SLOW) {
+          const Wrap w = wrap3(x, y, z, nx, ny, d.nz);
+#pragma unroll
+          for (int k = 1; k < Q; ++k) {
+            if (!((bb >> (k - 1)) & 1u)) continue;
+            const uint32_t t = d.tipo[nbr(k, -1, x, y, z, w, nx, ny)];
+            if (t == SOLIDO_MOVEL) g[k] = g[k] + Lit<R>::sixw(k) * (dotc<R>(k, R(P.belt[0]), R(P.belt[1]), R(P.belt[2])));
+            if (FRC && ct == FLUIDO && t == SOLIDO) {
+              const R q = R(2.0) * (g[k] + Lit<R>::w(k));
+              fx -= (double)(cx(k) * q); fy -= (double)(cy(k) * q); fz -= (double)(cz(k) * q);
+            }
+          }
+        } else if (FRC && ct == FLUIDO && (lw & LINK_BODY)) {
+#pragma unroll
+          for (int k = 1; k < Q; ++k) {
+            if (!((bb >> (k - 1)) & 1u)) continue;
+            const R q = R(2.0) * (g[k] + Lit<R>::w(k));
+            fx -= (double)(cx(k) * q); fy -= (double)(cy(k) * q); fz -= (double)(cz(k) * q);
+          }
+        }
+      }
+      R sp[9], dp[9];
+      moments_fast<R>(g, sp, dp, delta, rho, ux, uy, uz, uu, rinv);
+      if (MAC) d.macros[cell] = make_float4(ux, uy, uz, delta);
+      if (ct == FLUIDO) {
+        fluid = true;
+        R e0, ns[9], nd[9];
+        fluid_neq_fast<R>(sp, dp, delta, rho, ux, uy, uz, uu, e0, ns, nd);
+        const PiT<R> q = pi_fast<R>(ns);
+        closure_features(q.xx, q.yy, q.zz, q.xy, q.xz, q.yz, rinv, delta, feat);
+        feat[4] = omega0;
+#pragma unroll
+        for (int a = 0; a < 6; ++a) feat[a] = (feat[a] - __ldg(&F->mean[a])) * __ldg(&F->inv_std[a]);
+#pragma unroll
+        for (int i = 0; i < Q; ++i) stash[i][tid] = g[i];
+        stash[Q + 0][tid] = delta; stash[Q + 1][tid] = rho; stash[Q + 2][tid] = ux; stash[Q + 3][tid] = uy;
+        stash[Q + 4][tid] = uz; stash[Q + 5][tid] = uu; stash[Q + 6][tid] = rinv;
+      } else {
+        collide<R, true>(P, U, ct, x, z, g, sp, dp, delta, rho, ux, uy, uz, uu, rinv, emit);
+      }
+    }
+  }
+  __syncwarp();
+  const float yv = warp_mlp(*F, feat);
+  bool fell_back = false;
+  if (fluid) {
+#pragma unroll
+    for (int i = 0; i < Q; ++i) g[i] = stash[i][tid];
+    delta = stash[Q + 0][tid]; rho = stash[Q + 1][tid]; ux = stash[Q + 2][tid]; uy = stash[Q + 3][tid];
+    uz = stash[Q + 4][tid]; uu = stash[Q + 5][tid]; rinv = stash[Q + 6][tid];
+    R sp[9], dp[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      sp[k] = g[2 * k + 1] + g[2 * k + 2];
+      dp[k] = g[2 * k + 1] - g[2 * k + 2];
+    }
+    R e0, ns[9], nd[9];
+    fluid_neq_fast<R>(sp, dp, delta, rho, ux, uy, uz, uu, e0, ns, nd);
+    const float nu = closure_nu(*F, yv);
+    R omegaP, omegaM;
+    if (nu == nu) {
+      const float tauT = U.tau0 + 3.0f * nu, tm = tauT - 0.5f;
+      omegaP = __frcp_rn(tauT);
+      omegaM = __fdividef(tm, fmaf(0.5f, tm, P.magic));
+    } else {
+      fell_back = true;
+      smag_rates_fast<R>(P, U, ns, rinv, omegaP, omegaM);
+    }
+    trt_emit_fast<R>(U, x, g, e0, ns, nd, omegaP, omegaM, emit);
+  }
+  const unsigned fb = __ballot_sync(0xffffffffu, fell_back);
+  if (fb && (threadIdx.x & 31) == 0 && nfb) atomicAdd(nfb, (unsigned long long)__popc(fb));
   if (FRC) {
     const bool any = __any_sync(0xffffffffu, fx != 0.0 || fy != 0.0 || fz != 0.0);
     if (any) warp_add3(fx, fy, fz, d.force);
@@ -593,6 +739,9 @@ struct Ops {
   cudaError_t (*macros)(const Dev&, int parity, bool inplace, Launch, cudaStream_t);
   cudaError_t (*forces)(const Dev&, int parity, bool inplace, double* partials, Launch, cudaStream_t);
   cudaError_t (*mass)(const Dev&, int parity, bool inplace, double* partials, Launch, cudaStream_t);
+  // in-place FAST step with the learned closure; null for the fp64 judge
+  cudaError_t (*step_closure)(const Dev&, const Params&, int parity, bool mac, bool frc, const MlpFrag*,
+                              unsigned long long* fallback, Launch, cudaStream_t);
   int elem_bytes;
 };
 
@@ -676,10 +825,34 @@ struct OpsImpl {
     else k_mass<St, false><<<L.grid, L.block, 0, s>>>(d, parity, part);
     return cudaGetLastError();
   }
+  template <int PAR, bool MAC, bool FRC>
+  static void go_closure(const Dev& d, const Params& P, const Uni<float>& U, const MlpFrag* F,
+                         unsigned long long* nfb, Launch L, cudaStream_t s) {
+    if constexpr (sizeof(R) == 4) {
+      if ((int64_t)Q * d.N >= (int64_t)INT32_MAX) k_step_closure<St, PAR, MAC, FRC, true><<<L.grid, L.block, 0, s>>>(d, P, U, F, nfb, 1.0f / U.tau0);
+      else k_step_closure<St, PAR, MAC, FRC, false><<<L.grid, L.block, 0, s>>>(d, P, U, F, nfb, 1.0f / U.tau0);
+    }
+  }
+  static cudaError_t step_closure(const Dev& d, const Params& P, int parity, bool mac, bool frc, const MlpFrag* F,
+                                  unsigned long long* nfb, Launch L, cudaStream_t s) {
+    if constexpr (sizeof(R) == 4) {
+      const Uni<float> U = make_uni<float>(P);
+      if (parity == 0) {
+        if (mac) { frc ? go_closure<0, true, true>(d, P, U, F, nfb, L, s) : go_closure<0, true, false>(d, P, U, F, nfb, L, s); }
+        else { frc ? go_closure<0, false, true>(d, P, U, F, nfb, L, s) : go_closure<0, false, false>(d, P, U, F, nfb, L, s); }
+      } else {
+        if (mac) { frc ? go_closure<1, true, true>(d, P, U, F, nfb, L, s) : go_closure<1, true, false>(d, P, U, F, nfb, L, s); }
+        else { frc ? go_closure<1, false, true>(d, P, U, F, nfb, L, s) : go_closure<1, false, false>(d, P, U, F, nfb, L, s); }
+      }
+      return cudaGetLastError();
+    }
+    return cudaErrorNotSupported;
+  }
   static Ops make() {
     Ops o;
     o.step = &step; o.init = &init; o.put_dir = &put_dir; o.get_dir = &get_dir;
     o.macros = &macros; o.forces = &forces; o.mass = &mass;
+    o.step_closure = sizeof(R) == 4 ? &step_closure : nullptr;
     o.elem_bytes = (int)sizeof(typename St::store_t);
     return o;
   }

@@ -231,6 +231,20 @@ class SolverCUDA:
         register-cap variant (min resident blocks per SM: 8 or 6; 0 = default)."""
         nat.check(self._lib.lbm_set_launch(self._h, int(block_x), int(min_blocos)))
 
+    def definirFecho(self, pesos):
+        """Network of the learned closure (cfd__gb300.fecho weights dict);
+        configurar(closure=1) then selects it."""
+        from .fecho import para_struct
+        w = para_struct(pesos)
+        nat.check(self._lib.lbm_set_closure(self._h, C.byref(w)))
+        self.fontes["passo"] = "cfd__gb300/csrc/lbm_kernels.cuh:k_step_closure"
+
+    def estatisticasFecho(self):
+        """(fallback cells, fluid cells) over the closure steps since the last call."""
+        a, b = C.c_int64(), C.c_int64()
+        nat.check(self._lib.lbm_closure_stats(self._h, C.byref(a), C.byref(b)))
+        return int(a.value), int(b.value)
+
     def info(self):
         i = nat.Info()
         nat.check(self._lib.lbm_get_info(self._h, C.byref(i)))
