@@ -114,8 +114,10 @@ SIGNATURES = {
                                 C.POINTER(ClosureWeights), C.c_void_p]),
     "closure_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.POINTER(ClosureWeights),
                                C.POINTER(C.c_float), C.c_void_p]),
-    "closure_eval": (C.c_int, [C.POINTER(ClosureWeights), C.c_void_p, C.c_size_t, C.c_void_p]),
-    "closure_samples": (C.c_int, [C.c_void_p, C.c_float, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_size_t]),
+    "closure_eval": (C.c_int, [C.POINTER(ClosureWeights), C.c_void_p, C.c_size_t, C.c_int, C.c_void_p]),
+    "lbm_closure_engine": (C.c_int, [C.c_void_p, C.c_int]),
+    "closure_samples": (C.c_int, [C.c_void_p, C.c_float, C.c_float, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                  C.c_size_t]),
     "lbm_set_closure": (C.c_int, [C.c_void_p, C.POINTER(ClosureWeights)]),
     "lbm_closure_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "vox_voxelize": (C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.POINTER(Dims), C.c_float, C.c_int,

@@ -173,8 +173,8 @@ __global__ void k_adam(float* __restrict__ P, float* __restrict__ M, float* __re
   P[e] -= lr * (m * c1) / (sqrtf(v * c2) + eps);
 }
 
-// nu_t of feature rows through the step's tensor-core MLP (fragments read
-// from global memory, as in the fused step).
+// nu_t of feature rows through the step's warp engine (fragments read from
+// global memory, as in the fused step).
 __global__ void __launch_bounds__(128) k_eval(const float* __restrict__ feats, long long m,
                                               const MlpFrag* __restrict__ F, float* __restrict__ nu) {
   const long long i = (long long)blockIdx.x * 128 + threadIdx.x;
@@ -183,6 +183,23 @@ __global__ void __launch_bounds__(128) k_eval(const float* __restrict__ feats, l
   for (int a = 0; a < 6; ++a) x[a] = i < m ? (feats[i * 6 + a] - F->mean[a]) * F->inv_std[a] : 0.0f;
   const float y = warp_mlp(*F, x);
   if (i < m) nu[i] = closure_nu(*F, y);
+}
+
+// The same through the CTA-wide tcgen05 MLP (128 rows per block).
+__global__ void __launch_bounds__(128) k_eval_tc(const float* __restrict__ feats, long long m,
+                                                 const MlpFrag* __restrict__ F, float* __restrict__ nu,
+                                                 unsigned* __restrict__ err) {
+  __shared__ TcShared S;
+  const int tid = threadIdx.x;
+  const long long i = (long long)blockIdx.x * TC_ROWS + tid;
+  float x[6];
+#pragma unroll
+  for (int a = 0; a < 6; ++a) x[a] = i < m ? (feats[i * 6 + a] - F->mean[a]) * F->inv_std[a] : 0.0f;
+  const uint32_t tmem = tc_begin(S, F->tcb, tid);
+  const float y = tc_mlp(S, tmem, tid, x);
+  tc_end(S, tmem, tid);
+  if (i < m) nu[i] = closure_nu(*F, y);
+  if (tid == 0 && S.err) atomicOr(err, 1u);
 }
 
 // ---- training samples from a fine run ----
@@ -228,12 +245,12 @@ __global__ void k_filter(const float4* __restrict__ mac, const uint8_t* __restri
 
 // Pass 2: strain rate of the filtered velocity by central differences on the
 // coarse grid, residual stress tau_ab = <u_a u_b> - <u_a><u_b>, target
-// nu_t = max(0, -tau^d:S / (2 S:S)), and the features of the coarse
+// nu_t = max(0, -tau^d:S / (2 S:S)) (0 where |S| < s_min), and the features of the coarse
 // non-equilibrium stress Pi = -(2/3) rho (tau0c + 3 nu_t) S.  Rows for coarse
 // cells x0 <= X < x1 (all Y, Z), X fastest; target NaN where the cell or a
 // face neighbour is not fluid.
 __global__ void k_samples(const float* __restrict__ fil, int cx_, int cy_, int cz_, float tau0c, float omega0c,
-                          int x0, int x1, float* __restrict__ feats, float* __restrict__ target) {
+                          float s_min, int x0, int x1, float* __restrict__ feats, float* __restrict__ target) {
   const int wx = x1 - x0;
   const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const long long nr = (long long)wx * cy_ * cz_;
@@ -270,7 +287,9 @@ __global__ void k_samples(const float* __restrict__ fil, int cx_, int cy_, int c
   const float ss = sxx * sxx + syy * syy + szz * szz + 2.0f * (sxy * sxy + sxz * sxz + syz * syz);
   const float ts = (txx - tr3) * sxx + (tyy - tr3) * syy + (tzz - tr3) * szz +
                    2.0f * (txy * sxy + txz * sxz + tyz * syz);
-  const float nut = ss > 1e-20f ? fmaxf(0.0f, -ts / (2.0f * ss)) : 0.0f;
+  // |S| = sqrt(2 S:S) below s_min: no eddy viscosity (the ratio is
+  // ill-conditioned there and the dissipation nu_t |S|^2 negligible)
+  const float nut = (2.0f * ss > s_min * s_min && ss > 1e-30f) ? fmaxf(0.0f, -ts / (2.0f * ss)) : 0.0f;
   const float delta = c[3], rho = 1.0f + delta;
   const float k = -(2.0f / 3.0f) * rho * (tau0c + 3.0f * nut);
   float f[6];
@@ -350,6 +369,20 @@ void closure_pack(const closure_weights* w, MlpFrag* F) {
   }
   for (int j = 0; j < NH; ++j) { F->b1[j] = w->b1[j]; F->b2[j] = w->b2[j]; }
   F->b3 = w->b3;
+  // tcgen05 B operands, K-major core-matrix layout, bias in column K-slot kb
+  uint8_t* tb = reinterpret_cast<uint8_t*>(F->tcb);
+  auto put = [&](uint32_t base, int n, int k, int K, float v) {
+    const uint16_t h = f32_to_bf16(v);
+    memcpy(tb + base + tc_off(n, k, K), &h, 2);
+  };
+  for (int n = 0; n < NH; ++n) {
+    for (int k = 0; k < NI; ++k) put(0, n, k, TC_K1, w->w1[n * NI + k]);
+    put(0, n, NI, TC_K1, w->b1[n]);
+    for (int k = 0; k < NH; ++k) put(TC_B1_BYTES, n, k, TC_K2, w->w2[n * NH + k]);
+    put(TC_B1_BYTES, n, NH, TC_K2, w->b2[n]);
+  }
+  for (int k = 0; k < NH; ++k) put(TC_B1_BYTES + TC_B2_BYTES, 0, k, TC_K2, w->w3[k]);
+  put(TC_B1_BYTES + TC_B2_BYTES, 0, NH, TC_K2, w->b3);
   for (int a = 0; a < NI; ++a) {
     F->mean[a] = w->mean[a];
     F->inv_std[a] = w->std[a] != 0.0f ? 1.0f / w->std[a] : 0.0f;
@@ -361,7 +394,7 @@ void closure_pack(const closure_weights* w, MlpFrag* F) {
 // Rows of closure_samples (see include/lbm_closure.h); scratch is allocated
 // here.  Returns a CUDA error or cudaSuccess.
 cudaError_t closure_samples_launch(const float4* mac, const uint8_t* tipo, int nx, int ny, int nz, float tau0c,
-                                   int x0, int x1, float* feats_dev, float* target_dev, cudaStream_t s) {
+                                   float s_min, int x0, int x1, float* feats_dev, float* target_dev, cudaStream_t s) {
   const int cx_ = nx / 2, cy_ = ny / 2, cz_ = nz / 2;
   const long long nc = (long long)cx_ * cy_ * cz_;
   float* fil = nullptr;
@@ -369,8 +402,8 @@ cudaError_t closure_samples_launch(const float4* mac, const uint8_t* tipo, int n
   if (e != cudaSuccess) return e;
   k_filter<<<(unsigned)((nc + 255) / 256), 256, 0, s>>>(mac, tipo, nx, ny, nz, fil);
   const long long nr = (long long)(x1 - x0) * cy_ * cz_;
-  k_samples<<<(unsigned)((nr + 255) / 256), 256, 0, s>>>(fil, cx_, cy_, cz_, tau0c, 1.0f / tau0c, x0, x1, feats_dev,
-                                                       target_dev);
+  k_samples<<<(unsigned)((nr + 255) / 256), 256, 0, s>>>(fil, cx_, cy_, cz_, tau0c, 1.0f / tau0c, s_min, x0, x1,
+                                                       feats_dev, target_dev);
   e = cudaGetLastError();
   cudaError_t e2 = cudaStreamSynchronize(s);
   cudaFree(fil);
@@ -471,20 +504,28 @@ int closure_train(const float* feats, const float* target, size_t m, const closu
   return LBM_OK;
 }
 
-int closure_eval(const closure_weights* w, const float* feats, size_t m, float* nu_out) {
+int closure_eval(const closure_weights* w, const float* feats, size_t m, int engine, float* nu_out) {
   if (!w || !feats || !nu_out || m == 0) return cfail(LBM_EINVAL, "null argument or no samples");
+  if (engine != 0 && engine != 1) return cfail(LBM_EINVAL, "engine must be 0 or 1");
   MlpFrag F;
   closure_pack(w, &F);
   Mem mem;
   float *d_f, *d_nu;
   MlpFrag* d_F;
+  unsigned* d_err;
   CCK(mem.get(&d_f, sizeof(float) * m * NI), "features");
   CCK(mem.get(&d_nu, sizeof(float) * m), "output");
   CCK(mem.get(&d_F, sizeof(MlpFrag)), "fragments");
+  CCK(mem.get(&d_err, sizeof(unsigned)), "error flag");
   CCK(cudaMemcpy(d_f, feats, sizeof(float) * m * NI, cudaMemcpyHostToDevice), "upload");
   CCK(cudaMemcpy(d_F, &F, sizeof F, cudaMemcpyHostToDevice), "upload");
-  k_eval<<<(unsigned)((m + 127) / 128), 128>>>(d_f, (long long)m, d_F, d_nu);
+  CCK(cudaMemset(d_err, 0, sizeof(unsigned)), "clear");
+  if (engine == 1) k_eval_tc<<<(unsigned)((m + TC_ROWS - 1) / TC_ROWS), TC_ROWS>>>(d_f, (long long)m, d_F, d_nu, d_err);
+  else k_eval<<<(unsigned)((m + 127) / 128), 128>>>(d_f, (long long)m, d_F, d_nu);
   CCK(cudaGetLastError(), "eval kernel");
+  unsigned err = 0;
+  CCK(cudaMemcpy(&err, d_err, sizeof err, cudaMemcpyDeviceToHost), "download");
+  if (err) return cfail(LBM_ETIMEDOUT, "tensor-core MLP: an mbarrier wait gave up");
   CCK(cudaMemcpy(nu_out, d_nu, sizeof(float) * m, cudaMemcpyDeviceToHost), "download");
   return LBM_OK;
 }

@@ -15,10 +15,13 @@
 #include <cstdint>
 #include <cuda_bf16.h>
 
+#include "closure_tc.cuh"
+
 namespace lbm {
 
 // Weights in fragment order (built on the host by closure_pack).
 struct MlpFrag {
+  uint4 tcb[TC_B_BYTES / 16];   // B operands of the tcgen05 path (closure_tc.cuh)
   uint2 w1[4][32];      // layer 1: nt 0..3, k 0..15 (inputs 0..5, rest zero)
   uint2 w2[4][2][32];   // layer 2: nt 0..3, kt 0..1
   uint2 w3[2][32];      // layer 3: n 0 only (n 1..7 zero), kt 0..1

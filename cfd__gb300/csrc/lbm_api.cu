@@ -133,15 +133,18 @@ struct lbm_ctx {
   int64_t dev_bytes = 0;
   // learned closure
   lbm::MlpFrag* clo = nullptr;            // fragments of the network (device)
-  unsigned long long* clo_fb = nullptr;   // fallback counter (device)
-  int64_t clo_steps = 0;                  // closure steps since the last stats call
+  unsigned long long* clo_fb = nullptr;   // fallback counter (device), then the timeout flag
+  int64_t clo_steps = 0;                  // network evaluations since the last stats call
   int64_t n_fluido = 0;                   // FLUIDO cells of the current types
+  int clo_engine = 0;                     // 0 warp mma.sync, 1 CTA tcgen05
+  float* clo_nu = nullptr;                // held nu_t per cell (closure evaluated every k > 1 steps)
+  int clo_since = -1;                     // steps since the last evaluation; -1: evaluate next
 };
 
 namespace lbm {
 void closure_pack(const closure_weights* w, MlpFrag* F);
 cudaError_t closure_samples_launch(const float4* mac, const uint8_t* tipo, int nx, int ny, int nz, float tau0c,
-                                   int x0, int x1, float* feats_dev, float* target_dev, cudaStream_t s);
+                                   float s_min, int x0, int x1, float* feats_dev, float* target_dev, cudaStream_t s);
 }
 
 namespace {
@@ -230,15 +233,31 @@ int check_ready(lbm_ctx* c, bool need_cfg) {
 int launch_step(lbm_ctx* c, bool mac, double* force) {
   Dev d = dev_of(c);
   d.force = force;
-  if (c->P.closure == 1) {
-    if (!c->clo) return fail(LBM_ESTATE, "closure = 1 but no network set (call lbm_set_closure first)");
+  if (c->P.closure >= 1) {
+    if (!c->clo) return fail(LBM_ESTATE, "closure >= 1 but no network set (call lbm_set_closure first)");
     if (!c->inplace || (c->flags & LBM_FLAG_STRICT) || !c->ops.step_closure)
       return fail(LBM_ENOTSUP, "the learned closure runs in the in-place FAST step with fp32 arithmetic only");
-    cudaError_t e = c->ops.step_closure(d, c->P, parity(c), mac, force != nullptr, c->clo, c->clo_fb,
-                                        cell_launch(c), c->stream);
+    const int every = c->P.closure;
+    int mode = 0;
+    if (every > 1) {
+      if (!c->clo_nu) {
+        int r = dalloc(c, (void**)&c->clo_nu, sizeof(float) * (size_t)c->N, "held eddy viscosity");
+        if (r) return r;
+        c->clo_since = -1;
+      }
+      mode = (c->clo_since < 0 || c->clo_since >= every - 1) ? 1 : 2;
+    }
+    CloArgs A;
+    A.F = c->clo;
+    A.nfb = c->clo_fb;
+    A.err = reinterpret_cast<unsigned*>(c->clo_fb + 1);
+    A.nu = c->clo_nu;
+    A.omega0 = 1.0f / make_uni<float>(c->P).tau0;
+    cudaError_t e = c->ops.step_closure(d, c->P, parity(c), mac, force != nullptr, c->clo_engine, mode, A, c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "closure step kernel launch");
     c->steps++;
-    c->clo_steps++;
+    if (mode != 2) c->clo_steps++;
+    if (every > 1) c->clo_since = mode == 1 ? 0 : c->clo_since + 1;
     return LBM_OK;
   }
   cudaError_t e = c->ops.step(d, c->P, parity(c), c->inplace, mac, force != nullptr, !(c->flags & LBM_FLAG_STRICT),
@@ -296,7 +315,8 @@ int lbm_create(const lbm_dims* dims, int storage, int flags, lbm_ctx** out) {
 int lbm_destroy(lbm_ctx* c) {
   if (!c) return fail(LBM_EINVAL, "null context");
   if (c->stream) cudaStreamSynchronize(c->stream);
-  void* ps[] = {c->pop, c->pop2, c->tipo, c->link, c->macros, c->partials, c->red, c->fbuf, c->stage, c->clo, c->clo_fb};
+  void* ps[] = {c->pop, c->pop2, c->tipo, c->link, c->macros, c->partials, c->red, c->fbuf, c->stage, c->clo, c->clo_fb,
+                c->clo_nu};
   for (void* p : ps)
     if (p) cudaFree(p);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -315,7 +335,7 @@ int lbm_set_stream(lbm_ctx* c, void* s) {
 
 int lbm_configure(lbm_ctx* c, const lbm_params* p) {
   if (!c || !p) return fail(LBM_EINVAL, "null argument");
-  if (p->closure != 0 && p->closure != 1) return fail(LBM_EINVAL, "closure must be 0 or 1");
+  if (p->closure < 0 || p->closure > 4096) return fail(LBM_EINVAL, "closure must be 0 (Smagorinsky) or 1..4096");
   Params P;
   P.omega_plus = p->omega_plus; P.magic = p->magic; P.les_cs = p->les_cs;
   for (int a = 0; a < 3; ++a) { P.belt[a] = p->belt_u[a]; P.inlet[a] = p->inlet_u[a]; }
@@ -323,6 +343,7 @@ int lbm_configure(lbm_ctx* c, const lbm_params* p) {
   P.closure = p->closure;
   c->P = P;
   c->configured = true;
+  c->clo_since = -1;
   return LBM_OK;
 }
 
@@ -345,6 +366,7 @@ int lbm_set_types(lbm_ctx* c, const uint32_t* tipo, size_t n) {
   int64_t nf = 0;
   for (size_t i = 0; i < n; ++i) nf += t8[i] == LBM_FLUIDO;
   c->n_fluido = nf;
+  c->clo_since = -1;
   CK(cudaMemcpyAsync(c->tipo, t8.data(), n, cudaMemcpyHostToDevice, c->stream), "types upload");
   if (c->inplace) {
     Launch L = cell_launch(c);
@@ -360,6 +382,7 @@ int lbm_init_equilibrium(lbm_ctx* c) {
   int r = check_ready(c, true);
   if (r) return r;
   c->steps = 0;
+  c->clo_since = -1;
   CK(c->ops.init(dev_of(c), c->P, c->inplace, cell_launch(c), c->stream), "init kernel launch");
   c->state_set = true;
   return LBM_OK;
@@ -371,6 +394,7 @@ int lbm_set_populations(lbm_ctx* c, const double* g, size_t n) {
   int r = ensure_stage(c);
   if (r) return r;
   c->steps = 0;
+  c->clo_since = -1;
   for (int k = 0; k < Q; ++k) {
     CK(cudaMemcpyAsync(c->stage, g + (size_t)k * c->N, sizeof(double) * c->N, cudaMemcpyHostToDevice, c->stream),
        "population upload");
@@ -498,16 +522,25 @@ int lbm_set_closure(lbm_ctx* c, const closure_weights* w) {
   if (!c->clo) {
     int r = dalloc(c, (void**)&c->clo, sizeof(lbm::MlpFrag), "closure network");
     if (r) return r;
-    r = dalloc(c, (void**)&c->clo_fb, sizeof(unsigned long long), "closure counter");
+    r = dalloc(c, (void**)&c->clo_fb, 2 * sizeof(unsigned long long), "closure counter");
     if (r) return r;
-    CK(cudaMemsetAsync(c->clo_fb, 0, sizeof(unsigned long long), c->stream), "closure counter clear");
+    CK(cudaMemsetAsync(c->clo_fb, 0, 2 * sizeof(unsigned long long), c->stream), "closure counter clear");
   }
   CK(cudaMemcpyAsync(c->clo, &F, sizeof F, cudaMemcpyHostToDevice, c->stream), "closure upload");
   CK(cudaStreamSynchronize(c->stream), "closure upload sync");
+  c->clo_since = -1;
   return LBM_OK;
 }
 
-int closure_samples(lbm_ctx* c, float tau0_coarse, int x0, int x1, float* feats, float* target, size_t rows) {
+int lbm_closure_engine(lbm_ctx* c, int engine) {
+  if (!c) return fail(LBM_EINVAL, "null context");
+  if (engine != 0 && engine != 1) return fail(LBM_EINVAL, "engine must be 0 (warp mma.sync) or 1 (CTA tcgen05)");
+  c->clo_engine = engine;
+  return LBM_OK;
+}
+
+int closure_samples(lbm_ctx* c, float tau0_coarse, float s_min, int x0, int x1, float* feats, float* target,
+                    size_t rows) {
   if (!c || !feats || !target) return fail(LBM_EINVAL, "null argument");
   int r = check_ready(c, false);
   if (r) return r;
@@ -517,6 +550,7 @@ int closure_samples(lbm_ctx* c, float tau0_coarse, int x0, int x1, float* feats,
   const size_t nr = (size_t)(x1 - x0) * cy_ * cz_;
   if (rows != nr) return fail(LBM_EINVAL, "rows must be (x1 - x0) * (ny/2) * (nz/2)");
   if (!(tau0_coarse > 0.5f)) return fail(LBM_EINVAL, "tau0_coarse must exceed 1/2");
+  if (!(s_min >= 0.0f)) return fail(LBM_EINVAL, "s_min must be >= 0");
   if ((r = lbm_update_macros(c))) return r;
   float *df = nullptr, *dt = nullptr;
   if ((r = dalloc(c, (void**)&df, sizeof(float) * 6 * nr, "sample features"))) return r;
@@ -525,7 +559,7 @@ int closure_samples(lbm_ctx* c, float tau0_coarse, int x0, int x1, float* feats,
     return r;
   }
   cudaError_t e = lbm::closure_samples_launch(c->macros, c->tipo, c->dims.nx, c->dims.ny, c->dims.nz, tau0_coarse,
-                                              x0, x1, df, dt, c->stream);
+                                              s_min, x0, x1, df, dt, c->stream);
   if (e == cudaSuccess) e = cudaMemcpy(feats, df, sizeof(float) * 6 * nr, cudaMemcpyDeviceToHost);
   if (e == cudaSuccess) e = cudaMemcpy(target, dt, sizeof(float) * nr, cudaMemcpyDeviceToHost);
   cudaFree(df);
@@ -537,15 +571,16 @@ int closure_samples(lbm_ctx* c, float tau0_coarse, int x0, int x1, float* feats,
 
 int lbm_closure_stats(lbm_ctx* c, int64_t* fallback_cells, int64_t* fluid_cells) {
   if (!c || !fallback_cells || !fluid_cells) return fail(LBM_EINVAL, "null argument");
-  unsigned long long fb = 0;
+  unsigned long long fb[2] = {0, 0};
   if (c->clo_fb) {
-    CK(cudaMemcpyAsync(&fb, c->clo_fb, sizeof fb, cudaMemcpyDeviceToHost, c->stream), "closure counter download");
+    CK(cudaMemcpyAsync(fb, c->clo_fb, sizeof fb, cudaMemcpyDeviceToHost, c->stream), "closure counter download");
     CK(cudaMemsetAsync(c->clo_fb, 0, sizeof fb, c->stream), "closure counter clear");
     CK(cudaStreamSynchronize(c->stream), "closure counter sync");
   }
-  *fallback_cells = (int64_t)fb;
+  *fallback_cells = (int64_t)fb[0];
   *fluid_cells = c->n_fluido * c->clo_steps;
   c->clo_steps = 0;
+  if (fb[1]) return fail(LBM_ETIMEDOUT, "closure step: a tensor-core mbarrier wait gave up (those cells fell back)");
   return LBM_OK;
 }
 

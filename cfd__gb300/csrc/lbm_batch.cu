@@ -368,6 +368,7 @@ int lbm_batch_set_stream(lbm_batch* b, void* s) {
 int lbm_batch_configure(lbm_batch* b, int k, const lbm_params* p) {
   if (!b || !p) return bfail(LBM_EINVAL, "null argument");
   if (k < 0 || k >= (int)b->host.size()) return bfail(LBM_EINVAL, "tunnel index out of range");
+  if (p->closure != 0) return bfail(LBM_ENOTSUP, "the batched form runs the Smagorinsky closure only");
   Params P;
   P.omega_plus = p->omega_plus; P.magic = p->magic; P.les_cs = p->les_cs;
   for (int a = 0; a < 3; ++a) { P.belt[a] = p->belt_u[a]; P.inlet[a] = p->inlet_u[a]; }

@@ -231,22 +231,51 @@ k_step_inplace(Dev d, Params P, Uni<typename St::real> U) {
   }
 }
 
+// Arguments of the closure step.
+struct CloArgs {
+  const MlpFrag* F;             // the network
+  unsigned long long* nfb;      // fallback counter (cells whose output was not usable)
+  unsigned* err;                // set when a tensor-core wait gave up (engine 1)
+  float* nu;                    // per-cell nu_t: written by mode 1, read by mode 2
+  float omega0;                 // feature x4 = 1 / tau0
+};
+
+// Shared memory of the two network engines: the warp engine parks a fluid
+// cell's pulled g and moments (a column per thread) while the network runs,
+// so that the registers of the pull and of the network are not live at the
+// same time; the CTA engine holds its MMA operands (closure_tc.cuh).
+template <int ENG>
+struct CloShared {
+  float stash[Q + 7][128];
+};
+template <>
+struct CloShared<1> {
+  TcShared tc;
+};
+
 // In-place step with the learned eddy-viscosity closure (fp32 arithmetic,
-// FAST form).  The same pull, bounce-back and fused force as step_cell; for
-// FLUIDO cells the six features of the pulled non-equilibrium stress feed
-// the warp's tensor-core MLP (every lane takes part, with zero features when
-// it has no fluid cell), which gives nu_t and tau = tau0 + 3 nu_t, omega-
-// keeping Lambda fixed.  A fluid cell whose network output is not usable
-// relaxes with the Smagorinsky rates (src/core/emit/ir.js:284-299) and is
-// counted in *nfb.  Every other class goes through collide() unchanged.
-template <class St, int PAR, bool MAC, bool FRC, bool W64>
-__global__ void __launch_bounds__(128, 6)
-k_step_closure(Dev d, Params P, Uni<float> U, const MlpFrag* __restrict__ F, unsigned long long* __restrict__ nfb,
-               float omega0) {
+// FAST form).  The same pull, bounce-back and fused force as step_cell.
+// MODE 0: for FLUIDO cells the six features of the pulled non-equilibrium
+//   stress feed the network, which gives nu_t and tau = tau0 + 3 nu_t,
+//   omega- keeping Lambda fixed; a cell whose output is not usable relaxes
+//   with the Smagorinsky rates (src/core/emit/ir.js:284-299) and is counted.
+// MODE 1: the same, and nu_t (NaN for a fallback cell) is stored per cell.
+// MODE 2: no network: the rates come from the stored nu_t (Smagorinsky where
+//   it is NaN) -- the steps between two network evaluations of a closure
+//   that is evaluated every k-th step.
+// ENG 0: warp engine (closure_mlp.cuh, mma.sync per 32 cells); ENG 1: CTA
+// engine (closure_tc.cuh, tcgen05.mma per 128 cells).  Every other class goes
+// through collide() unchanged, before the network.  64 x 2 threads per block.
+template <class St, int PAR, bool MAC, bool FRC, bool W64, int ENG, int MODE>
+__global__ void __launch_bounds__(128, MODE == 2 ? 8 : 6)
+k_step_closure(Dev d, Params P, Uni<float> U, CloArgs A) {
   using R = float;
   using S = typename St::store_t;
   using Off = typename OffT<W64>::type;
   static_assert(sizeof(typename St::real) == 4, "closure step is fp32 arithmetic");
+  constexpr bool NET = MODE != 2;
+  __shared__ CloShared<NET ? ENG : 0> SH;
+  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int z = blockIdx.z;
@@ -257,6 +286,8 @@ k_step_closure(Dev d, Params P, Uni<float> U, const MlpFrag* __restrict__ F, uns
   S* const Fc = static_cast<S*>(d.pop) + cell;
   const Deltas<Off> D(x, y, z, nx, ny, d.nz);
   constexpr bool E = (PAR == 0);
+  uint32_t tmem = 0;
+  if constexpr (NET && ENG == 1) tmem = tc_begin(SH.tc, A.F->tcb, tid);
   double fx = 0.0, fy = 0.0, fz = 0.0;
   auto emit = [&](int i, R v) {
     if (i == 0) {
@@ -267,14 +298,6 @@ k_step_closure(Dev d, Params P, Uni<float> U, const MlpFrag* __restrict__ F, uns
       St::st(Fc + (Off)(E ? i : i - 1) * N, v);
     }
   };
-  // A fluid cell's pulled g and moments wait for the network in shared
-  // memory (column per thread), so that the registers of the pull and of the
-  // network are not live at the same time; the pair sums and the
-  // non-equilibrium parts are recomputed after it (same operations, same
-  // values).
-  constexpr int kStash = Q + 7;
-  __shared__ float stash[kStash][128];
-  const int tid = threadIdx.y * blockDim.x + threadIdx.x;
   R g[Q];
   R delta = R(0.0), rho = R(1.0), ux = R(0.0), uy = R(0.0), uz = R(0.0), uu = R(0.0), rinv = R(1.0);
   float feat[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
@@ -324,30 +347,56 @@ k_step_closure(Dev d, Params P, Uni<float> U, const MlpFrag* __restrict__ F, uns
       if (MAC) d.macros[cell] = make_float4(ux, uy, uz, delta);
       if (ct == FLUIDO) {
         fluid = true;
-        R e0, ns[9], nd[9];
-        fluid_neq_fast<R>(sp, dp, delta, rho, ux, uy, uz, uu, e0, ns, nd);
-        const PiT<R> q = pi_fast<R>(ns);
-        closure_features(q.xx, q.yy, q.zz, q.xy, q.xz, q.yz, rinv, delta, feat);
-        feat[4] = omega0;
+        if constexpr (NET) {
+          // Pi_ab = sum_i c_ia c_ib g_i - (delta / 3) delta_ab - rho u_a u_b
+          // (minus the shifted equilibrium's second moment), for the features
+          const PiT<R> m = pi_fast<R>(sp);
+          const R d3 = delta * R(1.0 / 3.0);
+          const R rux = rho * ux, ruy = rho * uy, ruz = rho * uz;
+          closure_features(m.xx - d3 - rux * ux, m.yy - d3 - ruy * uy, m.zz - d3 - ruz * uz, m.xy - rux * uy,
+                           m.xz - rux * uz, m.yz - ruy * uz, rinv, delta, feat);
+          feat[4] = A.omega0;
 #pragma unroll
-        for (int a = 0; a < 6; ++a) feat[a] = (feat[a] - __ldg(&F->mean[a])) * __ldg(&F->inv_std[a]);
+          for (int a = 0; a < 6; ++a) feat[a] = (feat[a] - __ldg(&A.F->mean[a])) * __ldg(&A.F->inv_std[a]);
+          if constexpr (ENG == 0) {
 #pragma unroll
-        for (int i = 0; i < Q; ++i) stash[i][tid] = g[i];
-        stash[Q + 0][tid] = delta; stash[Q + 1][tid] = rho; stash[Q + 2][tid] = ux; stash[Q + 3][tid] = uy;
-        stash[Q + 4][tid] = uz; stash[Q + 5][tid] = uu; stash[Q + 6][tid] = rinv;
+            for (int i = 0; i < Q; ++i) SH.stash[i][tid] = g[i];
+            SH.stash[Q + 0][tid] = delta; SH.stash[Q + 1][tid] = rho; SH.stash[Q + 2][tid] = ux;
+            SH.stash[Q + 3][tid] = uy; SH.stash[Q + 4][tid] = uz; SH.stash[Q + 5][tid] = uu;
+            SH.stash[Q + 6][tid] = rinv;
+          }
+        }
       } else {
         collide<R, true>(P, U, ct, x, z, g, sp, dp, delta, rho, ux, uy, uz, uu, rinv, emit);
       }
     }
   }
-  __syncwarp();
-  const float yv = warp_mlp(*F, feat);
+  float nu = 0.0f;
+  if constexpr (NET) {
+    float yv;
+    if constexpr (ENG == 0) {
+      __syncwarp();
+      yv = warp_mlp(*A.F, feat);
+    } else {
+      yv = tc_mlp(SH.tc, tmem, tid, feat);
+      tc_end(SH.tc, tmem, tid);
+    }
+    if (fluid) {
+      if constexpr (ENG == 0) {
+#pragma unroll
+        for (int i = 0; i < Q; ++i) g[i] = SH.stash[i][tid];
+        delta = SH.stash[Q + 0][tid]; rho = SH.stash[Q + 1][tid]; ux = SH.stash[Q + 2][tid];
+        uy = SH.stash[Q + 3][tid]; uz = SH.stash[Q + 4][tid]; uu = SH.stash[Q + 5][tid];
+        rinv = SH.stash[Q + 6][tid];
+      }
+      nu = closure_nu(*A.F, yv);
+      if (MODE == 1) A.nu[cell] = nu;
+    }
+  } else {
+    if (fluid) nu = __ldg(A.nu + cell);
+  }
   bool fell_back = false;
   if (fluid) {
-#pragma unroll
-    for (int i = 0; i < Q; ++i) g[i] = stash[i][tid];
-    delta = stash[Q + 0][tid]; rho = stash[Q + 1][tid]; ux = stash[Q + 2][tid]; uy = stash[Q + 3][tid];
-    uz = stash[Q + 4][tid]; uu = stash[Q + 5][tid]; rinv = stash[Q + 6][tid];
     R sp[9], dp[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) {
@@ -356,7 +405,6 @@ k_step_closure(Dev d, Params P, Uni<float> U, const MlpFrag* __restrict__ F, uns
     }
     R e0, ns[9], nd[9];
     fluid_neq_fast<R>(sp, dp, delta, rho, ux, uy, uz, uu, e0, ns, nd);
-    const float nu = closure_nu(*F, yv);
     R omegaP, omegaM;
     if (nu == nu) {
       const float tauT = U.tau0 + 3.0f * nu, tm = tauT - 0.5f;
@@ -368,8 +416,12 @@ k_step_closure(Dev d, Params P, Uni<float> U, const MlpFrag* __restrict__ F, uns
     }
     trt_emit_fast<R>(U, x, g, e0, ns, nd, omegaP, omegaM, emit);
   }
-  const unsigned fb = __ballot_sync(0xffffffffu, fell_back);
-  if (fb && (threadIdx.x & 31) == 0 && nfb) atomicAdd(nfb, (unsigned long long)__popc(fb));
+  if constexpr (NET) {
+    const unsigned fb = __ballot_sync(0xffffffffu, fell_back);
+    if (fb && (threadIdx.x & 31) == 0 && A.nfb) atomicAdd(A.nfb, (unsigned long long)__popc(fb));
+    if constexpr (ENG == 1)
+      if (tid == 0 && SH.tc.err && A.err) atomicOr(A.err, 1u);
+  }
   if (FRC) {
     const bool any = __any_sync(0xffffffffu, fx != 0.0 || fy != 0.0 || fz != 0.0);
     if (any) warp_add3(fx, fy, fz, d.force);
@@ -739,9 +791,10 @@ struct Ops {
   cudaError_t (*macros)(const Dev&, int parity, bool inplace, Launch, cudaStream_t);
   cudaError_t (*forces)(const Dev&, int parity, bool inplace, double* partials, Launch, cudaStream_t);
   cudaError_t (*mass)(const Dev&, int parity, bool inplace, double* partials, Launch, cudaStream_t);
-  // in-place FAST step with the learned closure; null for the fp64 judge
-  cudaError_t (*step_closure)(const Dev&, const Params&, int parity, bool mac, bool frc, const MlpFrag*,
-                              unsigned long long* fallback, Launch, cudaStream_t);
+  // in-place FAST step with the learned closure (engine 0/1, mode 0/1/2 of
+  // k_step_closure); null for the fp64 judge
+  cudaError_t (*step_closure)(const Dev&, const Params&, int parity, bool mac, bool frc, int engine, int mode,
+                              const CloArgs&, cudaStream_t);
   int elem_bytes;
 };
 
@@ -825,24 +878,34 @@ struct OpsImpl {
     else k_mass<St, false><<<L.grid, L.block, 0, s>>>(d, parity, part);
     return cudaGetLastError();
   }
-  template <int PAR, bool MAC, bool FRC>
-  static void go_closure(const Dev& d, const Params& P, const Uni<float>& U, const MlpFrag* F,
-                         unsigned long long* nfb, Launch L, cudaStream_t s) {
+  template <int PAR, bool MAC, bool FRC, int ENG, int MODE>
+  static void go_closure(const Dev& d, const Params& P, const Uni<float>& U, const CloArgs& A, cudaStream_t s) {
     if constexpr (sizeof(R) == 4) {
-      if ((int64_t)Q * d.N >= (int64_t)INT32_MAX) k_step_closure<St, PAR, MAC, FRC, true><<<L.grid, L.block, 0, s>>>(d, P, U, F, nfb, 1.0f / U.tau0);
-      else k_step_closure<St, PAR, MAC, FRC, false><<<L.grid, L.block, 0, s>>>(d, P, U, F, nfb, 1.0f / U.tau0);
+      // 64 x 2 threads: four warps, one 128-row MMA tile per block for engine 1
+      const dim3 block(64, 2), grid((d.nx + 63) / 64, (d.ny + 1) / 2, d.nz);
+      if ((int64_t)Q * d.N >= (int64_t)INT32_MAX)
+        k_step_closure<St, PAR, MAC, FRC, true, ENG, MODE><<<grid, block, 0, s>>>(d, P, U, A);
+      else
+        k_step_closure<St, PAR, MAC, FRC, false, ENG, MODE><<<grid, block, 0, s>>>(d, P, U, A);
     }
   }
-  static cudaError_t step_closure(const Dev& d, const Params& P, int parity, bool mac, bool frc, const MlpFrag* F,
-                                  unsigned long long* nfb, Launch L, cudaStream_t s) {
+  template <int PAR, bool MAC, bool FRC>
+  static void go_closure_m(const Dev& d, const Params& P, const Uni<float>& U, int engine, int mode,
+                           const CloArgs& A, cudaStream_t s) {
+    if (mode == 2) go_closure<PAR, MAC, FRC, 0, 2>(d, P, U, A, s);
+    else if (engine == 0) { mode == 1 ? go_closure<PAR, MAC, FRC, 0, 1>(d, P, U, A, s) : go_closure<PAR, MAC, FRC, 0, 0>(d, P, U, A, s); }
+    else { mode == 1 ? go_closure<PAR, MAC, FRC, 1, 1>(d, P, U, A, s) : go_closure<PAR, MAC, FRC, 1, 0>(d, P, U, A, s); }
+  }
+  static cudaError_t step_closure(const Dev& d, const Params& P, int parity, bool mac, bool frc, int engine,
+                                  int mode, const CloArgs& A, cudaStream_t s) {
     if constexpr (sizeof(R) == 4) {
       const Uni<float> U = make_uni<float>(P);
       if (parity == 0) {
-        if (mac) { frc ? go_closure<0, true, true>(d, P, U, F, nfb, L, s) : go_closure<0, true, false>(d, P, U, F, nfb, L, s); }
-        else { frc ? go_closure<0, false, true>(d, P, U, F, nfb, L, s) : go_closure<0, false, false>(d, P, U, F, nfb, L, s); }
+        if (mac) { frc ? go_closure_m<0, true, true>(d, P, U, engine, mode, A, s) : go_closure_m<0, true, false>(d, P, U, engine, mode, A, s); }
+        else { frc ? go_closure_m<0, false, true>(d, P, U, engine, mode, A, s) : go_closure_m<0, false, false>(d, P, U, engine, mode, A, s); }
       } else {
-        if (mac) { frc ? go_closure<1, true, true>(d, P, U, F, nfb, L, s) : go_closure<1, true, false>(d, P, U, F, nfb, L, s); }
-        else { frc ? go_closure<1, false, true>(d, P, U, F, nfb, L, s) : go_closure<1, false, false>(d, P, U, F, nfb, L, s); }
+        if (mac) { frc ? go_closure_m<1, true, true>(d, P, U, engine, mode, A, s) : go_closure_m<1, true, false>(d, P, U, engine, mode, A, s); }
+        else { frc ? go_closure_m<1, false, true>(d, P, U, engine, mode, A, s) : go_closure_m<1, false, false>(d, P, U, engine, mode, A, s); }
       }
       return cudaGetLastError();
     }

@@ -1,6 +1,8 @@
 """Studies of the storage forms and the batched form on one GB300.
 
     python -m cfd__gb300.estudos precisao [--steps 10000] [--grid 512,256,192]
+    python -m cfd__gb300.estudos lote [--steps 256]
+    python -m cfd__gb300.estudos fecho [--steps 16000] [--pesos w.npz]
 
 precisao: the 512x256x192 precision workload (25.2 M cells): the seeded
 superellipsoid (semi-axes 80x32x22 cells, 20k triangles, 0.3-cell jitter)
@@ -162,9 +164,175 @@ def lote(n_tunnels=64, steps=256, storages=("f32", "f16s"), seed=2026):
     return out
 
 
+def tuneis_fecho(seed=2026):
+    """The coarse 320x160x128 mesh-body tunnel and its 2x fine twin
+    640x320x256: the same 20k-triangle superellipsoid (48x20x14 cells on the
+    coarse grid) with every vertex scaled by 2, the floor two fine rows thick
+    so the no-slip wall sits where the coarse one does.  Returns
+    ((grid, types, sponge, frontal area), ...) for coarse and fine."""
+    from .geometry import corpo_config2
+    from .tunel import areaFrontalCorpo, montarTipos
+    from .voxel import voxelizar
+    gc = {"nx": 320, "ny": 160, "nz": 128}
+    gf = {"nx": 640, "ny": 320, "nz": 256}
+    pos, idx = corpo_config2(gc, seed)
+    out = []
+    for g, k in ((gc, 1.0), (gf, 2.0)):
+        vox = voxelizar((pos * np.float32(k)).astype(np.float32), idx, g, sdf=False)
+        mt = montarTipos(g, corpo=vox["tipo"], esteira=False)
+        if k == 2.0:
+            t = mt["tipo"].reshape(g["nz"], g["ny"], g["nx"])
+            row = t[1, 1:g["ny"] - 1, 1:g["nx"] - 1]
+            row[row == 0] = 7
+        out.append((g, mt["tipo"], mt["esponja"], areaFrontalCorpo(vox["tipo"], g)))
+    return out[0], out[1]
+
+
+def fecho(re_treino=(2000, 5000, 20000), re_teste=10000, passos_finos=16000, snapshots=4, intervalo=1000,
+          por_snapshot=300000, passos_treino=3000, cs=0.12, u=0.06, comprimento=96.0, semente=2026,
+          s_min=2e-4, pesos_saida=None):
+    """Learned-closure workload.  Fine runs (2x resolution, FP32, Smagorinsky
+    Cs) at the training Reynolds numbers give, at their last `snapshots`
+    states `intervalo` fine steps apart, a-priori samples (closure_samples:
+    2x2x2 box filter, least-squares eddy viscosity of the resolved residual
+    stress, coarse-grid features); `por_snapshot` valid rows are drawn from
+    x in [0.25, 0.85) of the coarse length; the target is 0 where the
+    filtered strain rate is below s_min and is clipped at the 99.9th
+    percentile of its positive values for training.  The MLP is trained on
+    them (batch 65 536, Adam) and evaluated at the held-out Reynolds number:
+    a-priori (held-out samples) against Smagorinsky, and a-posteriori by
+    coarse runs with the closure and with Smagorinsky whose Cd (over the last
+    half of passos_finos / 2 coarse steps) is compared with the fine run's.
+    Also: the fallback rate and the closure step's time against the
+    Smagorinsky step."""
+    import torch
+
+    from .fecho import amostras, avaliar, normalizacao, pesos_vazios, salvar, treinar
+    from .forces import coeficientes
+    from .solver import SolverCUDA
+    from .units import LatticeUnits
+    (gc, tc, ec, ac), (gf, tf, ef, af) = tuneis_fecho(semente)
+    units = LatticeUnits(u)
+    stream = torch.cuda.Stream()
+    rng = np.random.default_rng(semente)
+    cx = gc["nx"]
+    x0, x1 = int(0.25 * cx), int(0.85 * cx)
+    out = {"coarse": gc, "fine": gf, "frontal_area": {"coarse": ac, "fine": af}, "u_in": u, "cs": cs,
+           "length_coarse": comprimento, "fine_runs": {}, "coarse_runs": {}}
+
+    def cd_de(f, area, g):
+        return coeficientes(f, units, area, g)["cd"]
+
+    def rodar(g, tipo, esp, area, re, passos, bloco, closure=None, colher=None, cs_run=cs):
+        L = comprimento * g["nx"] / cx
+        nu = u * L / re
+        s = SolverCUDA(g, escrever_macros=False)
+        s.definirStream(stream.cuda_stream)
+        s.definirTipos(tipo)
+        s.configurar(omegaPlus=1.0 / (3.0 * nu + 0.5), lesCs=cs_run, inletU=[u, 0.0, 0.0], esponja=esp,
+                     closure=1 if closure is not None else 0)
+        if closure is not None:
+            s.definirFecho(closure)
+            s.estatisticasFecho()
+        s.inicializar()
+        cds, ms, feito, amos = [], 0.0, 0, []
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        while feito < passos:
+            n = min(bloco, passos - feito)
+            e0.record(stream)
+            s.passo(n - 1)
+            f = s.passoComForcas(1)
+            e1.record(stream)
+            e1.synchronize()
+            ms += e0.elapsed_time(e1)
+            feito += n
+            c = cd_de(f[-1] if np.ndim(f) > 1 else f, area, g)
+            cds.append(c)
+            if not np.isfinite(c) or abs(c) > 100:
+                break
+            if colher is not None and feito > passos - snapshots * intervalo and (passos - feito) % intervalo == 0:
+                amos.append(colher(s))
+        rec = {"Re": re, "omega_plus": 1.0 / (3.0 * nu + 0.5), "steps": feito, "ms_per_step": ms / max(feito, 1),
+               "MLUPS": s.N * feito / (ms / 1e3) / 1e6, "diverged": bool(feito < passos)}
+        tail = cds[len(cds) // 2:]
+        rec["cd"] = float(np.mean(tail)) if tail and not rec["diverged"] else float("nan")
+        rec["cd_std"] = float(np.std(tail)) if tail and not rec["diverged"] else float("nan")
+        if closure is not None:
+            fb, fl = s.estatisticasFecho()
+            rec["fallback_cells"], rec["fluid_cell_updates"] = fb, fl
+            rec["fallback_rate"] = fb / max(fl, 1)
+        s.destruir()
+        return rec, amos
+
+    def colhedor(re):
+        tau0c = 3.0 * u * comprimento / re + 0.5
+
+        def colher(s):
+            f, t = amostras(s, tau0c, x0, x1, s_min=s_min)
+            ok = np.flatnonzero(np.isfinite(t))
+            pick = rng.choice(ok, size=min(por_snapshot, ok.size), replace=False)
+            pick.sort()
+            return f[pick], t[pick]
+        return colher
+
+    dados = {}
+    for re in tuple(re_treino) + (re_teste,):
+        rec, amos = rodar(gf, tf, ef, af, re, passos_finos, intervalo // 2, colher=colhedor(re))
+        out["fine_runs"][str(re)] = rec
+        if amos:
+            dados[re] = (np.concatenate([a[0] for a in amos]), np.concatenate([a[1] for a in amos]))
+            rec["samples"] = int(dados[re][1].size)
+            rec["target_mean"] = float(dados[re][1].mean())
+            rec["target_zero_fraction"] = float((dados[re][1] == 0).mean())
+    treino = [re for re in re_treino if re in dados]
+    F = np.concatenate([dados[re][0] for re in treino])
+    T = np.concatenate([dados[re][1] for re in treino])
+    pos = T[T > 0]
+    t_clip = float(np.quantile(pos, 0.999)) if pos.size else 1.0
+    T = np.minimum(T, np.float32(t_clip))
+    p = pesos_vazios()
+    p.update(normalizacao(F, T))
+    t0 = time.time()
+    p, hist = treinar(F, T, p, passos=int(passos_treino * 2 // 3), lote=65536, lr=2e-3, semente=semente)
+    p, hist2 = treinar(F, T, p, passos=int(passos_treino // 3), lote=65536, lr=5e-4, semente=semente + 1,
+                       iniciar=False)
+    out["training"] = {"samples": int(T.size), "Re": list(treino), "steps": int(passos_treino), "batch": 65536,
+                       "seconds": time.time() - t0, "loss_first": float(hist[:10].mean()),
+                       "loss_last": float(hist2[-50:].mean()), "nu_scale": p["nu_scale"], "nu_max": p["nu_max"],
+                       "target_clip": t_clip}
+    if pesos_saida:
+        salvar(p, pesos_saida)
+    # a-priori on the held-out Reynolds number
+    if re_teste in dados:
+        Fv, Tv = dados[re_teste]
+        Tv = np.minimum(Tv, np.float32(t_clip))
+        nu_net = avaliar(p, Fv)
+        tau0c = 3.0 * u * comprimento / re_teste + 0.5
+        s_mag = 1.5 * np.exp(Fv[:, 0].astype(np.float64)) / (tau0c + 3.0 * Tv)   # |S| from x0
+        nu_smag = cs * cs * s_mag
+        ok = np.isfinite(nu_net)
+
+        def metr(a, b):
+            return {"rel_l2": float(np.linalg.norm(a - b) / np.linalg.norm(b)),
+                    "corr": float(np.corrcoef(a, b)[0, 1]), "mean_ratio": float(a.mean() / b.mean())}
+        out["a_priori"] = {"Re": re_teste, "rows": int(Tv.size), "closure": metr(nu_net[ok], Tv[ok]),
+                           "smagorinsky": metr(nu_smag, Tv), "fallback_rows": int((~ok).sum())}
+    passos_grossos = passos_finos // 2
+    for nome, clo, c_s in (("smagorinsky", None, cs), ("closure", p, cs), ("no_model", None, 0.0)):
+        rec, _ = rodar(gc, tc, ec, ac, re_teste, passos_grossos, intervalo // 4, closure=clo, cs_run=c_s)
+        out["coarse_runs"][nome] = rec
+    fine_cd = out["fine_runs"][str(re_teste)]["cd"]
+    for nome, rec in out["coarse_runs"].items():
+        rec["cd_err_vs_fine"] = (rec["cd"] - fine_cd) / fine_cd
+    sm, cl = out["coarse_runs"]["smagorinsky"], out["coarse_runs"]["closure"]
+    out["closure_overhead"] = cl["ms_per_step"] / sm["ms_per_step"] - 1.0
+    return out
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("study", choices=["precisao", "lote"])
+    ap.add_argument("study", choices=["precisao", "lote", "fecho"])
+    ap.add_argument("--pesos", default=None, help="fecho: write the trained weights (.npz) here")
     ap.add_argument("--steps", type=int, default=10000)
     ap.add_argument("--grid", default="512,256,192")
     a = ap.parse_args(argv)
@@ -172,6 +340,8 @@ def main(argv=None):
     t0 = time.time()
     if a.study == "lote":
         r = lote(steps=a.steps)
+    elif a.study == "fecho":
+        r = fecho(passos_finos=a.steps, pesos_saida=a.pesos)
     else:
         r = precisao(a.steps, {"nx": nx, "ny": ny, "nz": nz})
     r["wall_s"] = time.time() - t0

@@ -112,19 +112,21 @@ def treinar(feats, target, p, passos, lote=65536, lr=1e-3, beta1=0.9, beta2=0.99
     return de_struct(w, p), hist[:int(passos)]
 
 
-def avaliar(p, feats):
-    """nu_t per row through the step's tensor-core MLP; NaN = Smagorinsky fallback."""
+def avaliar(p, feats, motor=0):
+    """nu_t per row through a tensor-core engine of the step (0 warp mma.sync,
+    1 CTA tcgen05); NaN = Smagorinsky fallback."""
     L = nat.load()
     f, _ = _rows(feats)
     out = np.empty(f.shape[0], np.float32)
     w = para_struct(p)
-    nat.check(L.closure_eval(C.byref(w), nat.ptr(f), f.shape[0], nat.ptr(out)))
+    nat.check(L.closure_eval(C.byref(w), nat.ptr(f), f.shape[0], int(motor), nat.ptr(out)))
     return out
 
 
-def amostras(solver, tau0_grosso, x0=None, x1=None):
+def amostras(solver, tau0_grosso, x0=None, x1=None, s_min=0.0):
     """Rows of closure_samples for a fine SolverCUDA: (feats[m, 6], target[m]),
-    one row per coarse cell with x0 <= X < x1, target NaN where not usable."""
+    one row per coarse cell with x0 <= X < x1, target NaN where not usable,
+    0 where the filtered strain rate |S| is below s_min."""
     L = nat.load()
     cx, cy, cz = solver.nx // 2, solver.ny // 2, solver.nz // 2
     x0 = 0 if x0 is None else int(x0)
@@ -132,18 +134,32 @@ def amostras(solver, tau0_grosso, x0=None, x1=None):
     m = (x1 - x0) * cy * cz
     f = np.empty((m, NI), np.float32)
     t = np.empty(m, np.float32)
-    nat.check(L.closure_samples(solver._h, float(tau0_grosso), x0, x1, nat.ptr(f), nat.ptr(t), m))
+    nat.check(L.closure_samples(solver._h, float(tau0_grosso), float(s_min), x0, x1, nat.ptr(f), nat.ptr(t), m))
     return f, t
 
 
-def normalizacao(feats, target, q_escala=0.9, fator_max=50.0):
+def normalizacao(feats, target, q_escala=0.9, q_max=0.999, fator_max=20.0):
     """mean / std of the features; nu_scale = the q_escala quantile of the
-    positive targets; nu_max = fator_max times the largest target."""
+    positive targets; nu_max = fator_max times their q_max quantile."""
     f, t = _rows(feats, target)
     mean = f.mean(axis=0).astype(np.float32)
     std = f.std(axis=0).astype(np.float32)
     std[std < 1e-6] = 1.0
     pos = t[t > 0]
     escala = float(np.quantile(pos, q_escala)) if pos.size else 1e-4
-    return {"mean": mean, "std": std, "nu_scale": max(escala, 1e-8),
-            "nu_max": float(fator_max * max(float(t.max(initial=0.0)), escala))}
+    alto = float(np.quantile(pos, q_max)) if pos.size else escala
+    return {"mean": mean, "std": std, "nu_scale": max(escala, 1e-8), "nu_max": float(fator_max * max(alto, escala))}
+
+
+def salvar(p, caminho):
+    """Weights to an .npz file."""
+    np.savez(caminho, **{k: np.asarray(v) for k, v in p.items()})
+
+
+def carregar(caminho):
+    d = np.load(caminho)
+    p = pesos_vazios()
+    for k in d.files:
+        v = d[k]
+        p[k] = float(v) if k in ("nu_scale", "nu_max") else (np.float32(v) if v.shape == () else v.astype(np.float32))
+    return p

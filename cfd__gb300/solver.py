@@ -239,6 +239,11 @@ class SolverCUDA:
         nat.check(self._lib.lbm_set_closure(self._h, C.byref(w)))
         self.fontes["passo"] = "cfd__gb300/csrc/lbm_kernels.cuh:k_step_closure"
 
+    def motorFecho(self, motor: int):
+        """Tensor-core engine of the closure step: 0 warp mma.sync (default),
+        1 CTA tcgen05."""
+        nat.check(self._lib.lbm_closure_engine(self._h, int(motor)))
+
     def estatisticasFecho(self):
         """(fallback cells, fluid cells) over the closure steps since the last call."""
         a, b = C.c_int64(), C.c_int64()

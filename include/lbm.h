@@ -88,7 +88,8 @@ typedef struct { int32_t nx, ny, nz; } lbm_dims;
 /* Fields of the 80-byte Params uniform (src/core/emit/wgsl.js:123-135) as the
  * reference packs them (src/backend/webgpu/solver.js:285-291).  All fp32, as
  * the uniform is.  `closure` selects the eddy-viscosity model: 0 = Smagorinsky
- * (src/core/emit/ir.js:262-301), 1 = the learned MLP set by lbm_set_closure. */
+ * (src/core/emit/ir.js:262-301), 1 = the learned MLP set by lbm_set_closure
+ * evaluated every step, k > 1 = evaluated every k-th step (lbm_closure.h). */
 typedef struct {
   float omega_plus;      /* P.omegaPlus */
   float magic;           /* P.magic (TRT Lambda), default 3/16 */
@@ -98,7 +99,7 @@ typedef struct {
   float sponge_start;    /* P.sponge.x */
   float sponge_len;      /* P.sponge.y */
   float bl_thickness;    /* P.sponge.z (espessuraCL) */
-  int32_t closure;       /* 0 Smagorinsky, 1 learned closure */
+  int32_t closure;       /* 0 Smagorinsky, k >= 1 learned closure every k-th step */
 } lbm_params;
 
 typedef struct {

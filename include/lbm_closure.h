@@ -68,29 +68,42 @@ int closure_train(const float* feats, const float* target, size_t m, const closu
 int closure_grad(const float* feats, const float* target, size_t m, const closure_weights* w, float* loss,
                  float* grad);
 
-/* nu_t of m feature rows through the tensor-core path the step uses
- * (bf16 features and weights, fp32 accumulation); fallback cells get NaN. */
-int closure_eval(const closure_weights* w, const float* feats, size_t m, float* nu_out);
+/* nu_t of m feature rows through a tensor-core engine of the step (bf16
+ * features and weights, fp32 accumulation); fallback rows get NaN.
+ *   engine 0: warp-level mma.sync.m16n8k16, 32 cells per warp, biases added
+ *             in fp32 (the accumulators start at the bias);
+ *   engine 1: CTA-level tcgen05.mma, 128 cells per CTA, accumulators in
+ *             tensor memory, biases in bf16 as an extra K column. */
+int closure_eval(const closure_weights* w, const float* feats, size_t m, int engine, float* nu_out);
 
-/* Training samples from a fine run held by ctx (grid nx x ny x nz, all even
- * or not: the coarse grid is (nx/2, ny/2, nz/2)).  The fine macros are
- * box-filtered over 2x2x2 blocks; S is the strain rate of the filtered
- * velocity by central differences on the coarse grid; tau_ab = <u_a u_b> -
- * <u_a><u_b> the resolved residual stress; the target is the least-squares
- * eddy viscosity nu_t = max(0, -tau^d:S / (2 S:S)) in coarse lattice units,
- * and the features are those of the coarse non-equilibrium stress
+/* Training samples from a fine run held by ctx (grid nx x ny x nz; the
+ * coarse grid is (nx/2, ny/2, nz/2), an odd last fine layer is dropped).
+ * The fine macros are box-filtered over 2x2x2 blocks; S is the strain rate
+ * of the filtered velocity by central differences on the coarse grid;
+ * tau_ab = <u_a u_b> - <u_a><u_b> the resolved residual stress; the target
+ * is the least-squares eddy viscosity nu_t = max(0, -tau^d:S / (2 S:S)) in
+ * coarse lattice units, 0 where |S| = sqrt(2 S:S) < s_min (the ratio is
+ * ill-conditioned there), and the features are those of the coarse
+ * non-equilibrium stress
  * Pi = -(2/3) rho (tau0_coarse + 3 nu_t) S.  One row per coarse cell with
  * x0 <= X < x1 (X fastest, then Y, then Z): rows = (x1-x0)(ny/2)(nz/2),
  * feats 6 floats per row, target NaN where the coarse cell or one of its six
  * face neighbours has a fine cell that is not FLUIDO. */
-int closure_samples(lbm_ctx* ctx, float tau0_coarse, int x0, int x1, float* feats, float* target, size_t rows);
+int closure_samples(lbm_ctx* ctx, float tau0_coarse, float s_min, int x0, int x1, float* feats, float* target,
+                    size_t rows);
 
-/* Network for a solver context; lbm_params.closure = 1 then selects it.
- * LBM_ENOTSUP for the fp64 judge and for STRICT arithmetic. */
+/* Network for a solver context.  lbm_params.closure = 1 then evaluates it in
+ * every step; closure = k > 1 evaluates it every k-th step and relaxes the
+ * steps in between with the nu_t it gave (held per cell, 4 bytes a cell).
+ * LBM_ENOTSUP for the fp64 judge, STRICT arithmetic and ping-pong. */
 int lbm_set_closure(lbm_ctx* ctx, const closure_weights* w);
 
-/* Cells that fell back to Smagorinsky and FLUIDO cells seen since the last
- * call (closure steps only); resets both counters. */
+/* Engine of the fused step's network (see closure_eval); default 0. */
+int lbm_closure_engine(lbm_ctx* ctx, int engine);
+
+/* Network evaluations that fell back to Smagorinsky and FLUIDO cells the
+ * network was evaluated for, since the last call; resets both counters.
+ * LBM_ETIMEDOUT (counts still returned) if a tensor-core wait gave up. */
 int lbm_closure_stats(lbm_ctx* ctx, int64_t* fallback_cells, int64_t* fluid_cells);
 
 #ifdef __cplusplus

@@ -16,10 +16,13 @@ this file is the definition the kernels are checked against:
                       kernels' gradient is checked against this);
   * eval_bf16()       the inference path of the fused step: normalised
                       features and weights rounded to bf16 (round to nearest
-                      even), products summed exactly (fp64 here, fp32 in the
-                      tensor cores), hidden activations ReLU'd and rounded to
-                      bf16, output nu = nu_scale * softplus(y), NaN when not
-                      finite or above nu_max;
+                      even; the CTA engine also rounds the biases, which ride
+                      in the K dimension as products with a constant 1),
+                      products summed exactly
+                      (fp64 here, fp32 in the tensor cores), hidden
+                      activations ReLU'd and rounded to bf16, output
+                      nu = nu_scale * softplus(y), NaN when not finite or
+                      above nu_max;
   * samples()         the 2x2x2 box filter of a fine run's macros, the
                       filtered strain rate by central differences, the
                       residual stress, the target nu_t and the features of
@@ -118,25 +121,31 @@ def bf16(a):
     return r.view(np.float32)
 
 
-def eval_bf16(v, feats, mean, std, nu_scale, nu_max):
-    """nu per row as the tensor-core path computes it (see module text)."""
+def eval_bf16(v, feats, mean, std, nu_scale, nu_max, bias_bf16=False):
+    """nu per row as a tensor-core engine computes it (see module text);
+    bias_bf16: the biases rounded to bf16 (the CTA engine carries them in the
+    K dimension), else fp32 (the warp engine starts its accumulators at them)."""
     P = unpack(np.asarray(v, np.float32).astype(np.float64))
     x = bf16(normalise(feats, mean, std)).astype(np.float64)
     w1 = bf16(P["w1"].astype(np.float32)).astype(np.float64)
     w2 = bf16(P["w2"].astype(np.float32)).astype(np.float64)
     w3 = bf16(P["w3"].astype(np.float32)).astype(np.float64)
-    a1 = (x @ w1.T + np.float32(P["b1"]).astype(np.float64)).astype(np.float32)
+    rb = bf16 if bias_bf16 else (lambda a: np.asarray(a, np.float32))
+    b1 = rb(np.float32(P["b1"])).astype(np.float64)
+    b2 = rb(np.float32(P["b2"])).astype(np.float64)
+    b3 = float(rb(np.array([P["b3"]], np.float32))[0])
+    a1 = (x @ w1.T + b1).astype(np.float32)
     h1 = bf16(np.maximum(a1, 0)).astype(np.float64)
-    a2 = (h1 @ w2.T + np.float32(P["b2"]).astype(np.float64)).astype(np.float32)
+    a2 = (h1 @ w2.T + b2).astype(np.float32)
     h2 = bf16(np.maximum(a2, 0)).astype(np.float64)
-    y = (h2 @ w3 + float(np.float32(P["b3"]))).astype(np.float32).astype(np.float64)
+    y = (h2 @ w3 + b3).astype(np.float32).astype(np.float64)
     with np.errstate(over="ignore", invalid="ignore"):
         nu = float(np.float32(nu_scale)) * softplus(y)
     ok = np.isfinite(nu) & (nu >= 0) & (nu <= float(np.float32(nu_max)))
     return np.where(ok, nu, np.nan), y
 
 
-def samples(mac, tipo, tau0c, x0, x1):
+def samples(mac, tipo, tau0c, x0, x1, s_min=0.0):
     """mac: fine macros (nz, ny, nx, 4) = (ux, uy, uz, delta); tipo (nz, ny, nx).
     Returns (feats (rows, 6), target (rows,)) in the row order of
     closure_samples (X fastest over [x0, x1), then Y, then Z)."""
@@ -169,7 +178,7 @@ def samples(mac, tipo, tau0c, x0, x1):
     ss = sxx * sxx + syy * syy + szz * szz + 2.0 * (sxy * sxy + sxz * sxz + syz * syz)
     ts = (txx - tr3) * sxx + (tyy - tr3) * syy + (tzz - tr3) * szz + 2.0 * (txy * sxy + txz * sxz + tyz * syz)
     with np.errstate(divide="ignore", invalid="ignore"):
-        nut = np.where(ss > 1e-20, np.maximum(0.0, -ts / (2.0 * ss)), 0.0)
+        nut = np.where((2.0 * ss > s_min * s_min) & (ss > 1e-30), np.maximum(0.0, -ts / (2.0 * ss)), 0.0)
     delta = u[..., 3]
     rho = 1.0 + delta
     k = -(2.0 / 3.0) * rho * (tau0c + 3.0 * nut)

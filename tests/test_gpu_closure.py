@@ -54,12 +54,13 @@ def test_training_gradient_matches_fp64(native):
     np.testing.assert_allclose(g, g64, rtol=1e-3, atol=1e-5 * np.abs(g64).max())
 
 
-def test_inference_matches_bf16_emulation(native):
+@pytest.mark.parametrize("motor", [0, 1])
+def test_inference_matches_bf16_emulation(native, motor):
     from cfd__gb300 import fecho
     p = _pesos(4)
     f = _feats(20011, 5)          # not a multiple of the warp or block size
-    nu = fecho.avaliar(p, f)
-    ref, _ = CO.eval_bf16(fecho.vetor(p), f, p["mean"], p["std"], p["nu_scale"], p["nu_max"])
+    nu = fecho.avaliar(p, f, motor)
+    ref, _ = CO.eval_bf16(fecho.vetor(p), f, p["mean"], p["std"], p["nu_scale"], p["nu_max"], bias_bf16=motor == 1)
     assert np.isfinite(nu).all() and np.isfinite(ref).all()
     d = np.abs(nu - ref)
     tol = 1e-2 * np.abs(ref) + 1e-3 * p["nu_scale"]
@@ -69,18 +70,19 @@ def test_inference_matches_bf16_emulation(native):
     assert (d <= 0.1 * np.abs(ref) + 1e-2 * p["nu_scale"]).all()
 
 
-def test_inference_fallback_marks(native):
+@pytest.mark.parametrize("motor", [0, 1])
+def test_inference_fallback_marks(native, motor):
     from cfd__gb300 import fecho
     p = _pesos(6)
     p["nu_max"] = 1e-3            # most outputs above -> NaN
     f = _feats(4096, 7)
-    nu = fecho.avaliar(p, f)
-    ref, _ = CO.eval_bf16(fecho.vetor(p), f, p["mean"], p["std"], p["nu_scale"], p["nu_max"])
+    nu = fecho.avaliar(p, f, motor)
+    ref, _ = CO.eval_bf16(fecho.vetor(p), f, p["mean"], p["std"], p["nu_scale"], p["nu_max"], bias_bf16=motor == 1)
     agree = np.isnan(nu) == np.isnan(ref)
     assert agree.mean() > 0.99 and np.isnan(nu).any() and (~np.isnan(nu)).any()
     q = fecho.pesos_vazios()
     q["b3"] = np.float32(np.nan)
-    assert np.isnan(fecho.avaliar(q, f)).all()
+    assert np.isnan(fecho.avaliar(q, f, motor)).all()
 
 
 def test_training_deterministic_and_fits(native):
@@ -108,10 +110,10 @@ def test_samples_match_oracle(native):
     s.inicializar()
     s.passo(300)
     tau0c = 0.52
-    f, t = fecho.amostras(s, tau0c, 4, 30)
+    f, t = fecho.amostras(s, tau0c, 4, 30, s_min=1e-4)
     s.atualizarMacros()
     mac = s.lerMacros().reshape(32, 32, 64, 4)
-    fo, to = CO.samples(mac, np.asarray(tipo).reshape(32, 32, 64), tau0c, 4, 30)
+    fo, to = CO.samples(mac, np.asarray(tipo).reshape(32, 32, 64), tau0c, 4, 30, s_min=1e-4)
     s.destruir()
     assert np.array_equal(np.isnan(t), np.isnan(to))
     ok = ~np.isnan(t)
@@ -128,7 +130,7 @@ def test_samples_match_oracle(native):
     np.testing.assert_allclose(f[big], fo[big], rtol=1e-2, atol=1e-3)
 
 
-def _run_pair(p_closure, cfg_a, cfg_b, steps=(1, 7, 16), storage="f32"):
+def _run_pair(p_closure, cfg_a, cfg_b, steps=(1, 7, 16), storage="f32", motor=0):
     from cfd__gb300 import SolverCUDA
     grade, tipo, esp = all_types_tunnel()
     N = int(np.prod(list(grade.values())))
@@ -142,6 +144,7 @@ def _run_pair(p_closure, cfg_a, cfg_b, steps=(1, 7, 16), storage="f32"):
         s.configurar(**c)
         if pw is not None:
             s.definirFecho(pw)
+            s.motorFecho(motor)
         s.definirPopulacoes(g0)
         forces = []
         for n in steps:
@@ -154,30 +157,36 @@ def _run_pair(p_closure, cfg_a, cfg_b, steps=(1, 7, 16), storage="f32"):
     return out, fluid, tipo
 
 
-@pytest.mark.parametrize("storage", ["f32", "f16s", "bf16s"])
-def test_unusable_output_falls_back_bit_exact(native, storage):
+@pytest.mark.parametrize("storage,motor,every", [("f32", 0, 1), ("f16s", 0, 1), ("bf16s", 0, 1), ("f32", 1, 1),
+                                                 ("f32", 0, 4), ("f16s", 1, 3)])
+def test_unusable_output_falls_back_bit_exact(native, storage, motor, every):
     from cfd__gb300 import fecho
     p = fecho.pesos_vazios()
     p["b3"] = np.float32(np.nan)
     base = dict(omegaPlus=1.9, lesCs=0.12, inletU=[0.05, 0, 0.01], beltU=[0.05, 0, 0])
-    (a, b), fl, tipo = _run_pair(p, base, dict(base, closure=1), storage=storage)
+    (a, b), fl, tipo = _run_pair(p, base, dict(base, closure=every), storage=storage, motor=motor)
     assert np.array_equal(a[0][:, fl], b[0][:, fl])
     assert np.array_equal(a[1], b[1])
     nfluid = int((np.asarray(tipo).reshape(-1) == 0).sum())
-    assert b[2] == (nfluid * 27, nfluid * 27)
+    # steps 1, 1 (forces), 7, 1, 16, 1 = 27 steps; with every = k the
+    # network runs on steps 0, k, 2k, ... of the run
+    evals = 27 if every == 1 else len(range(0, 27, every))
+    assert b[2] == (nfluid * evals, nfluid * evals)
 
 
-def test_constant_nu_matches_plain_step(native):
+@pytest.mark.parametrize("motor,every", [(0, 1), (1, 1), (0, 5)])
+def test_constant_nu_matches_plain_step(native, motor, every):
     from cfd__gb300 import fecho
     nu0, tau0 = 0.02, 1.0 / 1.9
     p = fecho.pesos_vazios()
     p["nu_scale"] = 1.0
     p["nu_max"] = 1.0
-    p["b3"] = np.float32(np.log(np.expm1(nu0)))   # softplus(b3) = nu0
+    # softplus(b3) ~ nu0, b3 exact in bf16 (the CTA engine carries the bias in bf16)
+    p["b3"] = CO.bf16(np.array([np.log(np.expm1(nu0))], np.float32))[0]
     nu_eff = float(np.float32(1.0) * np.log1p(np.exp(np.float64(p["b3"]))))
     plain = dict(omegaPlus=1.0 / (tau0 + 3 * nu_eff), lesCs=0.0, inletU=[0.05, 0, 0.01], beltU=[0.05, 0, 0])
-    clo = dict(omegaPlus=1.9, lesCs=0.12, inletU=[0.05, 0, 0.01], beltU=[0.05, 0, 0], closure=1)
-    (a, b), fl, tipo = _run_pair(p, plain, clo)
+    clo = dict(omegaPlus=1.9, lesCs=0.12, inletU=[0.05, 0, 0.01], beltU=[0.05, 0, 0], closure=every)
+    (a, b), fl, tipo = _run_pair(p, plain, clo, motor=motor)
     ga, gb = a[0][:, fl], b[0][:, fl]
     assert np.abs(ga - gb).max() <= 2e-6 * np.abs(ga).max()
     np.testing.assert_allclose(a[1], b[1], rtol=1e-4, atol=1e-9)
@@ -194,6 +203,10 @@ def test_closure_errors(native):
         with pytest.raises(LbmError, match="ENOTSUP"):
             s.definirFecho(p)
         s.destruir()
+    s = SolverCUDA(grade)
+    with pytest.raises(LbmError, match="EINVAL"):
+        s.motorFecho(2)
+    s.destruir()
     s = SolverCUDA(grade)
     s.definirTipos(tipo)
     s.configurar(omegaPlus=1.9, esponja=esp, closure=1)
