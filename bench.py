@@ -247,6 +247,36 @@ def time_steps(s, stream, K):
     return e0.elapsed_time(e1)
 
 
+def reduce_max(value, world, device="cpu"):
+    """Max of a per-rank value over the ranks (the slowest rank's time)."""
+    if world <= 1:
+        return float(value)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def closure_forms(make, stream, steps, warmup, ms_plain, N):
+    """Step time of the learned closure (coefficient form, weights trained by
+    `python -m cfd__gb300.estudos fecho`) evaluated every step and every 8th
+    step, against the Smagorinsky step of the same tunnel."""
+    from cfd__gb300.fecho import carregar
+    p = carregar(os.path.join(ROOT, "cfd__gb300", "pesos", "fecho_coef.npz"))
+    out = {}
+    for every in (1, 8):
+        s = make("f32", closure=every, pesos=p)
+        s.passo(warmup)
+        ms = time_steps(s, stream, steps)
+        fb, fl = s.estatisticasFecho()
+        out[f"closure_every_{every}"] = {"MLUPS": N * steps / (ms / 1e3) / 1e6,
+                                         "overhead_vs_smagorinsky": (ms / steps) / ms_plain - 1.0,
+                                         "fallback_rate": fb / max(fl, 1), "engine": "warp mma.sync"}
+        s.destruir()
+    return out
+
+
 def run_ours(args):
     import torch
     world, rank, local = dist_setup()
@@ -263,11 +293,13 @@ def run_ours(args):
     stream = torch.cuda.Stream()
     vox = voxelizer_timing() if args.body == "mesh" else None
 
-    def make(storage):
+    def make(storage, closure=0, pesos=None):
         s = SolverCUDA(GRID, storage=storage, escrever_macros=False)
         s.definirStream(stream.cuda_stream)
         s.definirTipos(tipo)
-        s.configurar(**cfg)
+        s.configurar(**cfg, closure=closure)
+        if pesos is not None:
+            s.definirFecho(pesos)
         s.inicializar()
         return s
 
@@ -291,11 +323,7 @@ def run_ours(args):
         wall = time.perf_counter() - t0
         clk.stop()
     barrier()
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = reduce_max(ms, world, device="cuda")
     ms_step = ms / args.steps
     mlups = N * args.steps / (ms / 1e3) / 1e6 * world
 
@@ -330,6 +358,7 @@ def run_ours(args):
             forms[st] = {"MLUPS": m2, "vs_f32": m2 / (mlups / world),
                          "roofline_frac": BYTES_PER_CELL[st] * N / (ms2 / args.steps / 1e3) / 1e9 / peak}
             s2.destruir()
+        forms.update(closure_forms(make, stream, args.steps, args.warmup, ms_step, N))
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -339,7 +368,7 @@ def run_ours(args):
             cpu["voxelizer_ms_1_thread"] = cpu_voxelizer_ms()
     if rank == 0:
         line = {
-            "metric": "MLUPS (D3Q19 TRT+LES step, fp32 plain; 16-bit storage forms beside it)",
+            "metric": "MLUPS (D3Q19 TRT+LES step, fp32 plain; 16-bit storage and learned-closure forms beside it)",
             "value": mlups, "unit": "MLUPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": {"f32": "f32", "f16s": "f16 storage / f32 math", "bf16s": "bf16 storage / f32 math",

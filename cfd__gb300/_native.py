@@ -64,7 +64,8 @@ class ClosureWeights(C.Structure):
                 ("w2", C.c_float * (CLOSURE_H * CLOSURE_H)), ("b2", C.c_float * CLOSURE_H),
                 ("w3", C.c_float * CLOSURE_H), ("b3", C.c_float),
                 ("mean", C.c_float * CLOSURE_IN), ("std", C.c_float * CLOSURE_IN),
-                ("nu_scale", C.c_float), ("nu_max", C.c_float)]
+                ("nu_scale", C.c_float), ("nu_max", C.c_float),
+                ("lo", C.c_float * CLOSURE_IN), ("hi", C.c_float * CLOSURE_IN), ("coef", C.c_int32)]
 
 
 class ClosureCfg(C.Structure):

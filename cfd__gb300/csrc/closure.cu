@@ -33,7 +33,7 @@ constexpr int NP = NH * NI + NH + NH * NH + NH + NH + 1;   // 1313
 constexpr int OW1 = 0, OB1 = OW1 + NH * NI, OW2 = OB1 + NH, OB2 = OW2 + NH * NH, OW3 = OB2 + NH, OB3 = OW3 + NH;
 constexpr int TB = 64;   // samples per training block
 
-static_assert(sizeof(closure_weights) == sizeof(float) * (NP + 2 * NI + 2), "closure_weights layout");
+static_assert(sizeof(closure_weights) == sizeof(float) * (NP + 4 * NI + 3), "closure_weights layout");
 
 __device__ __forceinline__ float softplus(float y) { return y > 20.0f ? y : log1pf(expf(y)); }
 __device__ __forceinline__ float sigmoid(float y) { return 1.0f / (1.0f + expf(-y)); }
@@ -180,9 +180,12 @@ __global__ void __launch_bounds__(128) k_eval(const float* __restrict__ feats, l
   const long long i = (long long)blockIdx.x * 128 + threadIdx.x;
   float x[6];
 #pragma unroll
-  for (int a = 0; a < 6; ++a) x[a] = i < m ? (feats[i * 6 + a] - F->mean[a]) * F->inv_std[a] : 0.0f;
+  for (int a = 0; a < 6; ++a) x[a] = i < m ? feats[i * 6 + a] : 0.0f;
+  const bool inside = closure_in_range(*F, x);
+#pragma unroll
+  for (int a = 0; a < 6; ++a) x[a] = i < m ? (x[a] - F->mean[a]) * F->inv_std[a] : 0.0f;
   const float y = warp_mlp(*F, x);
-  if (i < m) nu[i] = closure_nu(*F, y);
+  if (i < m) nu[i] = inside ? closure_nu(*F, y) : __int_as_float(0x7fc00000);
 }
 
 // The same through the CTA-wide tcgen05 MLP (128 rows per block).
@@ -194,11 +197,14 @@ __global__ void __launch_bounds__(128) k_eval_tc(const float* __restrict__ feats
   const long long i = (long long)blockIdx.x * TC_ROWS + tid;
   float x[6];
 #pragma unroll
-  for (int a = 0; a < 6; ++a) x[a] = i < m ? (feats[i * 6 + a] - F->mean[a]) * F->inv_std[a] : 0.0f;
+  for (int a = 0; a < 6; ++a) x[a] = i < m ? feats[i * 6 + a] : 0.0f;
+  const bool inside = closure_in_range(*F, x);
+#pragma unroll
+  for (int a = 0; a < 6; ++a) x[a] = i < m ? (x[a] - F->mean[a]) * F->inv_std[a] : 0.0f;
   const uint32_t tmem = tc_begin(S, F->tcb, tid);
   const float y = tc_mlp(S, tmem, tid, x);
   tc_end(S, tmem, tid);
-  if (i < m) nu[i] = closure_nu(*F, y);
+  if (i < m) nu[i] = inside ? closure_nu(*F, y) : __int_as_float(0x7fc00000);
   if (tid == 0 && S.err) atomicOr(err, 1u);
 }
 
@@ -389,6 +395,8 @@ void closure_pack(const closure_weights* w, MlpFrag* F) {
   }
   F->nu_scale = w->nu_scale;
   F->nu_max = w->nu_max;
+  for (int a = 0; a < NI; ++a) { F->lo[a] = w->lo[a]; F->hi[a] = w->hi[a]; }
+  F->coef = w->coef != 0;
 }
 
 // Rows of closure_samples (see include/lbm_closure.h); scratch is allocated

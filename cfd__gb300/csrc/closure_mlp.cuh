@@ -28,7 +28,17 @@ struct MlpFrag {
   float b1[32], b2[32], b3;
   float mean[6], inv_std[6];
   float nu_scale, nu_max;
+  float lo[6], hi[6];           // raw-feature range of the training set
+  int coef;                     // output is Cs^2 (1) or nu_t (0)
 };
+
+// Raw features inside the trained range (false also for NaN features).
+__device__ __forceinline__ bool closure_in_range(const MlpFrag& F, const float (&f)[6]) {
+  bool ok = true;
+#pragma unroll
+  for (int a = 0; a < 6; ++a) ok = ok && f[a] >= __ldg(&F.lo[a]) && f[a] <= __ldg(&F.hi[a]);
+  return ok;
+}
 
 __device__ __forceinline__ void mma_bf16(float (&c)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
                                          uint2 b) {

@@ -139,6 +139,7 @@ struct lbm_ctx {
   int clo_engine = 0;                     // 0 warp mma.sync, 1 CTA tcgen05
   float* clo_nu = nullptr;                // held nu_t per cell (closure evaluated every k > 1 steps)
   int clo_since = -1;                     // steps since the last evaluation; -1: evaluate next
+  int clo_coef = 0;                       // the network gives Cs^2 (1) or nu_t (0)
 };
 
 namespace lbm {
@@ -253,6 +254,7 @@ int launch_step(lbm_ctx* c, bool mac, double* force) {
     A.err = reinterpret_cast<unsigned*>(c->clo_fb + 1);
     A.nu = c->clo_nu;
     A.omega0 = 1.0f / make_uni<float>(c->P).tau0;
+    A.coef = c->clo_coef;
     cudaError_t e = c->ops.step_closure(d, c->P, parity(c), mac, force != nullptr, c->clo_engine, mode, A, c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "closure step kernel launch");
     c->steps++;
@@ -519,6 +521,7 @@ int lbm_set_closure(lbm_ctx* c, const closure_weights* w) {
     return fail(LBM_ENOTSUP, "the learned closure runs in the in-place FAST step with fp32 arithmetic only");
   lbm::MlpFrag F;
   lbm::closure_pack(w, &F);
+  c->clo_coef = w->coef != 0;
   if (!c->clo) {
     int r = dalloc(c, (void**)&c->clo, sizeof(lbm::MlpFrag), "closure network");
     if (r) return r;

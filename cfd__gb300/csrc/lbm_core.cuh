@@ -331,6 +331,22 @@ __device__ __forceinline__ void smag_rates_fast(const Params& P, const Uni<R>& U
   }
 }
 
+// The same relaxation with a per-cell coefficient: c18 = 18 Cs^2 (the
+// learned closure's coefficient form), whatever U.les_on says.
+template <typename R>
+__device__ __forceinline__ void smag_rates_c18(const Params& P, const Uni<R>& U, const R* ns, R rinv, R c18,
+                                               R& omegaP, R& omegaM) {
+  const PiT<R> q = pi_fast<R>(ns);
+  const R pd = fma_r<R>(q.zz, q.zz, fma_r<R>(q.yy, q.yy, q.xx * q.xx));
+  const R po = fma_r<R>(q.yz, q.yz, fma_r<R>(q.xz, q.xz, q.xy * q.xy));
+  const R pp = fma_r<R>(R(2.0), po, pd);
+  const R qs = r_sqrt(R(2.0) * pp);
+  const R tauT = R(0.5) * (U.tau0 + r_sqrt(fma_r<R>(c18 * qs, rinv, U.tau0sq)));
+  omegaP = R(1.0) / tauT;
+  const R tm = tauT - R(0.5);
+  omegaM = tm / fma_r<R>(R(0.5), tm, R(P.magic));
+}
+
 // TRT per pair and the sponge blend (src/core/emit/ir.js:304-323, :458-478).
 template <typename R, typename Emit>
 __device__ __forceinline__ void trt_emit_fast(const Uni<R>& U, int x, const R* g, R e0, const R* ns, const R* nd,

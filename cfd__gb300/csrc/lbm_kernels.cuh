@@ -236,8 +236,9 @@ struct CloArgs {
   const MlpFrag* F;             // the network
   unsigned long long* nfb;      // fallback counter (cells whose output was not usable)
   unsigned* err;                // set when a tensor-core wait gave up (engine 1)
-  float* nu;                    // per-cell nu_t: written by mode 1, read by mode 2
+  float* nu;                    // per-cell output: written by mode 1, read by mode 2
   float omega0;                 // feature x4 = 1 / tau0
+  int coef;                     // 1: the output is a Smagorinsky Cs^2, 0: nu_t
 };
 
 // Shared memory of the two network engines: the warp engine parks a fluid
@@ -257,8 +258,10 @@ struct CloShared<1> {
 // FAST form).  The same pull, bounce-back and fused force as step_cell.
 // MODE 0: for FLUIDO cells the six features of the pulled non-equilibrium
 //   stress feed the network, which gives nu_t and tau = tau0 + 3 nu_t,
-//   omega- keeping Lambda fixed; a cell whose output is not usable relaxes
-//   with the Smagorinsky rates (src/core/emit/ir.js:284-299) and is counted.
+//   omega- keeping Lambda fixed (or, in the coefficient form, a per-cell
+//   Cs^2 for the Smagorinsky relaxation); a cell whose features are outside the
+//   trained range or whose output is not usable relaxes with the Smagorinsky
+//   rates (src/core/emit/ir.js:284-299) and is counted.
 // MODE 1: the same, and nu_t (NaN for a fallback cell) is stored per cell.
 // MODE 2: no network: the rates come from the stored nu_t (Smagorinsky where
 //   it is NaN) -- the steps between two network evaluations of a closure
@@ -301,7 +304,7 @@ k_step_closure(Dev d, Params P, Uni<float> U, CloArgs A) {
   R g[Q];
   R delta = R(0.0), rho = R(1.0), ux = R(0.0), uy = R(0.0), uz = R(0.0), uu = R(0.0), rinv = R(1.0);
   float feat[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-  bool fluid = false;
+  bool fluid = false, inside = false;
   if (inr) {
     const uint32_t lw = __ldg(d.link + cell);
     g[0] = St::ld(Fc);
@@ -356,6 +359,7 @@ k_step_closure(Dev d, Params P, Uni<float> U, CloArgs A) {
           closure_features(m.xx - d3 - rux * ux, m.yy - d3 - ruy * uy, m.zz - d3 - ruz * uz, m.xy - rux * uy,
                            m.xz - rux * uz, m.yz - ruy * uz, rinv, delta, feat);
           feat[4] = A.omega0;
+          inside = closure_in_range(*A.F, feat);
 #pragma unroll
           for (int a = 0; a < 6; ++a) feat[a] = (feat[a] - __ldg(&A.F->mean[a])) * __ldg(&A.F->inv_std[a]);
           if constexpr (ENG == 0) {
@@ -389,7 +393,7 @@ k_step_closure(Dev d, Params P, Uni<float> U, CloArgs A) {
         uy = SH.stash[Q + 3][tid]; uz = SH.stash[Q + 4][tid]; uu = SH.stash[Q + 5][tid];
         rinv = SH.stash[Q + 6][tid];
       }
-      nu = closure_nu(*A.F, yv);
+      nu = inside ? closure_nu(*A.F, yv) : __int_as_float(0x7fc00000);
       if (MODE == 1) A.nu[cell] = nu;
     }
   } else {
@@ -407,9 +411,14 @@ k_step_closure(Dev d, Params P, Uni<float> U, CloArgs A) {
     fluid_neq_fast<R>(sp, dp, delta, rho, ux, uy, uz, uu, e0, ns, nd);
     R omegaP, omegaM;
     if (nu == nu) {
-      const float tauT = U.tau0 + 3.0f * nu, tm = tauT - 0.5f;
-      omegaP = __frcp_rn(tauT);
-      omegaM = __fdividef(tm, fmaf(0.5f, tm, P.magic));
+      if (A.coef) {
+        // coefficient form: the output is Cs^2 of the Smagorinsky relaxation
+        smag_rates_c18<R>(P, U, ns, rinv, 18.0f * nu, omegaP, omegaM);
+      } else {
+        const float tauT = U.tau0 + 3.0f * nu, tm = tauT - 0.5f;
+        omegaP = __frcp_rn(tauT);
+        omegaM = __fdividef(tm, fmaf(0.5f, tm, P.magic));
+      }
     } else {
       fell_back = true;
       smag_rates_fast<R>(P, U, ns, rinv, omegaP, omegaM);

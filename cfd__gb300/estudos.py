@@ -2,7 +2,7 @@
 
     python -m cfd__gb300.estudos precisao [--steps 10000] [--grid 512,256,192]
     python -m cfd__gb300.estudos lote [--steps 256]
-    python -m cfd__gb300.estudos fecho [--steps 16000] [--pesos w.npz]
+    python -m cfd__gb300.estudos fecho [--steps 24000] [--pesos w.npz]
 
 precisao: the 512x256x192 precision workload (25.2 M cells): the seeded
 superellipsoid (semi-axes 80x32x22 cells, 20k triangles, 0.3-cell jitter)
@@ -188,23 +188,36 @@ def tuneis_fecho(seed=2026):
     return out[0], out[1]
 
 
-def fecho(re_treino=(2000, 5000, 20000), re_teste=10000, passos_finos=16000, snapshots=4, intervalo=1000,
+def fecho(re_treino=(2000, 5000, 20000), re_teste=10000, passos_finos=24000, snapshots=4, intervalo=1000,
           por_snapshot=300000, passos_treino=3000, cs=0.12, u=0.06, comprimento=96.0, semente=2026,
-          s_min=2e-4, pesos_saida=None):
-    """Learned-closure workload.  Fine runs (2x resolution, FP32, Smagorinsky
-    Cs) at the training Reynolds numbers give, at their last `snapshots`
-    states `intervalo` fine steps apart, a-priori samples (closure_samples:
-    2x2x2 box filter, least-squares eddy viscosity of the resolved residual
-    stress, coarse-grid features); `por_snapshot` valid rows are drawn from
-    x in [0.25, 0.85) of the coarse length; the target is 0 where the
-    filtered strain rate is below s_min and is clipped at the 99.9th
-    percentile of its positive values for training.  The MLP is trained on
-    them (batch 65 536, Adam) and evaluated at the held-out Reynolds number:
-    a-priori (held-out samples) against Smagorinsky, and a-posteriori by
-    coarse runs with the closure and with Smagorinsky whose Cd (over the last
-    half of passos_finos / 2 coarse steps) is compared with the fine run's.
-    Also: the fallback rate and the closure step's time against the
-    Smagorinsky step."""
+          s_min=2e-4, escalas=(2.0, 1.0, 0.5, 0.25, 0.125), cada=8, forma="coef", pesos_saida=None):
+    """Learned-closure workload.
+
+    Fine runs (2x resolution, FP32, Smagorinsky Cs) at the training and the
+    held-out Reynolds numbers; at their last `snapshots` states `intervalo`
+    fine steps apart, a-priori samples (closure_samples: 2x2x2 box filter,
+    least-squares eddy viscosity of the resolved residual stress, coarse-grid
+    features; target 0 where the filtered strain rate is below s_min);
+    `por_snapshot` valid rows drawn from x in [0.25, 0.85) of the coarse
+    length.  forma "nu": the network's output is nu_t and the target the
+    a-priori eddy viscosity; forma "coef" (default): the output is a
+    per-cell Smagorinsky Cs^2 used with the step's own |S| estimate, the
+    target nu_t / |S| of the filtered field, feature x0 (the magnitude,
+    whose in-situ distribution is dominated by grid-scale non-equilibrium
+    at omega near 2) switched off and the bounded invariants x1..x3 checked
+    against their mathematical range only.  Training on the training
+    Reynolds numbers (targets clipped at the 99.9th percentile of their
+    positive values; batch 65 536, Adam).
+    A-posteriori calibration: coarse runs at the training Reynolds numbers
+    with nu_t scaled by each factor in `escalas`; the factor with the
+    smallest mean |Cd error| against the fine runs is kept.  Evaluation at
+    the held-out Reynolds number: a-priori (held-out samples, network and
+    Smagorinsky against the target) and a-posteriori (coarse runs: learned
+    closure every step and every `cada`-th step, Smagorinsky, no model; Cd
+    over the second half of passos_finos / 2 coarse steps, from the force
+    averaged over each block of steps, against the fine run's Cd over the
+    same physical time).  Step time of each coarse form from 400 steps
+    timed alone, and the fallback rate of the network."""
     import torch
 
     from .fecho import amostras, avaliar, normalizacao, pesos_vazios, salvar, treinar
@@ -218,49 +231,51 @@ def fecho(re_treino=(2000, 5000, 20000), re_teste=10000, passos_finos=16000, sna
     cx = gc["nx"]
     x0, x1 = int(0.25 * cx), int(0.85 * cx)
     out = {"coarse": gc, "fine": gf, "frontal_area": {"coarse": ac, "fine": af}, "u_in": u, "cs": cs,
-           "length_coarse": comprimento, "fine_runs": {}, "coarse_runs": {}}
+           "length_coarse": comprimento, "s_min": s_min, "fine_runs": {}, "calibration": {}, "coarse_runs": {}}
 
-    def cd_de(f, area, g):
-        return coeficientes(f, units, area, g)["cd"]
-
-    def rodar(g, tipo, esp, area, re, passos, bloco, closure=None, colher=None, cs_run=cs):
+    def rodar(g, tipo, esp, area, re, passos, bloco, closure=None, cada_k=1, colher=None, cs_run=cs,
+              cronometrar=False):
         L = comprimento * g["nx"] / cx
         nu = u * L / re
         s = SolverCUDA(g, escrever_macros=False)
         s.definirStream(stream.cuda_stream)
         s.definirTipos(tipo)
         s.configurar(omegaPlus=1.0 / (3.0 * nu + 0.5), lesCs=cs_run, inletU=[u, 0.0, 0.0], esponja=esp,
-                     closure=1 if closure is not None else 0)
+                     closure=cada_k if closure is not None else 0)
         if closure is not None:
             s.definirFecho(closure)
             s.estatisticasFecho()
         s.inicializar()
-        cds, ms, feito, amos = [], 0.0, 0, []
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        cds, feito, amos = [], 0, []
+        t0 = time.time()
         while feito < passos:
             n = min(bloco, passos - feito)
-            e0.record(stream)
-            s.passo(n - 1)
-            f = s.passoComForcas(1)
-            e1.record(stream)
-            e1.synchronize()
-            ms += e0.elapsed_time(e1)
+            f = s.passoComForcas(n)
             feito += n
-            c = cd_de(f[-1] if np.ndim(f) > 1 else f, area, g)
+            c = coeficientes(f.mean(axis=0), units, area, g)["cd"]
             cds.append(c)
             if not np.isfinite(c) or abs(c) > 100:
                 break
             if colher is not None and feito > passos - snapshots * intervalo and (passos - feito) % intervalo == 0:
                 amos.append(colher(s))
-        rec = {"Re": re, "omega_plus": 1.0 / (3.0 * nu + 0.5), "steps": feito, "ms_per_step": ms / max(feito, 1),
-               "MLUPS": s.N * feito / (ms / 1e3) / 1e6, "diverged": bool(feito < passos)}
+        rec = {"Re": re, "omega_plus": 1.0 / (3.0 * nu + 0.5), "steps": feito, "diverged": bool(feito < passos),
+               "wall_s": time.time() - t0}
         tail = cds[len(cds) // 2:]
         rec["cd"] = float(np.mean(tail)) if tail and not rec["diverged"] else float("nan")
         rec["cd_std"] = float(np.std(tail)) if tail and not rec["diverged"] else float("nan")
         if closure is not None:
             fb, fl = s.estatisticasFecho()
-            rec["fallback_cells"], rec["fluid_cell_updates"] = fb, fl
+            rec["fallback_cells"], rec["network_cell_evaluations"] = fb, fl
             rec["fallback_rate"] = fb / max(fl, 1)
+        if cronometrar and not rec["diverged"]:
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            s.passo(400)
+            e1.record(stream)
+            e1.synchronize()
+            rec["ms_per_step"] = e0.elapsed_time(e1) / 400
+            rec["MLUPS"] = s.N / rec["ms_per_step"] / 1e3
         s.destruir()
         return rec, amos
 
@@ -287,11 +302,24 @@ def fecho(re_treino=(2000, 5000, 20000), re_teste=10000, passos_finos=16000, sna
     treino = [re for re in re_treino if re in dados]
     F = np.concatenate([dados[re][0] for re in treino])
     T = np.concatenate([dados[re][1] for re in treino])
+    def alvo(Fx, Tx, re):
+        if forma != "coef":
+            return Tx
+        tau0c = 3.0 * u * comprimento / re + 0.5
+        s_abs = 1.5 * np.exp(Fx[:, 0].astype(np.float64)) / (tau0c + 3.0 * Tx)   # |S| of the filtered field
+        return np.where(Tx > 0, Tx / np.maximum(s_abs, 1e-30), 0.0).astype(np.float32)
+    T = np.concatenate([alvo(dados[re][0], dados[re][1], re) for re in treino])
     pos = T[T > 0]
     t_clip = float(np.quantile(pos, 0.999)) if pos.size else 1.0
     T = np.minimum(T, np.float32(t_clip))
     p = pesos_vazios()
     p.update(normalizacao(F, T))
+    if forma == "coef":
+        p["coef"] = 1
+        p["mean"][0], p["std"][0] = 0.0, 1e30
+        bound = np.array([np.inf, 1.2248, 0.069, 1.0], np.float32)
+        p["lo"][:4] = -bound
+        p["hi"][:4] = bound
     t0 = time.time()
     p, hist = treinar(F, T, p, passos=int(passos_treino * 2 // 3), lote=65536, lr=2e-3, semente=semente)
     p, hist2 = treinar(F, T, p, passos=int(passos_treino // 3), lote=65536, lr=5e-4, semente=semente + 1,
@@ -299,16 +327,15 @@ def fecho(re_treino=(2000, 5000, 20000), re_teste=10000, passos_finos=16000, sna
     out["training"] = {"samples": int(T.size), "Re": list(treino), "steps": int(passos_treino), "batch": 65536,
                        "seconds": time.time() - t0, "loss_first": float(hist[:10].mean()),
                        "loss_last": float(hist2[-50:].mean()), "nu_scale": p["nu_scale"], "nu_max": p["nu_max"],
-                       "target_clip": t_clip}
-    if pesos_saida:
-        salvar(p, pesos_saida)
+                       "target_clip": t_clip, "form": forma}
     # a-priori on the held-out Reynolds number
     if re_teste in dados:
         Fv, Tv = dados[re_teste]
-        Tv = np.minimum(Tv, np.float32(t_clip))
-        nu_net = avaliar(p, Fv)
         tau0c = 3.0 * u * comprimento / re_teste + 0.5
         s_mag = 1.5 * np.exp(Fv[:, 0].astype(np.float64)) / (tau0c + 3.0 * Tv)   # |S| from x0
+        out_net = avaliar(p, Fv)
+        nu_net = out_net * s_mag if forma == "coef" else out_net
+        Tv = np.minimum(Tv, np.float32(t_clip * (np.max(s_mag) if forma == "coef" else 1.0)))
         nu_smag = cs * cs * s_mag
         ok = np.isfinite(nu_net)
 
@@ -318,14 +345,45 @@ def fecho(re_treino=(2000, 5000, 20000), re_teste=10000, passos_finos=16000, sna
         out["a_priori"] = {"Re": re_teste, "rows": int(Tv.size), "closure": metr(nu_net[ok], Tv[ok]),
                            "smagorinsky": metr(nu_smag, Tv), "fallback_rows": int((~ok).sum())}
     passos_grossos = passos_finos // 2
-    for nome, clo, c_s in (("smagorinsky", None, cs), ("closure", p, cs), ("no_model", None, 0.0)):
-        rec, _ = rodar(gc, tc, ec, ac, re_teste, passos_grossos, intervalo // 4, closure=clo, cs_run=c_s)
+    bloco_g = intervalo // 4
+
+    def escalado(c):
+        q = dict(p)
+        q["nu_scale"] = p["nu_scale"] * c
+        return q
+    # a-posteriori calibration on the training Reynolds numbers
+    melhor, melhor_err = 1.0, float("inf")
+    for c in escalas:
+        errs = []
+        for re in treino:
+            rec, _ = rodar(gc, tc, ec, ac, re, passos_grossos, bloco_g, closure=escalado(c), cada_k=cada)
+            fine_cd = out["fine_runs"][str(re)]["cd"]
+            errs.append(abs(rec["cd"] - fine_cd) / abs(fine_cd))
+        e = float(np.mean(errs)) if np.all(np.isfinite(errs)) else float("inf")
+        out["calibration"][str(c)] = {"cd_abs_err_per_Re": errs, "mean": e}
+        if e < melhor_err:
+            melhor, melhor_err = c, e
+    smag_train = []
+    for re in treino:
+        rec, _ = rodar(gc, tc, ec, ac, re, passos_grossos, bloco_g)
+        smag_train.append(abs(rec["cd"] - out["fine_runs"][str(re)]["cd"]) / abs(out["fine_runs"][str(re)]["cd"]))
+    out["calibration"]["chosen"] = melhor
+    out["calibration"]["smagorinsky_cd_abs_err_per_Re"] = smag_train
+    pf = escalado(melhor)
+    if pesos_saida:
+        salvar(pf, pesos_saida)
+    for nome, clo, k, c_s in (("smagorinsky", None, 1, cs), ("closure_every_step", pf, 1, cs),
+                              (f"closure_every_{cada}", pf, cada, cs), ("no_model", None, 1, 0.0)):
+        rec, _ = rodar(gc, tc, ec, ac, re_teste, passos_grossos, bloco_g, closure=clo, cada_k=k, cs_run=c_s,
+                       cronometrar=True)
         out["coarse_runs"][nome] = rec
     fine_cd = out["fine_runs"][str(re_teste)]["cd"]
     for nome, rec in out["coarse_runs"].items():
         rec["cd_err_vs_fine"] = (rec["cd"] - fine_cd) / fine_cd
-    sm, cl = out["coarse_runs"]["smagorinsky"], out["coarse_runs"]["closure"]
-    out["closure_overhead"] = cl["ms_per_step"] / sm["ms_per_step"] - 1.0
+    sm = out["coarse_runs"]["smagorinsky"]
+    out["closure_overhead"] = {nome: rec["ms_per_step"] / sm["ms_per_step"] - 1.0
+                               for nome, rec in out["coarse_runs"].items()
+                               if nome.startswith("closure") and "ms_per_step" in rec}
     return out
 
 

@@ -7,8 +7,10 @@ training (hand-written CUDA forward / backward / Adam), evaluation through the
 tensor-core path the fused step uses, and the training samples cut from a
 fine run.
 
-Network: 6 -> 32 -> 32 -> 1, ReLU hidden layers, nu_t = nu_scale *
-softplus(y).  Features (raw, then normalised (x - mean) / std):
+Network: 6 -> 32 -> 32 -> 1, ReLU hidden layers, output nu_scale *
+softplus(y): the eddy viscosity nu_t, or (coef = 1) a per-cell Smagorinsky
+coefficient Cs^2 that the step uses with its own |S| estimate.  Features
+(raw, then normalised (x - mean) / std):
     x0 = ln(qs/rho + 1e-9), qs = sqrt(2 Pi:Pi)
     x1 = tr(Pi) / (qs + 1e-12)
     x2 = det(Pi) / (qs^3 + 1e-30)
@@ -38,6 +40,9 @@ def pesos_vazios():
     d["std"] = np.ones(NI, np.float32)
     d["nu_scale"] = 1.0
     d["nu_max"] = 1.0
+    d["lo"] = np.full(NI, -np.inf, np.float32)
+    d["hi"] = np.full(NI, np.inf, np.float32)
+    d["coef"] = 0
     return d
 
 
@@ -65,6 +70,12 @@ def para_struct(p) -> nat.ClosureWeights:
         w.std[a] = float(p["std"][a])
     w.nu_scale = float(p["nu_scale"])
     w.nu_max = float(p["nu_max"])
+    lo = p.get("lo", np.full(NI, -np.inf))
+    hi = p.get("hi", np.full(NI, np.inf))
+    for a in range(NI):
+        w.lo[a] = float(lo[a])
+        w.hi[a] = float(hi[a])
+    w.coef = int(p.get("coef", 0))
     return w
 
 
@@ -75,6 +86,9 @@ def de_struct(w: nat.ClosureWeights, base=None):
     p["std"] = np.array(w.std[:], np.float32)
     p["nu_scale"] = float(w.nu_scale)
     p["nu_max"] = float(w.nu_max)
+    p["lo"] = np.array(w.lo[:], np.float32)
+    p["hi"] = np.array(w.hi[:], np.float32)
+    p["coef"] = int(w.coef)
     return p
 
 
@@ -138,9 +152,11 @@ def amostras(solver, tau0_grosso, x0=None, x1=None, s_min=0.0):
     return f, t
 
 
-def normalizacao(feats, target, q_escala=0.9, q_max=0.999, fator_max=20.0):
+def normalizacao(feats, target, q_escala=0.9, q_max=0.999, fator_max=20.0, q_faixa=1e-4):
     """mean / std of the features; nu_scale = the q_escala quantile of the
-    positive targets; nu_max = fator_max times their q_max quantile."""
+    positive targets; nu_max = fator_max times their q_max quantile; the
+    trained range [lo, hi] of each raw feature = its q_faixa and 1 - q_faixa
+    quantiles (a constant feature gets its value +- 1 %)."""
     f, t = _rows(feats, target)
     mean = f.mean(axis=0).astype(np.float32)
     std = f.std(axis=0).astype(np.float32)
@@ -148,7 +164,13 @@ def normalizacao(feats, target, q_escala=0.9, q_max=0.999, fator_max=20.0):
     pos = t[t > 0]
     escala = float(np.quantile(pos, q_escala)) if pos.size else 1e-4
     alto = float(np.quantile(pos, q_max)) if pos.size else escala
-    return {"mean": mean, "std": std, "nu_scale": max(escala, 1e-8), "nu_max": float(fator_max * max(alto, escala))}
+    lo = np.quantile(f, q_faixa, axis=0)
+    hi = np.quantile(f, 1.0 - q_faixa, axis=0)
+    larg = np.maximum(hi - lo, 0.01 * np.abs(hi))
+    lo = np.where(hi - lo < 1e-9, lo - larg, lo)
+    hi = np.where(hi - lo < 1e-9, hi + larg, hi)
+    return {"mean": mean, "std": std, "nu_scale": max(escala, 1e-8), "nu_max": float(fator_max * max(alto, escala)),
+            "lo": lo.astype(np.float32), "hi": hi.astype(np.float32)}
 
 
 def salvar(p, caminho):
@@ -161,5 +183,8 @@ def carregar(caminho):
     p = pesos_vazios()
     for k in d.files:
         v = d[k]
-        p[k] = float(v) if k in ("nu_scale", "nu_max") else (np.float32(v) if v.shape == () else v.astype(np.float32))
+        if k == "coef":
+            p[k] = int(v)
+        else:
+            p[k] = float(v) if k in ("nu_scale", "nu_max") else (np.float32(v) if v.shape == () else v.astype(np.float32))
     return p

@@ -16,9 +16,11 @@
  *   x3 = (Pxy^2 + Pxz^2 + Pyz^2) / (Pi:Pi/2 + 1e-30)
  *   x4 = omega0 = 1 / tau0     (the local molecular relaxation rate)
  *   x5 = 100 delta             (density deviation)
- * normalised as (x - mean) / std, rounded to bf16 for the tensor cores;
- * weights bf16, accumulation fp32 (mma.sync m16n8k16).  Training runs in fp32
- * with hand-written forward / backward / Adam kernels.
+ * checked against the trained range [lo, hi] (outside: Smagorinsky for that
+ * cell), normalised as (x - mean) / std, rounded to bf16 for the tensor cores;
+ * weights bf16, accumulation fp32 (tensor cores).  Training runs in fp32
+ * with hand-written forward / backward / Adam kernels.  A feature can be
+ * switched off by giving it a huge std (its normalised value is then 0).
  */
 #ifndef CFD_GB300_LBM_CLOSURE_H
 #define CFD_GB300_LBM_CLOSURE_H
@@ -45,6 +47,13 @@ typedef struct {
   float mean[CLOSURE_IN], std[CLOSURE_IN];
   float nu_scale;                      /* nu_t = nu_scale * softplus(y) */
   float nu_max;                        /* above this the cell falls back to Smagorinsky */
+  float lo[CLOSURE_IN], hi[CLOSURE_IN];   /* raw-feature range the network was trained on:
+                                             a cell outside it falls back to Smagorinsky
+                                             (-inf / +inf: no bound) */
+  int32_t coef;                        /* 0: the output is nu_t (tau = tau0 + 3 nu_t);
+                                          1: the output is a per-cell Smagorinsky Cs^2,
+                                          relaxed as src/core/emit/ir.js:284-299 does
+                                          with 18 Cs^2 from the network */
 } closure_weights;
 
 typedef struct {

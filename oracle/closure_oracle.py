@@ -121,7 +121,7 @@ def bf16(a):
     return r.view(np.float32)
 
 
-def eval_bf16(v, feats, mean, std, nu_scale, nu_max, bias_bf16=False):
+def eval_bf16(v, feats, mean, std, nu_scale, nu_max, bias_bf16=False, lo=None, hi=None):
     """nu per row as a tensor-core engine computes it (see module text);
     bias_bf16: the biases rounded to bf16 (the CTA engine carries them in the
     K dimension), else fp32 (the warp engine starts its accumulators at them)."""
@@ -142,6 +142,11 @@ def eval_bf16(v, feats, mean, std, nu_scale, nu_max, bias_bf16=False):
     with np.errstate(over="ignore", invalid="ignore"):
         nu = float(np.float32(nu_scale)) * softplus(y)
     ok = np.isfinite(nu) & (nu >= 0) & (nu <= float(np.float32(nu_max)))
+    f = np.asarray(feats, np.float32)
+    if lo is not None:
+        ok &= (f >= np.asarray(lo, np.float32)).all(axis=1)
+    if hi is not None:
+        ok &= (f <= np.asarray(hi, np.float32)).all(axis=1)
     return np.where(ok, nu, np.nan), y
 
 

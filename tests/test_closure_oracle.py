@@ -89,6 +89,6 @@ def test_samples_solid_masks_neighbours():
 
 def test_abi_struct_sizes():
     from cfd__gb300 import _native as nat
-    assert C.sizeof(nat.ClosureWeights) == 4 * (1313 + 14)
+    assert C.sizeof(nat.ClosureWeights) == 4 * (1313 + 27)
     assert C.sizeof(nat.ClosureCfg) == 40
     assert nat.ClosureCfg.seed.offset == 24

@@ -83,6 +83,17 @@ def test_inference_fallback_marks(native, motor):
     q = fecho.pesos_vazios()
     q["b3"] = np.float32(np.nan)
     assert np.isnan(fecho.avaliar(q, f, motor)).all()
+    # raw features outside the trained range fall back
+    r = dict(p)
+    r["nu_max"] = 1.0
+    r["lo"] = np.full(6, -2.0, np.float32)
+    r["hi"] = np.full(6, 2.0, np.float32)
+    nu = fecho.avaliar(r, f, motor)
+    ref, _ = CO.eval_bf16(fecho.vetor(r), f, r["mean"], r["std"], r["nu_scale"], r["nu_max"], bias_bf16=motor == 1,
+                          lo=r["lo"], hi=r["hi"])
+    out = (np.abs(f) > 2.0).any(axis=1)
+    assert out.any() and (~out).any()
+    assert np.isnan(nu[out]).all() and np.array_equal(np.isnan(nu), np.isnan(ref))
 
 
 def test_training_deterministic_and_fits(native):
@@ -97,7 +108,9 @@ def test_training_deterministic_and_fits(native):
     assert np.array_equal(fecho.vetor(a), fecho.vetor(b)) and np.array_equal(ha, hb)
     assert ha[-20:].mean() < 0.05 * ha[:5].mean(), (ha[:5], ha[-20:])
     nu = fecho.avaliar(a, f[:20000])
-    rel = np.linalg.norm(nu - t[:20000]) / np.linalg.norm(t[:20000])
+    ok = np.isfinite(nu)          # rows outside the trained range (1e-4 quantiles) fall back
+    assert ok.mean() > 0.995
+    rel = np.linalg.norm(nu[ok] - t[:20000][ok]) / np.linalg.norm(t[:20000][ok])
     assert rel < 0.1, rel
 
 
@@ -187,6 +200,26 @@ def test_constant_nu_matches_plain_step(native, motor, every):
     plain = dict(omegaPlus=1.0 / (tau0 + 3 * nu_eff), lesCs=0.0, inletU=[0.05, 0, 0.01], beltU=[0.05, 0, 0])
     clo = dict(omegaPlus=1.9, lesCs=0.12, inletU=[0.05, 0, 0.01], beltU=[0.05, 0, 0], closure=every)
     (a, b), fl, tipo = _run_pair(p, plain, clo, motor=motor)
+    ga, gb = a[0][:, fl], b[0][:, fl]
+    assert np.abs(ga - gb).max() <= 2e-6 * np.abs(ga).max()
+    np.testing.assert_allclose(a[1], b[1], rtol=1e-4, atol=1e-9)
+    assert b[2][0] == 0
+
+
+@pytest.mark.parametrize("motor,every", [(0, 1), (1, 1), (0, 4)])
+def test_constant_coefficient_matches_smagorinsky(native, motor, every):
+    """Coefficient form with a network that outputs a constant Cs^2 = 0.0144
+    relaxes like the Smagorinsky step with Cs = 0.12."""
+    from cfd__gb300 import fecho
+    p = fecho.pesos_vazios()
+    p["coef"] = 1
+    p["nu_scale"] = 0.0144
+    p["nu_max"] = 1.0
+    p["b3"] = CO.bf16(np.array([np.log(np.expm1(1.0))], np.float32))[0]   # softplus(b3) ~ 1
+    cs2 = float(np.float32(0.0144) * np.float32(np.log1p(np.exp(np.float64(p["b3"])))))
+    smag = dict(omegaPlus=1.9, lesCs=float(np.sqrt(cs2)), inletU=[0.05, 0, 0.01], beltU=[0.05, 0, 0])
+    clo = dict(smag, lesCs=0.3, closure=every)
+    (a, b), fl, tipo = _run_pair(p, smag, clo, motor=motor)
     ga, gb = a[0][:, fl], b[0][:, fl]
     assert np.abs(ga - gb).max() <= 2e-6 * np.abs(ga).max()
     np.testing.assert_allclose(a[1], b[1], rtol=1e-4, atol=1e-9)
