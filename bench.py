@@ -260,19 +260,22 @@ def reduce_max(value, world, device="cpu"):
 
 def closure_forms(make, stream, steps, warmup, ms_plain, N):
     """Step time of the learned closure (coefficient form, weights trained by
-    `python -m cfd__gb300.estudos fecho`) evaluated every step and every 8th
-    step, against the Smagorinsky step of the same tunnel."""
+    `python -m cfd__gb300.estudos fecho`) evaluated every step, every 8th and
+    every 16th step (warp engine) and every step on the CTA tcgen05 engine,
+    against the Smagorinsky step of the same tunnel."""
     from cfd__gb300.fecho import carregar
     p = carregar(os.path.join(ROOT, "cfd__gb300", "pesos", "fecho_coef.npz"))
     out = {}
-    for every in (1, 8):
+    for every, motor in ((1, 0), (8, 0), (16, 0), (1, 1)):
         s = make("f32", closure=every, pesos=p)
+        s.motorFecho(motor)
         s.passo(warmup)
         ms = time_steps(s, stream, steps)
         fb, fl = s.estatisticasFecho()
-        out[f"closure_every_{every}"] = {"MLUPS": N * steps / (ms / 1e3) / 1e6,
-                                         "overhead_vs_smagorinsky": (ms / steps) / ms_plain - 1.0,
-                                         "fallback_rate": fb / max(fl, 1), "engine": "warp mma.sync"}
+        name = f"closure_every_{every}" + ("_tcgen05" if motor else "")
+        out[name] = {"MLUPS": N * steps / (ms / 1e3) / 1e6, "overhead_vs_smagorinsky": (ms / steps) / ms_plain - 1.0,
+                     "fallback_rate": fb / max(fl, 1),
+                     "engine": "CTA tcgen05.mma, TMEM accumulators" if motor else "warp mma.sync"}
         s.destruir()
     return out
 

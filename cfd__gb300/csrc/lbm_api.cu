@@ -255,7 +255,8 @@ int launch_step(lbm_ctx* c, bool mac, double* force) {
     A.nu = c->clo_nu;
     A.omega0 = 1.0f / make_uni<float>(c->P).tau0;
     A.coef = c->clo_coef;
-    cudaError_t e = c->ops.step_closure(d, c->P, parity(c), mac, force != nullptr, c->clo_engine, mode, A, c->stream);
+    cudaError_t e = c->ops.step_closure(d, c->P, parity(c), mac, force != nullptr, c->clo_engine, mode, A,
+                                        cell_launch(c), c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "closure step kernel launch");
     c->steps++;
     if (mode != 2) c->clo_steps++;

@@ -128,7 +128,7 @@ __device__ __forceinline__ R signed_sum(const R* v, K coef) {
 //    omega- = (tau - 1/2) / (Lambda + (tau - 1/2)/2), which is
 //    1 / (Lambda / (1/omega+ - 1/2) + 1/2) with 1/omega+ = tau exactly
 //    (src/core/emit/ir.js:297-299).  Rounding differs from STRICT by ~1 ulp per
-//    operation; the fp64 judge always runs STRICT.
+//    operation; the fp64 reference form always runs STRICT.
 // Explicit fmaf() stays fused under -fmad=false, so both modes are fixed
 // sequences of IEEE operations.
 template <typename R>
@@ -488,7 +488,7 @@ __device__ __forceinline__ void collide(const Params& P, const Uni<R>& U, uint32
 }
 
 // ---------------------------------------------------------------- storage
-// Population storage forms.  Arithmetic is float (or double for the judge).
+// Population storage forms.  Arithmetic is float (or double for the fp64 reference form).
 struct StF32 {
   using store_t = float;
   using real = float;

@@ -268,7 +268,8 @@ struct CloShared<1> {
 //   that is evaluated every k-th step.
 // ENG 0: warp engine (closure_mlp.cuh, mma.sync per 32 cells); ENG 1: CTA
 // engine (closure_tc.cuh, tcgen05.mma per 128 cells).  Every other class goes
-// through collide() unchanged, before the network.  64 x 2 threads per block.
+// through collide() unchanged, before the network.  Modes 0 and 1 run 64 x 2
+// threads per block; mode 2 any shape.
 template <class St, int PAR, bool MAC, bool FRC, bool W64, int ENG, int MODE>
 __global__ void __launch_bounds__(128, MODE == 2 ? 8 : 6)
 k_step_closure(Dev d, Params P, Uni<float> U, CloArgs A) {
@@ -801,16 +802,16 @@ struct Ops {
   cudaError_t (*forces)(const Dev&, int parity, bool inplace, double* partials, Launch, cudaStream_t);
   cudaError_t (*mass)(const Dev&, int parity, bool inplace, double* partials, Launch, cudaStream_t);
   // in-place FAST step with the learned closure (engine 0/1, mode 0/1/2 of
-  // k_step_closure); null for the fp64 judge
+  // k_step_closure); null for the fp64 reference form
   cudaError_t (*step_closure)(const Dev&, const Params&, int parity, bool mac, bool frc, int engine, int mode,
-                              const CloArgs&, cudaStream_t);
+                              const CloArgs&, Launch, cudaStream_t);
   int elem_bytes;
 };
 
 template <class St>
 struct OpsImpl {
   using R = typename St::real;
-  // The fp64 judge is always STRICT.
+  // The fp64 reference form is always STRICT.
   static constexpr bool kFastOK = sizeof(R) == 4;
   template <int PAR, bool MAC, bool FRC, bool FAST>
   static void go_inplace(const Dev& d, const Params& P, const Uni<R>& U, Launch L, cudaStream_t s) {
@@ -888,10 +889,13 @@ struct OpsImpl {
     return cudaGetLastError();
   }
   template <int PAR, bool MAC, bool FRC, int ENG, int MODE>
-  static void go_closure(const Dev& d, const Params& P, const Uni<float>& U, const CloArgs& A, cudaStream_t s) {
+  static void go_closure(const Dev& d, const Params& P, const Uni<float>& U, const CloArgs& A, Launch L,
+                         cudaStream_t s) {
     if constexpr (sizeof(R) == 4) {
-      // 64 x 2 threads: four warps, one 128-row MMA tile per block for engine 1
-      const dim3 block(64, 2), grid((d.nx + 63) / 64, (d.ny + 1) / 2, d.nz);
+      // network steps: 64 x 2 threads, four warps (one 128-row MMA tile for
+      // engine 1); held steps: the plain step's launch shape
+      dim3 block(64, 2), grid((d.nx + 63) / 64, (d.ny + 1) / 2, d.nz);
+      if (MODE == 2) { block = L.block; grid = L.grid; }
       if ((int64_t)Q * d.N >= (int64_t)INT32_MAX)
         k_step_closure<St, PAR, MAC, FRC, true, ENG, MODE><<<grid, block, 0, s>>>(d, P, U, A);
       else
@@ -900,21 +904,21 @@ struct OpsImpl {
   }
   template <int PAR, bool MAC, bool FRC>
   static void go_closure_m(const Dev& d, const Params& P, const Uni<float>& U, int engine, int mode,
-                           const CloArgs& A, cudaStream_t s) {
-    if (mode == 2) go_closure<PAR, MAC, FRC, 0, 2>(d, P, U, A, s);
-    else if (engine == 0) { mode == 1 ? go_closure<PAR, MAC, FRC, 0, 1>(d, P, U, A, s) : go_closure<PAR, MAC, FRC, 0, 0>(d, P, U, A, s); }
-    else { mode == 1 ? go_closure<PAR, MAC, FRC, 1, 1>(d, P, U, A, s) : go_closure<PAR, MAC, FRC, 1, 0>(d, P, U, A, s); }
+                           const CloArgs& A, Launch L, cudaStream_t s) {
+    if (mode == 2) go_closure<PAR, MAC, FRC, 0, 2>(d, P, U, A, L, s);
+    else if (engine == 0) { mode == 1 ? go_closure<PAR, MAC, FRC, 0, 1>(d, P, U, A, L, s) : go_closure<PAR, MAC, FRC, 0, 0>(d, P, U, A, L, s); }
+    else { mode == 1 ? go_closure<PAR, MAC, FRC, 1, 1>(d, P, U, A, L, s) : go_closure<PAR, MAC, FRC, 1, 0>(d, P, U, A, L, s); }
   }
   static cudaError_t step_closure(const Dev& d, const Params& P, int parity, bool mac, bool frc, int engine,
-                                  int mode, const CloArgs& A, cudaStream_t s) {
+                                  int mode, const CloArgs& A, Launch L, cudaStream_t s) {
     if constexpr (sizeof(R) == 4) {
       const Uni<float> U = make_uni<float>(P);
       if (parity == 0) {
-        if (mac) { frc ? go_closure_m<0, true, true>(d, P, U, engine, mode, A, s) : go_closure_m<0, true, false>(d, P, U, engine, mode, A, s); }
-        else { frc ? go_closure_m<0, false, true>(d, P, U, engine, mode, A, s) : go_closure_m<0, false, false>(d, P, U, engine, mode, A, s); }
+        if (mac) { frc ? go_closure_m<0, true, true>(d, P, U, engine, mode, A, L, s) : go_closure_m<0, true, false>(d, P, U, engine, mode, A, L, s); }
+        else { frc ? go_closure_m<0, false, true>(d, P, U, engine, mode, A, L, s) : go_closure_m<0, false, false>(d, P, U, engine, mode, A, L, s); }
       } else {
-        if (mac) { frc ? go_closure_m<1, true, true>(d, P, U, engine, mode, A, s) : go_closure_m<1, true, false>(d, P, U, engine, mode, A, s); }
-        else { frc ? go_closure_m<1, false, true>(d, P, U, engine, mode, A, s) : go_closure_m<1, false, false>(d, P, U, engine, mode, A, s); }
+        if (mac) { frc ? go_closure_m<1, true, true>(d, P, U, engine, mode, A, L, s) : go_closure_m<1, true, false>(d, P, U, engine, mode, A, L, s); }
+        else { frc ? go_closure_m<1, false, true>(d, P, U, engine, mode, A, L, s) : go_closure_m<1, false, false>(d, P, U, engine, mode, A, L, s); }
       }
       return cudaGetLastError();
     }

@@ -10,7 +10,7 @@ voxelized on the GPU and centred vertically, free-slip walls on every side
 (the sphere case's tunnel, tests/validacao.html:224-231), u_in 0.05,
 nu 0.008 (omega+ 1.9084), Smagorinsky Cs 0.1.  The same run in four storage
 forms: fp32, fp16 of g*2^10, bf16 — all with fp32 arithmetic — and the fp64
-judge (fp64 storage and arithmetic).  Reported per form: MLUPS and fraction of
+fp64 reference form (fp64 storage and arithmetic).  Reported per form: MLUPS and fraction of
 the HBM roofline (bytes per cell 152 / 76 / 76 / 304), the drag coefficient
 averaged over the last quarter of the run (Maskell-corrected, theta 2.5) and
 its error against the fp64 run, and the relative L2 error of the velocity

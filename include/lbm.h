@@ -66,7 +66,7 @@ extern "C" {
 #define LBM_F32    0   /* fp32 g_i (152 B/cell/step) */
 #define LBM_F16S   1   /* fp16 of g_i * 2^10, fp32 arithmetic (76 B/cell/step) */
 #define LBM_BF16S  2   /* bf16 of g_i, fp32 arithmetic (76 B/cell/step) */
-#define LBM_F64    3   /* fp64 g_i and fp64 arithmetic: the accuracy judge */
+#define LBM_F64    3   /* fp64 g_i and fp64 arithmetic: the accuracy reference */
 
 /* lbm_create flags */
 #define LBM_FLAG_WRITE_MACROS  1  /* the last step of each lbm_step writes (u, delta) */

@@ -68,7 +68,7 @@ static const float SIXW_f[ORC_Q] = {
     0.166666667f, 0.166666667f, 0.166666667f, 0.166666667f, 0.166666667f, 0.166666667f,
     0.166666667f, 0.166666667f, 0.166666667f, 0.166666667f, 0.166666667f, 0.166666667f,
 };
-/* fp64 judge: the exact rationals rounded once to double */
+/* fp64 reference form: the exact rationals rounded once to double */
 static double W_d[ORC_Q];
 static double SIXW_d[ORC_Q];
 
@@ -174,7 +174,7 @@ static inline int orc_is_solid(uint32_t t) {
 #undef ORC_POW
 #undef ORC_FMA
 
-/* ---- fp64 instantiation (the accuracy judge) ---- */
+/* ---- fp64 instantiation (the accuracy reference) ---- */
 #define REAL double
 #define SFX _f64
 #define ORC_IS_FLOAT 0

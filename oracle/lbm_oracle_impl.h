@@ -81,7 +81,7 @@ static inline void FN(orc_equilibrium_fast)(REAL delta, REAL rho, REAL ux, REAL 
 void FN(orc_step)(const orc_params* P, int nx, int ny, int nz, const uint32_t* tipo,
                   const REAL* src, REAL* dst, float* macros, int storage, int nthreads, int fast_in) {
   /* FAST restatement: fixed fused multiply-adds (ORC_FMA), u = m (1/rho),
-   * omega- = (tau - 1/2) / (Lambda + (tau - 1/2)/2).  The fp64 judge is
+   * omega- = (tau - 1/2) / (Lambda + (tau - 1/2)/2).  The fp64 reference form is
    * always STRICT. */
   const int fast = ORC_IS_FLOAT ? fast_in : 0;
   const int64_t N = (int64_t)nx * ny * nz;

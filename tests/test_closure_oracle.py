@@ -92,3 +92,36 @@ def test_abi_struct_sizes():
     assert C.sizeof(nat.ClosureWeights) == 4 * (1313 + 27)
     assert C.sizeof(nat.ClosureCfg) == 40
     assert nat.ClosureCfg.seed.offset == 24
+
+
+def test_weights_round_trip_and_scaling(tmp_path):
+    from cfd__gb300 import fecho
+    rng = np.random.default_rng(9)
+    p = fecho.pesos_vazios()
+    p["w2"] = rng.normal(0, 1, (32, 32)).astype(np.float32)
+    p["b3"] = np.float32(-0.5)
+    f = rng.normal(0, 1, (5000, 6)).astype(np.float32)
+    t = np.where(rng.random(5000) < 0.3, 0.0, rng.lognormal(-8, 1, 5000)).astype(np.float32)
+    n = fecho.normalizacao(f, t)
+    p.update(n)
+    p["coef"] = 1
+    assert (n["lo"] < n["hi"]).all() and n["nu_scale"] > 0 and n["nu_max"] > n["nu_scale"]
+    # the struct the C ABI sees holds the same numbers
+    q = fecho.de_struct(fecho.para_struct(p))
+    assert np.array_equal(fecho.vetor(q), fecho.vetor(p)) and q["coef"] == 1
+    path = tmp_path / "w.npz"
+    fecho.salvar(p, path)
+    r = fecho.carregar(path)
+    assert np.array_equal(fecho.vetor(r), fecho.vetor(p))
+    for k in ("mean", "std", "lo", "hi"):
+        assert np.array_equal(r[k], p[k])
+    assert r["coef"] == 1 and r["nu_scale"] == p["nu_scale"]
+
+
+def test_committed_weights_load():
+    import os
+
+    from cfd__gb300 import fecho
+    p = fecho.carregar(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "cfd__gb300",
+                                    "pesos", "fecho_coef.npz"))
+    assert p["coef"] == 1 and np.isfinite(fecho.vetor(p)).all() and p["std"][0] > 1e20

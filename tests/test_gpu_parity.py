@@ -1,9 +1,9 @@
 """CUDA step vs the CPU oracle on identical inputs.
 
 fp32: bit-exact (the kernels are built with -fmad=false and IEEE div/sqrt and
-follow the shader's operation order).  The same holds for the fp64 judge and
+follow the shader's operation order).  The same holds for the fp64 reference form and
 for the 16-bit storage forms, whose rounding the oracle reproduces.  The
-spec bar (fp32 populations within 1e-5 relative after 1000 steps) is
+parity bar for this path (fp32 populations within 1e-5 relative after 1000 steps) is
 therefore met with margin; tests assert equality.
 Solid cells carry no state in the reference (nothing reads them), so
 population comparisons cover the non-solid cells.
