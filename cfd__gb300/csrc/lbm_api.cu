@@ -122,6 +122,8 @@ struct lbm_ctx {
   double* fbuf = nullptr;      // per-step fused forces
   int64_t fbuf_cap = 0;        // in steps
   double* stage = nullptr;     // N doubles for set/get
+  double* hpin = nullptr;      // pinned host staging for force read-backs
+  int64_t hpin_cap = 0;        // in doubles
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   Params P{};
@@ -223,6 +225,22 @@ int ensure_stage(lbm_ctx* c) {
 
 int parity(const lbm_ctx* c) { return c->inplace ? (int)(c->steps & 1) : 0; }
 
+// Pinned host staging of at least n doubles: a device-to-host copy into
+// pinned memory is a plain DMA, without the driver's pageable bounce buffer.
+int ensure_pinned(lbm_ctx* c, int64_t n) {
+  if (c->hpin_cap >= n) return LBM_OK;
+  if (c->hpin) { cudaFreeHost(c->hpin); c->hpin = nullptr; c->hpin_cap = 0; }
+  const int64_t cap = std::max<int64_t>(n, 64);
+  cudaError_t e = cudaHostAlloc((void**)&c->hpin, sizeof(double) * (size_t)cap, cudaHostAllocDefault);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    c->hpin = nullptr;
+    return fail(LBM_ENOMEM, std::string("pinned host staging: ") + cudaGetErrorString(e));
+  }
+  c->hpin_cap = cap;
+  return LBM_OK;
+}
+
 int check_ready(lbm_ctx* c, bool need_cfg) {
   if (!c) return fail(LBM_EINVAL, "null context");
   if (!c->types_set) return fail(LBM_ESTATE, "cell types not set (call lbm_set_types first)");
@@ -323,6 +341,7 @@ int lbm_destroy(lbm_ctx* c) {
   for (void* p : ps)
     if (p) cudaFree(p);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  if (c->hpin) cudaFreeHost(c->hpin);
   delete c;
   return LBM_OK;
 }
@@ -442,20 +461,29 @@ int lbm_step_forces(lbm_ctx* c, int n, double* out_f) {
   if (n == 0) return LBM_OK;
   const bool want_mac = (c->flags & LBM_FLAG_WRITE_MACROS) != 0;
   if (want_mac && (r = ensure_macros(c))) return r;
+  const size_t per = 3 * (size_t)kForceSlots;   // doubles per step
   if (c->fbuf_cap < n) {
-    if (c->fbuf) { cudaFree(c->fbuf); c->dev_bytes -= 3 * sizeof(double) * c->fbuf_cap; c->fbuf = nullptr; c->fbuf_cap = 0; }
-    r = dalloc(c, (void**)&c->fbuf, 3 * sizeof(double) * (size_t)n, "per-step forces");
+    if (c->fbuf) { cudaFree(c->fbuf); c->dev_bytes -= sizeof(double) * per * c->fbuf_cap; c->fbuf = nullptr; c->fbuf_cap = 0; }
+    r = dalloc(c, (void**)&c->fbuf, sizeof(double) * per * (size_t)n, "per-step forces");
     if (r) return r;
     c->fbuf_cap = n;
   }
-  CK(cudaMemsetAsync(c->fbuf, 0, 3 * sizeof(double) * (size_t)n, c->stream), "force buffer clear");
+  CK(cudaMemsetAsync(c->fbuf, 0, sizeof(double) * per * (size_t)n, c->stream), "force buffer clear");
   for (int k = 0; k < n; ++k) {
-    r = launch_step(c, want_mac && k == n - 1, c->fbuf + 3 * (size_t)k);
+    r = launch_step(c, want_mac && k == n - 1, c->fbuf + per * (size_t)k);
     if (r) return r;
   }
-  CK(cudaMemcpyAsync(out_f, c->fbuf, 3 * sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, c->stream),
+  if ((r = ensure_pinned(c, (int64_t)(per * (size_t)n)))) return r;
+  CK(cudaMemcpyAsync(c->hpin, c->fbuf, sizeof(double) * per * (size_t)n, cudaMemcpyDeviceToHost, c->stream),
      "force download");
   CK(cudaStreamSynchronize(c->stream), "force download sync");
+  for (int k = 0; k < n; ++k) {
+    const double* h = c->hpin + per * (size_t)k;
+    double f[3] = {0.0, 0.0, 0.0};
+    for (int q = 0; q < kForceSlots; ++q)
+      for (int a = 0; a < 3; ++a) f[a] += h[3 * q + a];
+    for (int a = 0; a < 3; ++a) out_f[3 * (size_t)k + a] = f[a];
+  }
   return LBM_OK;
 }
 
@@ -488,8 +516,10 @@ int lbm_forces(lbm_ctx* c, double f[3]) {
   CK(c->ops.forces(dev_of(c), parity(c), c->inplace, c->partials, L, c->stream), "force kernel launch");
   k_reduce3<<<1, 256, 0, c->stream>>>(c->partials, nb, c->red);
   CK(cudaGetLastError(), "reduce kernel launch");
-  CK(cudaMemcpyAsync(f, c->red, 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "force download");
+  if ((r = ensure_pinned(c, 3))) return r;
+  CK(cudaMemcpyAsync(c->hpin, c->red, 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream), "force download");
   CK(cudaStreamSynchronize(c->stream), "force sync");
+  memcpy(f, c->hpin, 3 * sizeof(double));
   return LBM_OK;
 }
 

@@ -38,7 +38,7 @@ struct Dev {
   const uint8_t* tipo;   // cell classes
   const uint32_t* link;  // link words (in-place layout)
   float4* macros;        // nullable
-  double* force;         // nullable: 3 doubles accumulated by the fused force
+  double* force;         // nullable: kForceSlots x 3 doubles accumulated by the fused force
 };
 
 struct Wrap {
@@ -78,6 +78,12 @@ __device__ __forceinline__ int64_t eso_loc(int k, int p, int64_t cell, int x, in
 }
 
 // Warp-level fp64 sum of three values; lane 0 adds them to dst atomically.
+// The fused force of one step accumulates into kForceSlots copies of
+// (fx, fy, fz), the block row picking the copy, so that the few thousand warps
+// that touch the body do not all serialise on the same three addresses; the
+// host sums the copies.
+constexpr int kForceSlots = 32;
+
 __device__ __forceinline__ void warp_add3(double a, double b, double c, double* dst) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -86,9 +92,10 @@ __device__ __forceinline__ void warp_add3(double a, double b, double c, double* 
     c += __shfl_xor_sync(0xffffffffu, c, o);
   }
   if ((threadIdx.x & 31) == 0) {
-    atomicAdd(dst + 0, a);
-    atomicAdd(dst + 1, b);
-    atomicAdd(dst + 2, c);
+    double* slot = dst + 3 * ((blockIdx.y + blockIdx.z * gridDim.y) & (kForceSlots - 1));
+    atomicAdd(slot + 0, a);
+    atomicAdd(slot + 1, b);
+    atomicAdd(slot + 2, c);
   }
 }
 
@@ -132,9 +139,13 @@ struct Deltas {
 // One cell of the in-place step (everything the step does for cell x, y, z).
 // Shared by the single-tunnel kernel and the batched kernel, so both run
 // the identical arithmetic.
+// FRC: the cell's momentum-exchange force is parked in shared memory
+// (park[0][t], park[1][t], park[2][t], volatile so it is not kept in
+// registers through the collide) for the warp reduction at the kernel's end.
 template <class St, int PAR, bool MAC, bool FRC, bool W64, bool FAST>
 __device__ __forceinline__ void step_cell(const Dev& d, const Params& P, const Uni<typename St::real>& U, int x, int y,
-                                          int z, double& fx, double& fy, double& fz) {
+                                          int z, volatile double (*park)[128], int t) {
+  double fx = 0.0, fy = 0.0, fz = 0.0;
   using R = typename St::real;
   using S = typename St::store_t;
   using Off = typename OffT<W64>::type;
@@ -195,6 +206,7 @@ __device__ __forceinline__ void step_cell(const Dev& d, const Params& P, const U
           }
         }
       }
+      if (FRC) { park[0][t] = fx; park[1][t] = fy; park[2][t] = fz; }
       R delta, rho, ux, uy, uz, uu, rinv = R(0.0);
       R sp[9], dp[9];
       if (FAST) moments_fast<R>(g, sp, dp, delta, rho, ux, uy, uz, uu, rinv);
@@ -216,16 +228,21 @@ __device__ __forceinline__ void step_cell(const Dev& d, const Params& P, const U
 }
 
 // MINB: minimum resident 128-thread blocks per SM the register allocation
-// must allow (8 -> 64 registers, 6 -> 80); the autotuner picks per form.
+// must allow (8 -> 64 registers, 6 -> 80); the autotuner picks per form.  The
+// fused force parks in shared memory, so the force variant fits 64 too.
 template <class St, int PAR, bool MAC, bool FRC, bool W64, bool FAST, int MINB>
 __global__ void __launch_bounds__(128, MINB)
 k_step_inplace(Dev d, Params P, Uni<typename St::real> U) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int z = blockIdx.z;
-  double fx = 0.0, fy = 0.0, fz = 0.0;
-  if (x < d.nx && y < d.ny) step_cell<St, PAR, MAC, FRC, W64, FAST>(d, P, U, x, y, z, fx, fy, fz);
+  __shared__ double park[FRC ? 3 : 1][128];     // blocks have at most 128 threads
+  const int t = threadIdx.y * blockDim.x + threadIdx.x;
+  if (FRC) { park[0][t] = 0.0; park[1][t] = 0.0; park[2][t] = 0.0; }
+  if (x < d.nx && y < d.ny) step_cell<St, PAR, MAC, FRC, W64, FAST>(d, P, U, x, y, z, park, t);
   if (FRC) {
+    const volatile double (*pk)[128] = park;
+    const double fx = pk[0][t], fy = pk[1][t], fz = pk[2][t];
     const bool any = __any_sync(0xffffffffu, fx != 0.0 || fy != 0.0 || fz != 0.0);
     if (any) warp_add3(fx, fy, fz, d.force);
   }
@@ -815,7 +832,7 @@ struct OpsImpl {
   static constexpr bool kFastOK = sizeof(R) == 4;
   template <int PAR, bool MAC, bool FRC, bool FAST>
   static void go_inplace(const Dev& d, const Params& P, const Uni<R>& U, Launch L, cudaStream_t s) {
-    constexpr int kDefault = sizeof(R) == 8 ? 4 : ((FRC || MAC) ? 6 : 8);
+    constexpr int kDefault = sizeof(R) == 8 ? 4 : (MAC ? 6 : 8);
     const bool w64 = (int64_t)Q * d.N >= (int64_t)INT32_MAX;
     if constexpr (!MAC && !FRC && sizeof(typename St::store_t) <= 4) {
       if (L.pipe > 0 && !w64) {
