@@ -121,6 +121,11 @@ SIGNATURES = {
                                   C.c_size_t]),
     "lbm_set_closure": (C.c_int, [C.c_void_p, C.POINTER(ClosureWeights)]),
     "lbm_closure_stats": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
+    "lbm_state_bytes": (C.c_int, [C.c_void_p, C.POINTER(C.c_size_t)]),
+    "lbm_save_state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    "lbm_load_state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    "lbm_read_macros_async": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    "lbm_macros_ready": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "vox_voxelize": (C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.POINTER(Dims), C.c_float, C.c_int,
                                C.c_void_p, C.c_void_p, C.POINTER(VoxStats)]),
 }

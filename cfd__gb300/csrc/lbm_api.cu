@@ -14,6 +14,7 @@
 
 #include "../../include/lbm.h"
 #include "../../include/lbm_closure.h"
+#include "../../include/lbm_state.h"
 #include "lbm_kernels.cuh"
 
 using namespace lbm;
@@ -123,6 +124,7 @@ struct lbm_ctx {
   int64_t fbuf_cap = 0;        // in steps
   double* stage = nullptr;     // N doubles for set/get
   double* hpin = nullptr;      // pinned host staging for force read-backs
+  cudaEvent_t mac_evt = nullptr;   // completion of the last asynchronous macros read-back
   int64_t hpin_cap = 0;        // in doubles
   cudaStream_t stream = nullptr;
   bool own_stream = false;
@@ -342,6 +344,7 @@ int lbm_destroy(lbm_ctx* c) {
     if (p) cudaFree(p);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   if (c->hpin) cudaFreeHost(c->hpin);
+  if (c->mac_evt) cudaEventDestroy(c->mac_evt);
   delete c;
   return LBM_OK;
 }
@@ -538,6 +541,85 @@ int lbm_mass(lbm_ctx* c, double* sum) {
   CK(cudaStreamSynchronize(c->stream), "mass sync");
   *sum = out[0];
   return LBM_OK;
+}
+
+static_assert(sizeof(lbm_state_header) == 48, "lbm_state_header layout");
+
+int lbm_state_bytes(lbm_ctx* c, size_t* bytes) {
+  if (!c || !bytes) return fail(LBM_EINVAL, "null argument");
+  *bytes = sizeof(lbm_state_header) + (size_t)Q * (size_t)c->N * (size_t)c->ops.elem_bytes;
+  return LBM_OK;
+}
+
+int lbm_save_state(lbm_ctx* c, void* dst, size_t bytes) {
+  if (!c || !dst) return fail(LBM_EINVAL, "null argument");
+  int r = check_ready(c, false);
+  if (r) return r;
+  if (!c->state_set) return fail(LBM_ESTATE, "no state yet (initialise or set populations first)");
+  size_t need = 0;
+  lbm_state_bytes(c, &need);
+  if (bytes < need) return fail(LBM_EINVAL, "checkpoint buffer too small (see lbm_state_bytes)");
+  lbm_state_header h;
+  memset(&h, 0, sizeof h);
+  h.magic = LBM_STATE_MAGIC;
+  h.version = LBM_STATE_VERSION;
+  h.nx = c->dims.nx; h.ny = c->dims.ny; h.nz = c->dims.nz;
+  h.storage = c->storage;
+  h.layout = c->inplace ? 0 : 1;
+  h.parity = parity(c);
+  h.steps = c->steps;
+  h.payload_bytes = need - sizeof h;
+  memcpy(dst, &h, sizeof h);
+  CK(cudaMemcpyAsync(static_cast<char*>(dst) + sizeof h, c->pop, h.payload_bytes, cudaMemcpyDeviceToHost, c->stream),
+     "state download");
+  CK(cudaStreamSynchronize(c->stream), "state download sync");
+  return LBM_OK;
+}
+
+int lbm_load_state(lbm_ctx* c, const void* src, size_t bytes) {
+  if (!c || !src) return fail(LBM_EINVAL, "null argument");
+  if (bytes < sizeof(lbm_state_header)) return fail(LBM_EINVAL, "checkpoint shorter than its header");
+  lbm_state_header h;
+  memcpy(&h, src, sizeof h);
+  if (h.magic != LBM_STATE_MAGIC || h.version != LBM_STATE_VERSION) return fail(LBM_EINVAL, "not a checkpoint of this library");
+  size_t need = 0;
+  lbm_state_bytes(c, &need);
+  if (h.nx != c->dims.nx || h.ny != c->dims.ny || h.nz != c->dims.nz)
+    return fail(LBM_EINVAL, "checkpoint grid differs from the context's");
+  if (h.storage != c->storage) return fail(LBM_EINVAL, "checkpoint storage form differs from the context's");
+  if (h.layout != (c->inplace ? 0 : 1)) return fail(LBM_EINVAL, "checkpoint layout differs from the context's");
+  if (h.payload_bytes + sizeof h != need || bytes < need) return fail(LBM_EINVAL, "checkpoint size does not match");
+  if (c->inplace && h.parity != (int)(h.steps & 1)) return fail(LBM_EINVAL, "checkpoint parity and step count disagree");
+  CK(cudaMemcpyAsync(c->pop, static_cast<const char*>(src) + sizeof h, h.payload_bytes, cudaMemcpyHostToDevice, c->stream),
+     "state upload");
+  CK(cudaStreamSynchronize(c->stream), "state upload sync");
+  c->steps = h.steps;
+  c->clo_since = -1;
+  c->state_set = true;
+  return LBM_OK;
+}
+
+int lbm_read_macros_async(lbm_ctx* c, float* out, size_t n) {
+  if (!c || !out) return fail(LBM_EINVAL, "null argument");
+  if ((int64_t)n != 4 * c->N) return fail(LBM_EINVAL, "macros array must hold 4*N floats");
+  int r = check_ready(c, false);
+  if (r) return r;
+  if ((r = ensure_macros(c))) return r;
+  if (!c->mac_evt) CK(cudaEventCreateWithFlags(&c->mac_evt, cudaEventDisableTiming), "event create");
+  CK(c->ops.macros(dev_of(c), parity(c), c->inplace, cell_launch(c), c->stream), "macros kernel launch");
+  CK(cudaMemcpyAsync(out, c->macros, sizeof(float4) * (size_t)c->N, cudaMemcpyDeviceToHost, c->stream),
+     "macros download");
+  CK(cudaEventRecord(c->mac_evt, c->stream), "event record");
+  return LBM_OK;
+}
+
+int lbm_macros_ready(lbm_ctx* c, int* ready) {
+  if (!c || !ready) return fail(LBM_EINVAL, "null argument");
+  if (!c->mac_evt) { *ready = 1; return LBM_OK; }
+  const cudaError_t e = cudaEventQuery(c->mac_evt);
+  if (e == cudaSuccess) { *ready = 1; return LBM_OK; }
+  if (e == cudaErrorNotReady) { cudaGetLastError(); *ready = 0; return LBM_OK; }
+  return cuda_fail(e, "macros read-back");
 }
 
 int lbm_sync(lbm_ctx* c) {

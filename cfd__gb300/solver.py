@@ -231,6 +231,37 @@ class SolverCUDA:
         register-cap variant (min resident blocks per SM: 8 or 6; 0 = default)."""
         nat.check(self._lib.lbm_set_launch(self._h, int(block_x), int(min_blocos)))
 
+    # --------------------------------------------------------------- state I/O
+    def salvarEstado(self) -> bytes:
+        """Checkpoint of the population set (include/lbm_state.h)."""
+        n = C.c_size_t()
+        nat.check(self._lib.lbm_state_bytes(self._h, C.byref(n)))
+        buf = np.empty(n.value, np.uint8)
+        nat.check(self._lib.lbm_save_state(self._h, nat.ptr(buf), n.value))
+        return buf.tobytes()
+
+    def carregarEstado(self, blob: bytes):
+        """Restore a checkpoint taken by salvarEstado on a solver of the same
+        grid, storage form and layout; the step count comes with it."""
+        buf = np.frombuffer(blob, np.uint8)
+        nat.check(self._lib.lbm_load_state(self._h, nat.ptr(buf), buf.size))
+        self.passos = int(np.frombuffer(blob[32:40], np.int64)[0])
+
+    def lerMacrosAssincrono(self, destino=None):
+        """Start a macros read-back into destino (4*N float32, kept alive by the
+        caller; page-locked memory lets it overlap) and return it at once;
+        macrosProntos() tells when it has landed."""
+        if destino is None:
+            destino = np.empty(4 * self.N, np.float32)
+        self._macros_async = destino
+        nat.check(self._lib.lbm_read_macros_async(self._h, nat.ptr(destino), destino.size))
+        return destino
+
+    def macrosProntos(self) -> bool:
+        r = C.c_int()
+        nat.check(self._lib.lbm_macros_ready(self._h, C.byref(r)))
+        return bool(r.value)
+
     def definirFecho(self, pesos):
         """Network of the learned closure (cfd__gb300.fecho weights dict);
         configurar(closure=1) then selects it."""
