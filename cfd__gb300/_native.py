@@ -126,6 +126,17 @@ SIGNATURES = {
     "lbm_load_state": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "lbm_read_macros_async": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "lbm_macros_ready": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "vis_fumaca_create": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
+    "vis_fumaca_destroy": (C.c_int, [C.c_void_p]),
+    "vis_fumaca_limpar": (C.c_int, [C.c_void_p]),
+    "vis_fumaca_passo": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "vis_fumaca_ler": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    "vis_fumaca_definir": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    "vis_esteiras_create": (C.c_int, [C.c_void_p, C.c_size_t, C.POINTER(C.c_void_p)]),
+    "vis_esteiras_destroy": (C.c_int, [C.c_void_p]),
+    "vis_esteiras_definir": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    "vis_esteiras_ler": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
+    "vis_esteiras_passo": (C.c_int, [C.c_void_p, C.c_float, C.c_int, C.c_uint32]),
     "vox_voxelize": (C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.POINTER(Dims), C.c_float, C.c_int,
                                C.c_void_p, C.c_void_p, C.POINTER(VoxStats)]),
 }

@@ -39,6 +39,7 @@ UNITS = {
     "lbm_noalloc.cu": ["-fmad=false"],
     "lbm_batch.cu": ["-fmad=false"],
     "closure.cu": ["-fmad=false"],
+    "vis.cu": ["-fmad=false"],
 }
 
 

@@ -622,6 +622,26 @@ int lbm_macros_ready(lbm_ctx* c, int* ready) {
   return cuda_fail(e, "macros read-back");
 }
 
+}  // extern "C"
+
+namespace lbm {
+// Device view of a context for the other units of the library (visualisation).
+int ctx_view(lbm_ctx* c, CtxView* v) {
+  if (!c || !v) return fail(LBM_EINVAL, "null argument");
+  int r = check_ready(c, false);
+  if (r) return r;
+  if ((r = ensure_macros(c))) return r;
+  v->nx = c->dims.nx; v->ny = c->dims.ny; v->nz = c->dims.nz;
+  v->N = c->N;
+  v->macros = c->macros;
+  v->tipo = c->tipo;
+  v->stream = c->stream;
+  return LBM_OK;
+}
+}  // namespace lbm
+
+extern "C" {
+
 int lbm_sync(lbm_ctx* c) {
   if (!c) return fail(LBM_EINVAL, "null context");
   CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");

@@ -27,6 +27,8 @@
 #include "closure_mlp.cuh"
 #include "lbm_core.cuh"
 
+struct lbm_ctx;   // include/lbm.h
+
 namespace lbm {
 
 // Device-side view of one context's buffers.
@@ -950,6 +952,16 @@ struct OpsImpl {
     return o;
   }
 };
+
+// What other units of the library see of a context.
+struct CtxView {
+  int nx, ny, nz;
+  int64_t N;
+  float4* macros;
+  const uint8_t* tipo;
+  cudaStream_t stream;
+};
+int ctx_view(::lbm_ctx* c, CtxView* v);   // lbm_api.cu; makes sure the macros buffer exists
 
 Ops ops_f32();
 Ops ops_f64();

@@ -1,0 +1,86 @@
+/*
+ * lbm_vis.h — the visualisation compute of the wind tunnel as CUDA kernels on
+ * headless device buffers, reading a solver context's macros field
+ * (ux, uy, uz, delta per cell) and cell types.
+ *
+ * The reference runs these as WebGPU compute passes inside its renderer; the
+ * arithmetic is restated here without a graphics API:
+ *
+ *  - smoke: a passive density field advected by the flow, one step =
+ *    semi-Lagrangian back-trace (pass `recuar`, src/render/fumaca.js:147-160)
+ *    then the MacCormack correction with the eight-corner limiter, the
+ *    dissipation, the domain cut-off and the rake emission (pass `corrigir`,
+ *    src/render/fumaca.js:186-218; rake src/render/fumaca.js:96-132).  The
+ *    density is stored as fp16, as the reference's rgba16float volume is;
+ *    density samples are trilinear with clamp-to-edge, evaluated exactly in
+ *    fp32 (the reference leaves that to the texture unit).
+ *  - streak particles: Euler sub-steps through the nearest-cell velocity,
+ *    ageing and the hashed respawn (src/render/renderer.js:50-117).
+ *
+ * Both read ctx's macros buffer as it is: it is current after a step with
+ * LBM_FLAG_WRITE_MACROS or after lbm_update_macros.
+ */
+#ifndef CFD_GB300_LBM_VIS_H
+#define CFD_GB300_LBM_VIS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "lbm.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Rake (src/render/fumaca.js:62-67, :583-590): the emission plane x, the
+ * filament spacing along y and z, the filament radius, and the y / z extent. */
+typedef struct {
+  float x, passo_y, passo_z, raio;
+  float y0, y1, z0, z1;
+} vis_rake;
+
+/* One advection step's parameters (src/render/fumaca.js:603-615): dt in
+ * lattice steps, dissipation per step, injected density, and the advance in
+ * cells this step stands for (dt * 0.05 in the reference). */
+typedef struct {
+  float dt, dissipacao, taxa, avanco;
+} vis_fumo;
+
+typedef struct vis_fumaca vis_fumaca;
+
+/* Three fp16 volumes of the context's grid (current, next, intermediate),
+ * zeroed. */
+int vis_fumaca_create(lbm_ctx* ctx, vis_fumaca** out);
+int vis_fumaca_destroy(vis_fumaca* f);
+int vis_fumaca_limpar(vis_fumaca* f);
+
+/* One smoke step on the context's stream. */
+int vis_fumaca_passo(vis_fumaca* f, const vis_rake* rake, const vis_fumo* params);
+
+/* Current density as fp16 bit patterns (n = N), read or written; both
+ * synchronise. */
+int vis_fumaca_ler(vis_fumaca* f, uint16_t* out, size_t n);
+int vis_fumaca_definir(vis_fumaca* f, const uint16_t* in, size_t n);
+
+/* Streak particles (src/render/renderer.js:51): pos = (x, y, z, life),
+ * ant = (previous x, y, z, 1 when a trace is drawn / 0 on respawn). */
+typedef struct {
+  float pos[4];
+  float ant[4];
+} vis_part;
+
+typedef struct vis_esteiras vis_esteiras;
+
+int vis_esteiras_create(lbm_ctx* ctx, size_t n, vis_esteiras** out);
+int vis_esteiras_destroy(vis_esteiras* e);
+int vis_esteiras_definir(vis_esteiras* e, const vis_part* in, size_t n);
+int vis_esteiras_ler(vis_esteiras* e, vis_part* out, size_t n);
+
+/* One frame: nsub Euler sub-steps of dt_quadro / nsub each through the
+ * nearest-cell velocity; `quadro` seeds the respawn hash. */
+int vis_esteiras_passo(vis_esteiras* e, float dt_quadro, int nsub, uint32_t quadro);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CFD_GB300_LBM_VIS_H */

@@ -1,0 +1,146 @@
+"""CPU restatement of the visualisation compute (include/lbm_vis.h) — TEST
+INFRASTRUCTURE ONLY: tests/ use it as the checker for cfd__gb300/csrc/vis.cu.
+Nothing in the product imports it.
+
+numpy float32, each operation rounded as written (the kernels are built with
+-fmad=false), density volumes in float16 as the reference's rgba16float
+volume:
+  * fumaca_passo   one smoke step: back-trace (src/render/fumaca.js:147-160),
+                   MacCormack correction with the eight-corner limiter,
+                   dissipation, domain cut-off and rake (:96-132, :186-218);
+                   trilinear samples with clamp-to-edge at t = p - 0.5,
+                   interpolated along x, y, z as a + f (b - a);
+  * esteiras_passo one frame of the streak particles
+                   (src/render/renderer.js:51-116), with its integer hash.
+exp() of the rake may differ from the GPU's expf in the last place; tests
+allow for that where the rake is active.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+f32 = np.float32
+
+
+def _sample(vol, ax, ay, az):
+    nz, ny, nx = vol.shape
+    v = vol.astype(np.float32)
+    tx, ty, tz = ax - f32(0.5), ay - f32(0.5), az - f32(0.5)
+    bx, by, bz = np.floor(tx), np.floor(ty), np.floor(tz)
+    fx, fy, fz = tx - bx, ty - by, tz - bz
+    x0 = np.clip(bx.astype(np.int64), 0, nx - 1); x1 = np.clip(bx.astype(np.int64) + 1, 0, nx - 1)
+    y0 = np.clip(by.astype(np.int64), 0, ny - 1); y1 = np.clip(by.astype(np.int64) + 1, 0, ny - 1)
+    z0 = np.clip(bz.astype(np.int64), 0, nz - 1); z1 = np.clip(bz.astype(np.int64) + 1, 0, nz - 1)
+
+    def lerp(a, b, f):
+        return a + f * (b - a)
+    c00 = lerp(v[z0, y0, x0], v[z0, y0, x1], fx)
+    c10 = lerp(v[z0, y1, x0], v[z0, y1, x1], fx)
+    c01 = lerp(v[z1, y0, x0], v[z1, y0, x1], fx)
+    c11 = lerp(v[z1, y1, x0], v[z1, y1, x1], fx)
+    return lerp(lerp(c00, c10, fy), lerp(c01, c11, fy), fz)
+
+
+def _inside(shape, ax, ay, az):
+    nz, ny, nx = shape
+    return ((ax >= f32(0.5)) & (ay >= f32(0.5)) & (az >= f32(0.5)) & (ax <= f32(nx) - f32(0.5)) &
+            (ay <= f32(ny) - f32(0.5)) & (az <= f32(nz) - f32(0.5)))
+
+
+def rake(R, F, px, py, pz):
+    meia = np.maximum(f32(1.5), f32(F["avanco"]) * f32(0.6))
+    dx = np.abs(px - f32(R["x"]))
+    ay = (py - f32(R["y0"])) / f32(R["passo_y"])
+    az = (pz - f32(R["z0"])) / f32(R["passo_z"])
+    fy = np.abs((ay - np.floor(ay)) - f32(0.5)) * f32(R["passo_y"])
+    fz = np.abs((az - np.floor(az)) - f32(0.5)) * f32(R["passo_z"])
+    r = np.sqrt(fy * fy + fz * fz) / np.maximum(f32(R["raio"]), f32(1e-3))
+    with np.errstate(over="ignore"):
+        val = f32(F["taxa"]) * np.exp(-r * r * f32(5.5)) * (f32(1.0) - f32(0.35) * dx / meia)
+    off = (dx > meia) | (py < f32(R["y0"])) | (py > f32(R["y1"])) | (pz < f32(R["z0"])) | (pz > f32(R["z1"]))
+    return np.where(off, f32(0.0), val).astype(np.float32)
+
+
+def fumaca_passo(cur, mac, tipo, R, F):
+    """cur: float16 (nz, ny, nx); mac: float32 (nz, ny, nx, 4); tipo: (nz, ny, nx)."""
+    nz, ny, nx = cur.shape
+    z, y, x = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    px, py, pz = x.astype(f32) + f32(0.5), y.astype(f32) + f32(0.5), z.astype(f32) + f32(0.5)
+    ux, uy, uz = (mac[..., k].astype(np.float32) for k in range(3))
+    solid = np.isin(np.asarray(tipo), [1, 4, 7])
+    dt = f32(F["dt"])
+    ax, ay, az = px - ux * dt, py - uy * dt, pz - uz * dt
+    d = _sample(cur, ax, ay, az)
+    d = np.where(_inside(cur.shape, ax, ay, az), d, f32(0.0))
+    mid = np.where(solid, f32(0.0), d).astype(np.float16)
+    chapeu = mid.astype(np.float32)
+    voltando = _sample(mid, px + ux * dt, py + uy * dt, pz + uz * dt)
+    original = cur.astype(np.float32)
+    d = chapeu + f32(0.5) * (original - voltando)
+    bx, by, bz = np.floor(ax - f32(0.5)), np.floor(ay - f32(0.5)), np.floor(az - f32(0.5))
+    lo = np.full(cur.shape, f32(1e30))
+    hi = np.full(cur.shape, f32(-1e30))
+    c = cur.astype(np.float32)
+    for k in range(8):
+        qx = np.clip((bx + f32(k & 1)).astype(np.int64), 0, nx - 1)
+        qy = np.clip((by + f32((k >> 1) & 1)).astype(np.int64), 0, ny - 1)
+        qz = np.clip((bz + f32((k >> 2) & 1)).astype(np.int64), 0, nz - 1)
+        v = c[qz, qy, qx]
+        lo = np.minimum(lo, v)
+        hi = np.maximum(hi, v)
+    d = np.minimum(np.maximum(d, lo), hi) * f32(F["dissipacao"])
+    d = np.where(_inside(cur.shape, ax, ay, az), d, f32(0.0))
+    d = np.maximum(d, rake(R, F, px, py, pz))
+    d = np.minimum(np.maximum(d, f32(0.0)), f32(4.0))
+    return np.where(solid, f32(0.0), d).astype(np.float16)
+
+
+def _hash01(n):
+    n = np.asarray(n, np.uint32)
+    with np.errstate(over="ignore"):
+        x = n * np.uint32(747796405) + np.uint32(2891336453)
+        x = ((x >> ((x >> np.uint32(28)) + np.uint32(4))) ^ x) * np.uint32(277803737)
+    return ((x >> np.uint32(22)) ^ x).astype(np.float32) / f32(4294967296.0)
+
+
+def esteiras_passo(parts, mac, dt_quadro, nsub, quadro):
+    """parts: float32 (n, 8) = pos xyzw, ant xyzw; mac: float32 (nz, ny, nx, 4)."""
+    nz, ny, nx = mac.shape[:3]
+    P = np.array(parts, np.float32, copy=True)
+
+    def nearest(px, py, pz):
+        ix = np.clip(px.astype(np.int64), 0, nx - 1)
+        iy = np.clip(py.astype(np.int64), 0, ny - 1)
+        iz = np.clip(pz.astype(np.int64), 0, nz - 1)
+        return mac[iz, iy, ix].astype(np.float32)
+    m = nearest(P[:, 0], P[:, 1], P[:, 2])
+    ns = max(int(nsub), 1)
+    dt = f32(dt_quadro) / f32(ns)
+    x, y, z = P[:, 0].copy(), P[:, 1].copy(), P[:, 2].copy()
+    for _ in range(ns):
+        u = nearest(x, y, z)
+        x = x + u[:, 0] * dt
+        y = y + u[:, 1] * dt
+        z = z + u[:, 2] * dt
+    w = P[:, 3] - f32(1.0)
+    fx, fy, fz = f32(nx), f32(ny), f32(nz)
+    fora = (x >= fx - f32(1.0)) | (x < f32(1.0)) | (y < f32(1.0)) | (y >= fy - f32(1.0)) | (z < f32(0.5)) | \
+        (z >= fz - f32(1.0))
+    presa = np.sqrt(m[:, 0] * m[:, 0] + m[:, 1] * m[:, 1] + m[:, 2] * m[:, 2]) < f32(1e-5)
+    renasce = fora | presa | (w <= f32(0.0))
+    with np.errstate(over="ignore"):
+        s = np.arange(P.shape[0], dtype=np.uint32) * np.uint32(3) + np.uint32(quadro) * np.uint32(7919)
+    rx = f32(2.0) + _hash01(s) * f32(3.0)
+    ry = f32(2.0) + _hash01(s + np.uint32(1)) * (fy - f32(4.0))
+    rz = f32(0.5) + _hash01(s + np.uint32(2)) * (fz - f32(2.0))
+    rw = f32(220.0) + _hash01(s + np.uint32(5)) * f32(260.0)
+    out = np.empty_like(P)
+    out[:, 0] = np.where(renasce, rx, x)
+    out[:, 1] = np.where(renasce, ry, y)
+    out[:, 2] = np.where(renasce, rz, z)
+    out[:, 3] = np.where(renasce, rw, w)
+    out[:, 4] = np.where(renasce, rx, P[:, 0])
+    out[:, 5] = np.where(renasce, ry, P[:, 1])
+    out[:, 6] = np.where(renasce, rz, P[:, 2])
+    out[:, 7] = np.where(renasce, f32(0.0), f32(1.0))
+    return out
