@@ -280,6 +280,64 @@ def closure_forms(make, stream, steps, warmup, ms_plain, N):
     return out
 
 
+def vis_timing(make, stream, N, peak):
+    """Visualisation compute on the bench tunnel (include/lbm_vis.h): one smoke
+    step (back-trace + MacCormack, fp16 volume; algorithmic bytes per voxel:
+    2 x 16 B macros + 2 x 1 B types + 2 B current x 3 reads + 2 B
+    intermediate write + read + 2 B next write = 44 B), a 640x360 ray-march
+    of the volume, and one frame of 65 536 streak particles in 8 sub-steps."""
+    import torch
+
+    from cfd__gb300.visual import Esteiras, Fumaca, camera_orbita, posicionar_rake
+    s = make("f32")
+    s.passo(20)
+    s.atualizarMacros()
+    f = Fumaca(s)
+    ext = {"min": [0.28 * GRID["nx"], GRID["ny"] * 0.5 - 20, 3], "tamanho": [96, 40, 28],
+           "centro": [0.28 * GRID["nx"] + 48, GRID["ny"] * 0.5, 17]}
+    rake = posicionar_rake(GRID["ny"], GRID["nz"], ext)
+    for _ in range(5):
+        f.passo(rake, dt=44.0)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(20):
+        f.passo(rake, dt=44.0)
+    e1.record(stream)
+    e1.synchronize()
+    ms_smoke = e0.elapsed_time(e1) / 20
+    inv, eye = camera_orbita(GRID["nx"], GRID["ny"], GRID["nz"])
+    f.render(inv, eye, largura=640, altura=360)
+    t0 = time.perf_counter()
+    img = f.render(inv, eye, largura=640, altura=360)
+    ms_render = (time.perf_counter() - t0) * 1e3
+    rng = np.random.default_rng(0)
+    n = 65536
+    parts = np.zeros((n, 8), np.float32)
+    parts[:, 0] = rng.uniform(2, 5, n)
+    parts[:, 1] = rng.uniform(2, GRID["ny"] - 2, n)
+    parts[:, 2] = rng.uniform(1, GRID["nz"] - 2, n)
+    parts[:, 3] = rng.uniform(200, 400, n)
+    e = Esteiras(s, n)
+    e.definir(parts)
+    e.passo(24.0, 8, 0)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for q in range(20):
+        e.passo(24.0, 8, q)
+    e1.record(stream)
+    e1.synchronize()
+    ms_parts = e0.elapsed_time(e1) / 20
+    out = {"smoke_step_ms": ms_smoke, "smoke_Mvoxels_per_s": N / ms_smoke / 1e3,
+           "smoke_roofline_frac": 44 * N / (ms_smoke / 1e3) / 1e9 / peak,
+           "render_640x360_ms_e2e": ms_render, "render_mean_alpha": float(img[..., 3].mean()),
+           "particles_65536x8_ms": ms_parts}
+    e.destruir()
+    f.destruir()
+    s.destruir()
+    return out
+
+
 def run_ours(args):
     import torch
     world, rank, local = dist_setup()
@@ -362,6 +420,7 @@ def run_ours(args):
                          "roofline_frac": BYTES_PER_CELL[st] * N / (ms2 / args.steps / 1e3) / 1e9 / peak}
             s2.destruir()
         forms.update(closure_forms(make, stream, args.steps, args.warmup, ms_step, N))
+        forms["visual"] = vis_timing(make, stream, N, peak)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:

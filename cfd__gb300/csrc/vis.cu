@@ -166,9 +166,11 @@ __device__ __forceinline__ float4 nearest(const float4* mac, Grid g, float px, f
   return mac[((int64_t)z * g.ny + y) * g.nx + x];
 }
 
-// One frame of the streak particles (src/render/renderer.js:61-116).
+// One frame of the streak particles (src/render/renderer.js:61-116); RAS:
+// the ground streaks (src/render/rasante.js:95-149).
+template <bool RAS>
 __global__ void k_esteiras(vis_part* __restrict__ parts, long long n, const float4* __restrict__ mac, Grid g,
-                           float dt_quadro, int nsub, uint32_t quadro) {
+                           float dt_quadro, int nsub, uint32_t quadro, float altura) {
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   vis_part P = parts[i];
@@ -184,20 +186,124 @@ __global__ void k_esteiras(vis_part* __restrict__ parts, long long n, const floa
   }
   float w = P.pos[3] - 1.0f;
   const float fx = (float)g.nx, fy = (float)g.ny, fz = (float)g.nz;
-  const bool fora = x >= fx - 1.0f || x < 1.0f || y < 1.0f || y >= fy - 1.0f || z < 0.5f || z >= fz - 1.0f;
+  const bool fora = x >= fx - 1.0f || x < 1.0f || y < 1.0f || y >= fy - 1.0f || z < (RAS ? 0.4f : 0.5f) ||
+                    z >= fz - 1.0f;
   const bool presa = sqrtf(m.x * m.x + m.y * m.y + m.z * m.z) < 1e-5f;
   if (fora || presa || w <= 0.0f) {
     const uint32_t s = (uint32_t)i * 3u + quadro * 7919u;
-    x = 2.0f + hash01(s) * 3.0f;
-    y = 2.0f + hash01(s + 1u) * (fy - 4.0f);
-    z = 0.5f + hash01(s + 2u) * (fz - 2.0f);
-    w = 220.0f + hash01(s + 5u) * 260.0f;
+    if (RAS) {
+      const float h = hash01(s + 2u);
+      x = 1.5f + hash01(s) * 4.0f;
+      y = 1.0f + hash01(s + 1u) * (fy - 2.0f);
+      z = 0.6f + h * h * h * altura;
+      w = 150.0f + hash01(s + 5u) * 320.0f;
+    } else {
+      x = 2.0f + hash01(s) * 3.0f;
+      y = 2.0f + hash01(s + 1u) * (fy - 4.0f);
+      z = 0.5f + hash01(s + 2u) * (fz - 2.0f);
+      w = 220.0f + hash01(s + 5u) * 260.0f;
+    }
     P.ant[0] = x; P.ant[1] = y; P.ant[2] = z; P.ant[3] = 0.0f;
   } else {
     P.ant[0] = P.pos[0]; P.ant[1] = P.pos[1]; P.ant[2] = P.pos[2]; P.ant[3] = 1.0f;
   }
   P.pos[0] = x; P.pos[1] = y; P.pos[2] = z; P.pos[3] = w;
   parts[i] = P;
+}
+
+// ---- ray-march of the smoke volume (src/render/fumaca.js:257-349) ----
+struct V3 {
+  float x, y, z;
+};
+__device__ __forceinline__ V3 v3(float x, float y, float z) { return V3{x, y, z}; }
+__device__ __forceinline__ V3 operator+(V3 a, V3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ V3 operator-(V3 a, V3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ V3 operator*(V3 a, float s) { return v3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ float dot3(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ V3 normalize3(V3 a) {
+  const float l = sqrtf(dot3(a, a));
+  return v3(a.x / l, a.y / l, a.z / l);
+}
+__device__ __forceinline__ float fract(float x) { return x - floorf(x); }
+
+// clip space (ndc.x, ndc.y, depth) -> world through the inverse view-projection
+__device__ __forceinline__ V3 world_of(const float* m, float nx_, float ny_, float z) {
+  float h[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) h[i] = ((m[i] * nx_ + m[4 + i] * ny_) + m[8 + i] * z) + m[12 + i];
+  return v3(h[0] / h[3], h[1] / h[3], h[2] / h[3]);
+}
+
+__device__ __forceinline__ float hash12(float px, float py) {
+  float p3x = fract(px * 0.1031f), p3y = fract(py * 0.1031f), p3z = fract(px * 0.1031f);
+  const float d = p3x * (p3y + 33.33f) + p3y * (p3z + 33.33f) + p3z * (p3x + 33.33f);
+  p3x = p3x + d; p3y = p3y + d; p3z = p3z + d;
+  return fract((p3x + p3y) * p3z);
+}
+
+__device__ __forceinline__ float density_at(const __half* vol, Grid g, float k, V3 w) {
+  const float px = w.x / k + (float)g.nx * 0.5f, py = w.y / k + (float)g.ny * 0.5f, pz = w.z / k;
+  const float ux = px / (float)g.nx, uy = py / (float)g.ny, uz = pz / (float)g.nz;
+  if (ux < 0.0f || uy < 0.0f || uz < 0.0f || ux > 1.0f || uy > 1.0f || uz > 1.0f) return 0.0f;
+  return sample3(vol, g, px, py, pz);
+}
+
+__global__ void k_render(const __half* __restrict__ vol, Grid g, vis_camera cam, float4* __restrict__ img) {
+  const int ix = blockIdx.x * blockDim.x + threadIdx.x;
+  const int iy = blockIdx.y * blockDim.y + threadIdx.y;
+  if (ix >= cam.largura || iy >= cam.altura) return;
+  const float fx = (float)ix + 0.5f, fy = (float)iy + 0.5f;
+  const float ndx = fx / (float)cam.largura * 2.0f - 1.0f;
+  const float ndy = 1.0f - fy / (float)cam.altura * 2.0f;
+  float4 out = make_float4(0.f, 0.f, 0.f, 0.f);
+  const V3 origem = v3(cam.olho[0], cam.olho[1], cam.olho[2]);
+  const V3 alvo = world_of(cam.inv_view_proj, ndx, ndy, 1.0f);
+  const V3 dir = normalize3(alvo - origem);
+  const float k = (1.0f / (float)g.nx) * 2.0f;
+  const V3 lo = v3(-(float)g.nx * 0.5f * k, -(float)g.ny * 0.5f * k, 0.0f);
+  const V3 hi = v3((float)g.nx * 0.5f * k, (float)g.ny * 0.5f * k, (float)g.nz * k);
+  // slab test (src/render/comum.js:81-89)
+  const float ivx = 1.0f / dir.x, ivy = 1.0f / dir.y, ivz = 1.0f / dir.z;
+  const float ax = (lo.x - origem.x) * ivx, bx = (hi.x - origem.x) * ivx;
+  const float ay = (lo.y - origem.y) * ivy, by = (hi.y - origem.y) * ivy;
+  const float az = (lo.z - origem.z) * ivz, bz = (hi.z - origem.z) * ivz;
+  const float tmin = fmaxf(fmaxf(fminf(ax, bx), fminf(ay, by)), fminf(az, bz));
+  const float tmax = fminf(fminf(fmaxf(ax, bx), fmaxf(ay, by)), fmaxf(az, bz));
+  const float t0 = fmaxf(tmin, 0.0f), t1 = tmax;
+  if (t1 > t0) {
+    const int np = cam.passos, nl = cam.passos_luz;
+    const float ds = (t1 - t0) / (float)np;
+    const float sigma = cam.densidade, gg = cam.g;
+    const V3 luz_dir = normalize3(v3(cam.luz[0], cam.luz[1], cam.luz[2]));
+    // Henyey-Greenstein
+    const float g2 = gg * gg;
+    const float dd = 1.0f + g2 - 2.0f * gg * dot3(dir, luz_dir);
+    const float fase = (1.0f - g2) / (12.566370614f * fmaxf(dd * sqrtf(dd), 1e-4f));
+    const float jitter = hash12(fx + cam.quadro * 0.618f, fy + cam.quadro * 0.618f) * ds;
+    float T = 1.0f, Lr = 0.0f, Lg = 0.0f, Lb = 0.0f;
+    float s = t0 + jitter;
+    const float dl = (hi.z - lo.z) / (float)nl * 0.9f;
+    for (int i = 0; i < np; ++i) {
+      if (T < 0.01f) break;
+      const V3 w = origem + dir * s;
+      const float d = density_at(vol, g, k, w);
+      s = s + ds;
+      if (d <= 0.001f) continue;
+      const float st = d * sigma;
+      const float atenua = 1.0f - expf(-st * ds);
+      float tau = 0.0f;
+      for (int j = 1; j <= nl; ++j) tau = tau + density_at(vol, g, k, w + luz_dir * ((float)j * dl)) * sigma * dl;
+      const float luz = expf(-tau);
+      const float ambiente = 0.16f + 0.10f * expf(-tau * 0.35f);
+      const float c = T * atenua * (luz * fase * 3.6f + ambiente) * cam.luz[3];
+      Lr = Lr + c * 0.96f;
+      Lg = Lg + c * 0.97f;
+      Lb = Lb + c * 1.0f;
+      T = T * expf(-st * ds);
+    }
+    out = make_float4(Lr, Lg, Lb, 1.0f - T);
+  }
+  img[(size_t)iy * cam.largura + ix] = out;
 }
 
 }  // namespace
@@ -344,9 +450,46 @@ int vis_esteiras_passo(vis_esteiras* e, float dt_quadro, int nsub, uint32_t quad
   int r = ctx_view(e->ctx, &v);
   if (r) return r;
   const Grid g{v.nx, v.ny, v.nz};
-  k_esteiras<<<(unsigned)((e->n + 127) / 128), 128, 0, v.stream>>>(e->parts, (long long)e->n, v.macros, g, dt_quadro,
-                                                                  nsub, quadro);
+  k_esteiras<false><<<(unsigned)((e->n + 127) / 128), 128, 0, v.stream>>>(e->parts, (long long)e->n, v.macros, g,
+                                                                         dt_quadro, nsub, quadro, 0.0f);
   VCK(cudaGetLastError(), "particle kernel");
+  return LBM_OK;
+}
+
+int vis_rasantes_passo(vis_esteiras* e, float dt_quadro, int nsub, uint32_t quadro, float altura) {
+  if (!e) return vfail(LBM_EINVAL, "null particles");
+  if (nsub < 1 || nsub > 4096) return vfail(LBM_EINVAL, "sub-steps must be 1..4096");
+  CtxView v;
+  int r = ctx_view(e->ctx, &v);
+  if (r) return r;
+  const Grid g{v.nx, v.ny, v.nz};
+  k_esteiras<true><<<(unsigned)((e->n + 127) / 128), 128, 0, v.stream>>>(e->parts, (long long)e->n, v.macros, g,
+                                                                        dt_quadro, nsub, quadro, altura);
+  VCK(cudaGetLastError(), "ground streak kernel");
+  return LBM_OK;
+}
+
+int vis_fumaca_render(vis_fumaca* f, const vis_camera* cam, float* rgba, size_t n) {
+  if (!f || !cam || !rgba) return vfail(LBM_EINVAL, "null argument");
+  if (cam->largura < 1 || cam->altura < 1 || cam->largura > 16384 || cam->altura > 16384)
+    return vfail(LBM_EINVAL, "image size must be 1..16384 per side");
+  if (cam->passos < 1 || cam->passos > 4096 || cam->passos_luz < 1 || cam->passos_luz > 256)
+    return vfail(LBM_EINVAL, "march steps must be 1..4096 (light 1..256)");
+  const size_t px = (size_t)cam->largura * (size_t)cam->altura;
+  if (n != 4 * px) return vfail(LBM_EINVAL, "rgba must hold largura * altura * 4 floats");
+  CtxView v;
+  int r = ctx_view(f->ctx, &v);
+  if (r) return r;
+  float4* d_img = nullptr;
+  VCK(cudaMalloc(&d_img, sizeof(float4) * px), "image");
+  const Grid g{f->nx, f->ny, f->nz};
+  const dim3 block(16, 8), grid((cam->largura + 15) / 16, (cam->altura + 7) / 8);
+  k_render<<<grid, block, 0, v.stream>>>(f->vol[0], g, *cam, d_img);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(rgba, d_img, sizeof(float4) * px, cudaMemcpyDeviceToHost, v.stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(v.stream);
+  cudaFree(d_img);
+  VCK(e, "smoke render");
   return LBM_OK;
 }
 

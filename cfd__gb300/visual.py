@@ -24,6 +24,42 @@ class Part(C.Structure):
     _fields_ = [("pos", C.c_float * 4), ("ant", C.c_float * 4)]
 
 
+class Camera(C.Structure):
+    _fields_ = [("inv_view_proj", C.c_float * 16), ("olho", C.c_float * 3), ("densidade", C.c_float),
+                ("g", C.c_float), ("passos", C.c_int32), ("passos_luz", C.c_int32), ("luz", C.c_float * 4),
+                ("quadro", C.c_float), ("largura", C.c_int32), ("altura", C.c_int32)]
+
+
+def camera_orbita(nx, ny, nz, azimute=0.6, elevacao=0.35, distancia=2.6, fov=0.8, aspecto=16 / 9):
+    """A view-projection looking at the middle of the tunnel floor from an
+    orbit (world = lattice scaled by 2/nx, origin at the floor's centre, z up;
+    src/render/comum.js:56-71), depth mapped to [0, 1] as WebGPU does.
+    Returns (inv_view_proj column-major, eye)."""
+    k = 2.0 / nx
+    alvo = np.array([0.0, 0.0, nz * k * 0.35])
+    olho = alvo + distancia * np.array([np.cos(elevacao) * np.cos(azimute), np.cos(elevacao) * np.sin(azimute),
+                                        np.sin(elevacao)])
+    f = alvo - olho
+    f = f / np.linalg.norm(f)
+    up = np.array([0.0, 0.0, 1.0])
+    r = np.cross(f, up)
+    r = r / np.linalg.norm(r)
+    u = np.cross(r, f)
+    view = np.eye(4)
+    view[0, :3], view[1, :3], view[2, :3] = r, u, -f
+    view[:3, 3] = -view[:3, :3] @ olho
+    near, far = 0.05, 50.0
+    t = 1.0 / np.tan(fov / 2)
+    proj = np.zeros((4, 4))
+    proj[0, 0] = t / aspecto
+    proj[1, 1] = t
+    proj[2, 2] = far / (near - far)
+    proj[2, 3] = near * far / (near - far)
+    proj[3, 2] = -1.0
+    inv = np.linalg.inv(proj @ view)
+    return inv.T.reshape(-1).astype(np.float32), olho.astype(np.float32)
+
+
 def posicionar_rake(ny, nz, extentos, colunas=7, linhas=5):
     """VolumeFumaca.posicionarRake + _recalcularGrade (src/render/fumaca.js:539-590):
     the rake in front of the body, covering it with margin; filament spacing
@@ -69,6 +105,24 @@ class Fumaca:
         a = np.ascontiguousarray(dens, np.float16).reshape(-1)
         nat.check(self._lib.vis_fumaca_definir(self._h, nat.ptr(a), a.size))
 
+    def render(self, inv_view_proj, olho, largura=320, altura=180, densidade=70.0, g=0.45, passos=96,
+               passos_luz=5, luz=(-0.35, 0.55, 0.76), intensidade=1.0, quadro=0):
+        """Ray-march of the volume into an (altura, largura, 4) float32 image
+        (premultiplied radiance, 1 - transmittance; row 0 at the top)."""
+        cam = Camera()
+        for i in range(16):
+            cam.inv_view_proj[i] = float(inv_view_proj[i])
+        for i in range(3):
+            cam.olho[i] = float(olho[i])
+        cam.densidade, cam.g, cam.passos, cam.passos_luz = float(densidade), float(g), int(passos), int(passos_luz)
+        for i in range(3):
+            cam.luz[i] = float(luz[i])
+        cam.luz[3] = float(intensidade)
+        cam.quadro, cam.largura, cam.altura = float(quadro), int(largura), int(altura)
+        out = np.empty((int(altura), int(largura), 4), np.float32)
+        nat.check(self._lib.vis_fumaca_render(self._h, C.byref(cam), nat.ptr(out), out.size))
+        return out
+
     def destruir(self):
         if getattr(self, "_h", None):
             nat.check(self._lib.vis_fumaca_destroy(self._h))
@@ -96,6 +150,11 @@ class Esteiras:
 
     def passo(self, dt_quadro, subpassos=1, quadro=0):
         nat.check(self._lib.vis_esteiras_passo(self._h, float(dt_quadro), int(subpassos), int(quadro) & 0xFFFFFFFF))
+
+    def passo_rasantes(self, dt_quadro, subpassos=1, quadro=0, altura=6.0):
+        """The ground-streak frame (src/render/rasante.js:95-149) on the same records."""
+        nat.check(self._lib.vis_rasantes_passo(self._h, float(dt_quadro), int(subpassos), int(quadro) & 0xFFFFFFFF,
+                                               float(altura)))
 
     def destruir(self):
         if getattr(self, "_h", None):

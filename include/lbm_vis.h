@@ -80,6 +80,30 @@ int vis_esteiras_ler(vis_esteiras* e, vis_part* out, size_t n);
  * nearest-cell velocity; `quadro` seeds the respawn hash. */
 int vis_esteiras_passo(vis_esteiras* e, float dt_quadro, int nsub, uint32_t quadro);
 
+/* The same frame for the ground streaks (src/render/rasante.js:95-149): they
+ * leave below z = 0.4 and respawn just after the inlet, biased to the floor
+ * (z = 0.6 + h^3 * altura). */
+int vis_rasantes_passo(vis_esteiras* e, float dt_quadro, int nsub, uint32_t quadro, float altura);
+
+/* Camera of the smoke render (the reference's scene uniform,
+ * src/render/comum.js:31-47, and smoke light, src/render/fumaca.js:62-67). */
+typedef struct {
+  float inv_view_proj[16];   /* column-major, clip space -> world (depth 0..1) */
+  float olho[3];             /* camera position, world */
+  float densidade;           /* extinction per unit density */
+  float g;                   /* Henyey-Greenstein anisotropy */
+  int32_t passos, passos_luz;
+  float luz[4];              /* light direction (normalised inside), intensity */
+  float quadro;              /* frame number for the per-pixel jitter */
+  int32_t largura, altura;   /* image in pixels */
+} vis_camera;
+
+/* Ray-march of the current smoke volume (src/render/fumaca.js:218-349) into
+ * rgba (largura * altura * 4 floats, row 0 at the top, premultiplied
+ * radiance and 1 - transmittance); no opaque depth buffer, rays that miss the
+ * domain give 0.  Synchronises. */
+int vis_fumaca_render(vis_fumaca* f, const vis_camera* cam, float* rgba, size_t n);
+
 #ifdef __cplusplus
 }
 #endif

@@ -11,9 +11,12 @@ volume:
                    trilinear samples with clamp-to-edge at t = p - 0.5,
                    interpolated along x, y, z as a + f (b - a);
   * esteiras_passo one frame of the streak particles
-                   (src/render/renderer.js:51-116), with its integer hash.
-exp() of the rake may differ from the GPU's expf in the last place; tests
-allow for that where the rake is active.
+                   (src/render/renderer.js:51-116) or of the ground streaks
+                   (src/render/rasante.js:95-149), with the integer hash;
+  * render         the ray-march of the smoke volume into an image
+                   (src/render/fumaca.js:257-349).
+exp() of the rake and of the ray-march may differ from the GPU's expf in the
+last place; tests allow for that where it is used.
 """
 from __future__ import annotations
 
@@ -103,8 +106,9 @@ def _hash01(n):
     return ((x >> np.uint32(22)) ^ x).astype(np.float32) / f32(4294967296.0)
 
 
-def esteiras_passo(parts, mac, dt_quadro, nsub, quadro):
-    """parts: float32 (n, 8) = pos xyzw, ant xyzw; mac: float32 (nz, ny, nx, 4)."""
+def esteiras_passo(parts, mac, dt_quadro, nsub, quadro, rasantes=False, altura=0.0):
+    """parts: float32 (n, 8) = pos xyzw, ant xyzw; mac: float32 (nz, ny, nx, 4).
+    rasantes: the ground streaks (src/render/rasante.js:95-149)."""
     nz, ny, nx = mac.shape[:3]
     P = np.array(parts, np.float32, copy=True)
 
@@ -124,16 +128,24 @@ def esteiras_passo(parts, mac, dt_quadro, nsub, quadro):
         z = z + u[:, 2] * dt
     w = P[:, 3] - f32(1.0)
     fx, fy, fz = f32(nx), f32(ny), f32(nz)
-    fora = (x >= fx - f32(1.0)) | (x < f32(1.0)) | (y < f32(1.0)) | (y >= fy - f32(1.0)) | (z < f32(0.5)) | \
+    zmin = f32(0.4) if rasantes else f32(0.5)
+    fora = (x >= fx - f32(1.0)) | (x < f32(1.0)) | (y < f32(1.0)) | (y >= fy - f32(1.0)) | (z < zmin) | \
         (z >= fz - f32(1.0))
     presa = np.sqrt(m[:, 0] * m[:, 0] + m[:, 1] * m[:, 1] + m[:, 2] * m[:, 2]) < f32(1e-5)
     renasce = fora | presa | (w <= f32(0.0))
     with np.errstate(over="ignore"):
         s = np.arange(P.shape[0], dtype=np.uint32) * np.uint32(3) + np.uint32(quadro) * np.uint32(7919)
-    rx = f32(2.0) + _hash01(s) * f32(3.0)
-    ry = f32(2.0) + _hash01(s + np.uint32(1)) * (fy - f32(4.0))
-    rz = f32(0.5) + _hash01(s + np.uint32(2)) * (fz - f32(2.0))
-    rw = f32(220.0) + _hash01(s + np.uint32(5)) * f32(260.0)
+    if rasantes:
+        h = _hash01(s + np.uint32(2))
+        rx = f32(1.5) + _hash01(s) * f32(4.0)
+        ry = f32(1.0) + _hash01(s + np.uint32(1)) * (fy - f32(2.0))
+        rz = f32(0.6) + h * h * h * f32(altura)
+        rw = f32(150.0) + _hash01(s + np.uint32(5)) * f32(320.0)
+    else:
+        rx = f32(2.0) + _hash01(s) * f32(3.0)
+        ry = f32(2.0) + _hash01(s + np.uint32(1)) * (fy - f32(4.0))
+        rz = f32(0.5) + _hash01(s + np.uint32(2)) * (fz - f32(2.0))
+        rw = f32(220.0) + _hash01(s + np.uint32(5)) * f32(260.0)
     out = np.empty_like(P)
     out[:, 0] = np.where(renasce, rx, x)
     out[:, 1] = np.where(renasce, ry, y)
@@ -144,3 +156,91 @@ def esteiras_passo(parts, mac, dt_quadro, nsub, quadro):
     out[:, 6] = np.where(renasce, rz, P[:, 2])
     out[:, 7] = np.where(renasce, f32(0.0), f32(1.0))
     return out
+
+
+def _fract(x):
+    return x - np.floor(x)
+
+
+def render(vol, inv_view_proj, olho, largura, altura, densidade, g, passos, passos_luz, luz, intensidade, quadro):
+    """Ray-march of a float16 volume (src/render/fumaca.js:257-349) into an
+    (altura, largura, 4) float32 image; no opaque depth; rays that miss give 0."""
+    nz, ny, nx = vol.shape
+    m = np.asarray(inv_view_proj, np.float32)
+    iy, ix = np.meshgrid(np.arange(altura), np.arange(largura), indexing="ij")
+    fx, fy = ix.astype(f32) + f32(0.5), iy.astype(f32) + f32(0.5)
+    ndx = fx / f32(largura) * f32(2.0) - f32(1.0)
+    ndy = f32(1.0) - fy / f32(altura) * f32(2.0)
+    h = [((m[i] * ndx + m[4 + i] * ndy) + m[8 + i] * f32(1.0)) + m[12 + i] for i in range(4)]
+    alvo = [h[0] / h[3], h[1] / h[3], h[2] / h[3]]
+    o = [f32(v) for v in olho]
+    d = [alvo[0] - o[0], alvo[1] - o[1], alvo[2] - o[2]]
+    ln = np.sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2])
+    d = [d[0] / ln, d[1] / ln, d[2] / ln]
+    k = (f32(1.0) / f32(nx)) * f32(2.0)
+    lo = [-f32(nx) * f32(0.5) * k, -f32(ny) * f32(0.5) * k, f32(0.0)]
+    hi = [f32(nx) * f32(0.5) * k, f32(ny) * f32(0.5) * k, f32(nz) * k]
+    with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
+        inv = [f32(1.0) / d[a] for a in range(3)]
+        ta = [(lo[a] - o[a]) * inv[a] for a in range(3)]
+        tb = [(hi[a] - o[a]) * inv[a] for a in range(3)]
+    tmin = np.maximum(np.maximum(np.minimum(ta[0], tb[0]), np.minimum(ta[1], tb[1])), np.minimum(ta[2], tb[2]))
+    tmax = np.minimum(np.minimum(np.maximum(ta[0], tb[0]), np.maximum(ta[1], tb[1])), np.maximum(ta[2], tb[2]))
+    t0 = np.maximum(tmin, f32(0.0))
+    t1 = tmax
+    hit = t1 > t0
+    ds = (t1 - t0) / f32(passos)
+    ll = np.sqrt(f32(luz[0]) ** 2 + f32(luz[1]) ** 2 + f32(luz[2]) ** 2)
+    L = [f32(luz[0]) / ll, f32(luz[1]) / ll, f32(luz[2]) / ll]
+    gg = f32(g)
+    g2 = gg * gg
+    cos = d[0] * L[0] + d[1] * L[1] + d[2] * L[2]
+    dd = f32(1.0) + g2 - f32(2.0) * gg * cos
+    fase = (f32(1.0) - g2) / (f32(12.566370614) * np.maximum(dd * np.sqrt(dd), f32(1e-4)))
+    qx = fx + f32(quadro) * f32(0.618)
+    qy = fy + f32(quadro) * f32(0.618)
+    p3x, p3y, p3z = _fract(qx * f32(0.1031)), _fract(qy * f32(0.1031)), _fract(qx * f32(0.1031))
+    dt_ = p3x * (p3y + f32(33.33)) + p3y * (p3z + f32(33.33)) + p3z * (p3x + f32(33.33))
+    p3x, p3y, p3z = p3x + dt_, p3y + dt_, p3z + dt_
+    jitter = _fract((p3x + p3y) * p3z) * ds
+
+    def dens(wx, wy, wz):
+        px = wx / k + f32(nx) * f32(0.5)
+        py = wy / k + f32(ny) * f32(0.5)
+        pz = wz / k
+        ux, uy, uz = px / f32(nx), py / f32(ny), pz / f32(nz)
+        out = (ux < 0) | (uy < 0) | (uz < 0) | (ux > 1) | (uy > 1) | (uz > 1)
+        v = _sample(vol, np.where(out, f32(1.0), px), np.where(out, f32(1.0), py), np.where(out, f32(1.0), pz))
+        return np.where(out, f32(0.0), v).astype(np.float32)
+    T = np.ones(fx.shape, np.float32)
+    Lr, Lg, Lb = (np.zeros(fx.shape, np.float32) for _ in range(3))
+    s = t0 + jitter
+    sigma = f32(densidade)
+    dl = (hi[2] - lo[2]) / f32(passos_luz) * f32(0.9)
+    alive = hit.copy()
+    for _ in range(passos):
+        alive &= ~(T < f32(0.01))
+        wx, wy, wz = o[0] + d[0] * s, o[1] + d[1] * s, o[2] + d[2] * s
+        dv = dens(wx, wy, wz)
+        s = s + ds
+        act = alive & ~(dv <= f32(0.001))
+        st = dv * sigma
+        with np.errstate(over="ignore", invalid="ignore"):
+            atenua = f32(1.0) - np.exp(-st * ds)
+            tau = np.zeros(fx.shape, np.float32)
+            for j in range(1, passos_luz + 1):
+                off = f32(j) * dl
+                tau = tau + dens(wx + L[0] * off, wy + L[1] * off, wz + L[2] * off) * sigma * dl
+            lz = np.exp(-tau)
+            amb = f32(0.16) + f32(0.10) * np.exp(-tau * f32(0.35))
+            c = T * atenua * (lz * fase * f32(3.6) + amb) * f32(intensidade)
+            Lr = np.where(act, Lr + c * f32(0.96), Lr)
+            Lg = np.where(act, Lg + c * f32(0.97), Lg)
+            Lb = np.where(act, Lb + c * f32(1.0), Lb)
+            T = np.where(act, T * np.exp(-st * ds), T)
+    img = np.zeros((altura, largura, 4), np.float32)
+    img[..., 0] = np.where(hit, Lr, 0)
+    img[..., 1] = np.where(hit, Lg, 0)
+    img[..., 2] = np.where(hit, Lb, 0)
+    img[..., 3] = np.where(hit, f32(1.0) - T, 0)
+    return img

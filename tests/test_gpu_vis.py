@@ -106,3 +106,45 @@ def test_vis_argument_checks(native):
     f.destruir()
     e.destruir()
     s.destruir()
+
+
+def test_ground_streaks_bit_exact(native):
+    from cfd__gb300.visual import Esteiras
+    s, grade, tipo, mac = _state(45)
+    n = 3000
+    rng = np.random.default_rng(3)
+    parts = np.zeros((n, 8), np.float32)
+    parts[:, 0] = rng.uniform(0, grade["nx"], n)
+    parts[:, 1] = rng.uniform(0, grade["ny"], n)
+    parts[:, 2] = rng.uniform(0, 4, n)
+    parts[:, 3] = rng.uniform(-5, 300, n)
+    e = Esteiras(s, n)
+    e.definir(parts)
+    for quadro in range(4):
+        parts = V.esteiras_passo(parts, mac, 9.0, 3, quadro, rasantes=True, altura=5.5)
+        e.passo_rasantes(9.0, 3, quadro, altura=5.5)
+        assert np.array_equal(e.ler(), parts)
+    e.destruir()
+    s.destruir()
+
+
+def test_smoke_render_matches_oracle(native):
+    from cfd__gb300.visual import Fumaca, camera_orbita
+    s, grade, tipo, mac = _state(46)
+    f = Fumaca(s)
+    rng = np.random.default_rng(5)
+    vol = np.zeros(f.shape, np.float16)
+    vol[2:12, 5:18, 8:30] = rng.uniform(0, 1.5, (10, 13, 22)).astype(np.float16)
+    f.definir(vol)
+    inv, eye = camera_orbita(grade["nx"], grade["ny"], grade["nz"], aspecto=64 / 36)
+    kw = dict(largura=64, altura=36, densidade=70.0, g=0.45, passos=48, passos_luz=5, luz=(-0.35, 0.55, 0.76),
+              intensidade=1.0, quadro=3)
+    got = f.render(inv, eye, **kw)
+    ref = V.render(vol, inv, eye, kw["largura"], kw["altura"], kw["densidade"], kw["g"], kw["passos"],
+                   kw["passos_luz"], kw["luz"], kw["intensidade"], kw["quadro"])
+    assert (ref[..., 3] > 0.05).sum() > 50
+    close = np.abs(got - ref) <= 1e-4 + 1e-3 * np.abs(ref)
+    assert close.mean() > 0.99, close.mean()
+    assert np.abs(got - ref).max() < 2e-2
+    f.destruir()
+    s.destruir()
