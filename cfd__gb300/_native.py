@@ -139,6 +139,7 @@ SIGNATURES = {
     "vis_esteiras_passo": (C.c_int, [C.c_void_p, C.c_float, C.c_int, C.c_uint32]),
     "vis_rasantes_passo": (C.c_int, [C.c_void_p, C.c_float, C.c_int, C.c_uint32, C.c_float]),
     "vis_fumaca_render": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t]),
+    "vis_cp_triangulos": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.c_float, C.c_void_p]),
     "vox_voxelize": (C.c_int, [C.c_void_p, C.c_size_t, C.c_void_p, C.c_size_t, C.POINTER(Dims), C.c_float, C.c_int,
                                C.c_void_p, C.c_void_p, C.POINTER(VoxStats)]),
 }

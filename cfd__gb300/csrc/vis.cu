@@ -306,6 +306,25 @@ __global__ void k_render(const __half* __restrict__ vol, Grid g, vis_camera cam,
   img[(size_t)iy * cam.largura + ix] = out;
 }
 
+// Surface Cp per triangle (src/render/renderer.js:168-180, at the centroid).
+__global__ void k_cp(const float* __restrict__ pos, const uint32_t* __restrict__ idx, long long nt,
+                     const float4* __restrict__ mac, const uint8_t* __restrict__ tipo, Grid g, float u_ref,
+                     float* __restrict__ cp) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nt) return;
+  const uint32_t a = idx[3 * t], b = idx[3 * t + 1], c = idx[3 * t + 2];
+  const V3 v0 = v3(pos[3 * a], pos[3 * a + 1], pos[3 * a + 2]);
+  const V3 v1 = v3(pos[3 * b], pos[3 * b + 1], pos[3 * b + 2]);
+  const V3 v2 = v3(pos[3 * c], pos[3 * c + 1], pos[3 * c + 2]);
+  const V3 e1 = v1 - v0, e2 = v2 - v0;
+  const V3 n = normalize3(v3(e1.y * e2.z - e1.z * e2.y, e1.z * e2.x - e1.x * e2.z, e1.x * e2.y - e1.y * e2.x));
+  const V3 cen = v3(((v0.x + v1.x) + v2.x) / 3.0f, ((v0.y + v1.y) + v2.y) / 3.0f, ((v0.z + v1.z) + v2.z) / 3.0f);
+  V3 fora = cen + n * 1.8f;
+  if (solid_at(tipo, g, (int)fora.x, (int)fora.y, (int)fora.z)) fora = cen - n * 1.8f;
+  const float4 m = nearest(mac, g, fora.x, fora.y, fora.z);
+  cp[t] = m.w / fmaxf(1.5f * u_ref * u_ref, 1e-12f);
+}
+
 }  // namespace
 
 extern "C" {
@@ -466,6 +485,36 @@ int vis_rasantes_passo(vis_esteiras* e, float dt_quadro, int nsub, uint32_t quad
   k_esteiras<true><<<(unsigned)((e->n + 127) / 128), 128, 0, v.stream>>>(e->parts, (long long)e->n, v.macros, g,
                                                                         dt_quadro, nsub, quadro, altura);
   VCK(cudaGetLastError(), "ground streak kernel");
+  return LBM_OK;
+}
+
+int vis_cp_triangulos(lbm_ctx* ctx, const float* pos, size_t nv, const uint32_t* idx, size_t nt, float u_ref,
+                      float* cp_out) {
+  if (!ctx || !pos || !idx || !cp_out || nv == 0 || nt == 0) return vfail(LBM_EINVAL, "null argument or empty mesh");
+  for (size_t i = 0; i < 3 * nt; ++i)
+    if (idx[i] >= nv) return vfail(LBM_EINVAL, "triangle index out of range");
+  CtxView v;
+  int r = ctx_view(ctx, &v);
+  if (r) return r;
+  float *d_pos = nullptr, *d_cp = nullptr;
+  uint32_t* d_idx = nullptr;
+  cudaError_t e = cudaMalloc(&d_pos, sizeof(float) * 3 * nv);
+  if (e == cudaSuccess) e = cudaMalloc(&d_idx, sizeof(uint32_t) * 3 * nt);
+  if (e == cudaSuccess) e = cudaMalloc(&d_cp, sizeof(float) * nt);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_pos, pos, sizeof(float) * 3 * nv, cudaMemcpyHostToDevice, v.stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_idx, idx, sizeof(uint32_t) * 3 * nt, cudaMemcpyHostToDevice, v.stream);
+  if (e == cudaSuccess) {
+    const Grid g{v.nx, v.ny, v.nz};
+    k_cp<<<(unsigned)((nt + 127) / 128), 128, 0, v.stream>>>(d_pos, d_idx, (long long)nt, v.macros, v.tipo, g, u_ref,
+                                                             d_cp);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(cp_out, d_cp, sizeof(float) * nt, cudaMemcpyDeviceToHost, v.stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(v.stream);
+  cudaFree(d_pos);
+  cudaFree(d_idx);
+  cudaFree(d_cp);
+  VCK(e, "surface Cp");
   return LBM_OK;
 }
 

@@ -161,3 +161,15 @@ class Esteiras:
             nat.check(self._lib.vis_esteiras_destroy(self._h))
             self._h = None
 
+
+def cp_superficie(solver, pos, idx, u_ref):
+    """Surface Cp per triangle of a mesh in lattice coordinates (the body
+    shader's sample, src/render/renderer.js:168-180, at each centroid), from
+    the solver's current macros."""
+    lib = nat.load()
+    p = np.ascontiguousarray(pos, np.float32).reshape(-1, 3)
+    t = np.ascontiguousarray(idx, np.uint32).reshape(-1, 3)
+    out = np.empty(t.shape[0], np.float32)
+    nat.check(lib.vis_cp_triangulos(solver._h, nat.ptr(p), p.shape[0], nat.ptr(t), t.shape[0], float(u_ref),
+                                    nat.ptr(out)))
+    return out

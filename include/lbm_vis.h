@@ -104,6 +104,15 @@ typedef struct {
  * domain give 0.  Synchronises. */
 int vis_fumaca_render(vis_fumaca* f, const vis_camera* cam, float* rgba, size_t n);
 
+/* Surface pressure coefficient of a triangle mesh (lattice coordinates), one
+ * value per triangle at its centroid, as the body shader samples it per
+ * fragment (src/render/renderer.js:168-180): the face normal
+ * n = normalize(cross(v1 - v0, v2 - v0)), the sample point c + 1.8 n (or
+ * c - 1.8 n when that cell is solid), Cp = delta / max(1.5 u_ref^2, 1e-12)
+ * from the nearest cell's macros.  Synchronises. */
+int vis_cp_triangulos(lbm_ctx* ctx, const float* pos, size_t nv, const uint32_t* idx, size_t nt, float u_ref,
+                      float* cp_out);
+
 #ifdef __cplusplus
 }
 #endif

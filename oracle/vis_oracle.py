@@ -244,3 +244,28 @@ def render(vol, inv_view_proj, olho, largura, altura, densidade, g, passos, pass
     img[..., 2] = np.where(hit, Lb, 0)
     img[..., 3] = np.where(hit, f32(1.0) - T, 0)
     return img
+
+
+def cp_triangulos(pos, idx, mac, tipo, u_ref):
+    """Surface Cp per triangle at its centroid (src/render/renderer.js:168-180)."""
+    nz, ny, nx = np.asarray(tipo).shape
+    p = np.asarray(pos, np.float32).reshape(-1, 3)
+    t = np.asarray(idx, np.int64).reshape(-1, 3)
+    v0, v1, v2 = p[t[:, 0]], p[t[:, 1]], p[t[:, 2]]
+    e1, e2 = v1 - v0, v2 - v0
+    n = np.stack([e1[:, 1] * e2[:, 2] - e1[:, 2] * e2[:, 1], e1[:, 2] * e2[:, 0] - e1[:, 0] * e2[:, 2],
+                  e1[:, 0] * e2[:, 1] - e1[:, 1] * e2[:, 0]], axis=1)
+    ln = np.sqrt(n[:, 0] * n[:, 0] + n[:, 1] * n[:, 1] + n[:, 2] * n[:, 2])
+    n = n / ln[:, None]
+    cen = ((v0 + v1) + v2) / f32(3.0)
+    fora = cen + n * f32(1.8)
+
+    def cell(q):
+        ix = np.clip(q[:, 0].astype(np.int64), 0, nx - 1)
+        iy = np.clip(q[:, 1].astype(np.int64), 0, ny - 1)
+        iz = np.clip(q[:, 2].astype(np.int64), 0, nz - 1)
+        return iz, iy, ix
+    solid = np.isin(np.asarray(tipo)[cell(fora)], [1, 4, 7])
+    fora = np.where(solid[:, None], cen - n * f32(1.8), fora)
+    delta = np.asarray(mac, np.float32)[cell(fora) + (3,)]
+    return delta / np.maximum(f32(1.5) * f32(u_ref) * f32(u_ref), f32(1e-12))

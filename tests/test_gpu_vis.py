@@ -148,3 +148,16 @@ def test_smoke_render_matches_oracle(native):
     assert np.abs(got - ref).max() < 2e-2
     f.destruir()
     s.destruir()
+
+
+def test_surface_cp_bit_exact(native):
+    from cfd__gb300.geometry import superelipsoide
+    from cfd__gb300.visual import cp_superficie
+    s, grade, tipo, mac = _state(47)
+    pos, idx = superelipsoide(6.0, 4.0, 3.0, 2.5, 3.0, 600, 0.0, 5)
+    pos = (pos + np.array([grade["nx"] * 0.35, grade["ny"] * 0.5, grade["nz"] * 0.5], np.float32)).astype(np.float32)
+    got = cp_superficie(s, pos, idx, 0.05)
+    ref = V.cp_triangulos(pos, idx, mac, tipo, 0.05)
+    assert got.shape == (idx.shape[0],) and np.isfinite(got).all()
+    assert np.array_equal(got, ref)
+    s.destruir()
