@@ -391,6 +391,7 @@ def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("study", choices=["precisao", "lote", "fecho"])
     ap.add_argument("--pesos", default=None, help="fecho: write the trained weights (.npz) here")
+    ap.add_argument("--cada", type=int, default=8, help="fecho: the held form's evaluation period (calibration)")
     ap.add_argument("--steps", type=int, default=10000)
     ap.add_argument("--grid", default="512,256,192")
     a = ap.parse_args(argv)
@@ -399,7 +400,7 @@ def main(argv=None):
     if a.study == "lote":
         r = lote(steps=a.steps)
     elif a.study == "fecho":
-        r = fecho(passos_finos=a.steps, pesos_saida=a.pesos)
+        r = fecho(passos_finos=a.steps, pesos_saida=a.pesos, cada=a.cada)
     else:
         r = precisao(a.steps, {"nx": nx, "ny": ny, "nz": nz})
     r["wall_s"] = time.time() - t0
