@@ -188,6 +188,19 @@ def cpu_voxelizer_ms():
     return (time.perf_counter() - t0) * 1e3
 
 
+def cpu_model():
+    """CPU model of the host, from /proc/cpuinfo (x86 'model name', Arm 'CPU part')."""
+    try:
+        txt = open("/proc/cpuinfo").read()
+    except OSError:
+        return "unknown"
+    for key in ("model name", "Model", "CPU part"):
+        for line in txt.splitlines():
+            if line.lower().startswith(key.lower()) and ":" in line:
+                return line.split(":", 1)[1].strip()
+    return "unknown"
+
+
 def cpu_measure(tipo, cfg, target_s=10.0, threads=None):
     """The oracle step on the host cores, bounded to ~target_s seconds."""
     from oracle import oracle as O
@@ -426,6 +439,9 @@ def run_ours(args):
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_measure(tipo, cfg, target_s=args.cpu_seconds)
         cpu.pop("seconds", None)
+        one = cpu_measure(tipo, cfg, target_s=max(2.0, args.cpu_seconds / 4), threads=1)
+        cpu["single_thread_MLUPS"] = one["value"]
+        cpu["cpu_model"] = cpu_model()
         if vox is not None:
             cpu["voxelizer_ms_1_thread"] = cpu_voxelizer_ms()
     if rank == 0:

@@ -196,3 +196,30 @@ def test_pipelined_step_equals_plain_step(native, storage, strict, kz):
         b.passo(n)
         fl = _fluid(tipo)
         assert np.array_equal(a.lerPopulacoes()[:, fl], b.lerPopulacoes()[:, fl]), (storage, strict, kz, a.passos)
+
+
+@pytest.mark.parametrize("dims", [(640, 320, 256), (512, 512, 440)])
+def test_largest_grids_keep_uniform_flow(native, dims):
+    """Size-independent check at the reference's largest preset (640x320x256,
+    src/backend/caps.js:75) and past the 2^31 population-index limit
+    (512x512x440: 19 N > 2^31, the 64-bit offset path): a uniform flow in a
+    periodic all-fluid box stays bit-identical in every cell (the property
+    tests/nucleo.html:107-130 checks), with the fp64 mass equal to N times
+    the common delta."""
+    from cfd__gb300 import SolverCUDA
+    nx, ny, nz = dims
+    N = nx * ny * nz
+    s = SolverCUDA({"nx": nx, "ny": ny, "nz": nz}, escrever_macros=False)
+    s.definirTipos(np.zeros(N, np.uint32))
+    s.configurar(omegaPlus=1.9, lesCs=0.1, inletU=[0.05, 0.01, -0.02], esponja={"inicio": nx + 10, "comprimento": 4})
+    s.inicializar()
+    s.passo(6)
+    s.atualizarMacros()
+    m = s.lerMacros().reshape(-1, 4)
+    for k in range(4):
+        assert m[:, k].min() == m[:, k].max(), k
+    np.testing.assert_allclose(m[0, :3], [0.05, 0.01, -0.02], rtol=1e-6)
+    assert abs(float(m[0, 3])) < 1e-6
+    mass = s.massa()                      # N identical deltas, summed in fp64
+    assert abs(mass - N * float(m[0, 3])) <= 1e-9 * max(1.0, abs(mass))
+    s.destruir()
