@@ -194,11 +194,13 @@ def cpu_model():
         txt = open("/proc/cpuinfo").read()
     except OSError:
         return "unknown"
-    for key in ("model name", "Model", "CPU part"):
+    for key in ("model name", "Model"):
         for line in txt.splitlines():
             if line.lower().startswith(key.lower()) and ":" in line:
                 return line.split(":", 1)[1].strip()
-    return "unknown"
+    parts = sorted({line.split(":", 1)[1].strip() for line in txt.splitlines() if line.startswith("CPU part")})
+    impl = sorted({line.split(":", 1)[1].strip() for line in txt.splitlines() if line.startswith("CPU implementer")})
+    return f"Arm CPU implementer {','.join(impl)} part {','.join(parts)}" if parts else "unknown"
 
 
 def cpu_measure(tipo, cfg, target_s=10.0, threads=None):
