@@ -89,6 +89,8 @@ SIGNATURES = {
     "lbm_get_populations": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "lbm_step": (C.c_int, [C.c_void_p, C.c_int]),
     "lbm_step_forces": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p]),
+    "lbm_step_forces_async": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.POINTER(C.c_int64)]),
+    "lbm_forces_done": (C.c_int, [C.c_void_p, C.c_int64, C.c_int, C.POINTER(C.c_int)]),
     "lbm_update_macros": (C.c_int, [C.c_void_p]),
     "lbm_read_macros": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "lbm_forces": (C.c_int, [C.c_void_p, C.c_void_p]),

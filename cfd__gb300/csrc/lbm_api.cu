@@ -68,6 +68,17 @@ __global__ void k_links(const uint8_t* __restrict__ tipo, uint32_t* __restrict__
 
 // Deterministic single-block sum of n triples: each thread walks a fixed
 // stride, then a fixed tree.  out[3].
+// Per step k: the kForceSlots copies of the fused force summed in slot order.
+__global__ void k_sum_slots(const double* __restrict__ slots, int n, double* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 3 * n) return;
+  const int k = i / 3, a = i % 3;
+  const double* h = slots + (size_t)k * 3 * kForceSlots;
+  double f = 0.0;
+  for (int q = 0; q < kForceSlots; ++q) f += h[3 * q + a];
+  out[i] = f;
+}
+
 __global__ void k_reduce3(const double* __restrict__ part, int64_t n, double* __restrict__ out) {
   __shared__ double sh[3][256];
   const int t = threadIdx.x;
@@ -125,6 +136,12 @@ struct lbm_ctx {
   double* stage = nullptr;     // N doubles for set/get
   double* hpin = nullptr;      // pinned host staging for force read-backs
   cudaEvent_t mac_evt = nullptr;   // completion of the last asynchronous macros read-back
+  // asynchronous force read-backs: a ring of events, one per ticket
+  static constexpr int kTickets = 16;
+  cudaEvent_t frc_evt[kTickets] = {};
+  int64_t frc_ticket = 0;          // last issued
+  double* fsum = nullptr;          // 3 doubles per step, summed on the device
+  int64_t fsum_cap = 0;
   int64_t hpin_cap = 0;        // in doubles
   cudaStream_t stream = nullptr;
   bool own_stream = false;
@@ -345,6 +362,9 @@ int lbm_destroy(lbm_ctx* c) {
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   if (c->hpin) cudaFreeHost(c->hpin);
   if (c->mac_evt) cudaEventDestroy(c->mac_evt);
+  for (int k = 0; k < lbm_ctx::kTickets; ++k)
+    if (c->frc_evt[k]) cudaEventDestroy(c->frc_evt[k]);
+  if (c->fsum) cudaFree(c->fsum);
   delete c;
   return LBM_OK;
 }
@@ -488,6 +508,66 @@ int lbm_step_forces(lbm_ctx* c, int n, double* out_f) {
     for (int a = 0; a < 3; ++a) out_f[3 * (size_t)k + a] = f[a];
   }
   return LBM_OK;
+}
+
+int lbm_step_forces_async(lbm_ctx* c, int n, double* out_f, int64_t* ticket) {
+  int r = check_ready(c, true);
+  if (r) return r;
+  if (n < 1 || !out_f || !ticket) return fail(LBM_EINVAL, "bad step count or null output");
+  const int64_t t = c->frc_ticket + 1;
+  const int slot = (int)(t % lbm_ctx::kTickets);
+  if (c->frc_evt[slot]) {
+    // the ticket that used this event 16 calls ago must have finished
+    const cudaError_t q = cudaEventQuery(c->frc_evt[slot]);
+    if (q == cudaErrorNotReady) { cudaGetLastError(); return fail(LBM_ESTATE, "16 asynchronous force read-backs already in flight"); }
+    if (q != cudaSuccess) return cuda_fail(q, "force event");
+  } else {
+    CK(cudaEventCreateWithFlags(&c->frc_evt[slot], cudaEventDisableTiming), "event create");
+  }
+  const bool want_mac = (c->flags & LBM_FLAG_WRITE_MACROS) != 0;
+  if (want_mac && (r = ensure_macros(c))) return r;
+  const size_t per = 3 * (size_t)kForceSlots;
+  if (c->fbuf_cap < n) {
+    if (c->fbuf) { cudaFree(c->fbuf); c->dev_bytes -= sizeof(double) * per * c->fbuf_cap; c->fbuf = nullptr; c->fbuf_cap = 0; }
+    r = dalloc(c, (void**)&c->fbuf, sizeof(double) * per * (size_t)n, "per-step forces");
+    if (r) return r;
+    c->fbuf_cap = n;
+  }
+  if (c->fsum_cap < n) {
+    if (c->fsum) { cudaFree(c->fsum); c->dev_bytes -= sizeof(double) * 3 * c->fsum_cap; c->fsum = nullptr; c->fsum_cap = 0; }
+    r = dalloc(c, (void**)&c->fsum, sizeof(double) * 3 * (size_t)n, "per-step force sums");
+    if (r) return r;
+    c->fsum_cap = n;
+  }
+  CK(cudaMemsetAsync(c->fbuf, 0, sizeof(double) * per * (size_t)n, c->stream), "force buffer clear");
+  for (int k = 0; k < n; ++k) {
+    r = launch_step(c, want_mac && k == n - 1, c->fbuf + per * (size_t)k);
+    if (r) return r;
+  }
+  k_sum_slots<<<(3 * n + 127) / 128, 128, 0, c->stream>>>(c->fbuf, n, c->fsum);
+  CK(cudaGetLastError(), "force sum launch");
+  CK(cudaMemcpyAsync(out_f, c->fsum, sizeof(double) * 3 * (size_t)n, cudaMemcpyDeviceToHost, c->stream),
+     "force download");
+  CK(cudaEventRecord(c->frc_evt[slot], c->stream), "event record");
+  c->frc_ticket = t;
+  *ticket = t;
+  return LBM_OK;
+}
+
+int lbm_forces_done(lbm_ctx* c, int64_t ticket, int wait, int* done) {
+  if (!c || !done) return fail(LBM_EINVAL, "null argument");
+  if (ticket < 1 || ticket > c->frc_ticket) return fail(LBM_EINVAL, "unknown ticket");
+  if (ticket <= c->frc_ticket - lbm_ctx::kTickets) { *done = 1; return LBM_OK; }   // older than the ring: finished
+  cudaEvent_t ev = c->frc_evt[ticket % lbm_ctx::kTickets];
+  if (wait) {
+    CK(cudaEventSynchronize(ev), "force read-back wait");
+    *done = 1;
+    return LBM_OK;
+  }
+  const cudaError_t q = cudaEventQuery(ev);
+  if (q == cudaSuccess) { *done = 1; return LBM_OK; }
+  if (q == cudaErrorNotReady) { cudaGetLastError(); *done = 0; return LBM_OK; }
+  return cuda_fail(q, "force read-back");
 }
 
 int lbm_update_macros(lbm_ctx* c) {

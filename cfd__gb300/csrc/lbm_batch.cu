@@ -88,7 +88,7 @@ __global__ void __launch_bounds__(kTile, 8) k_batch_step(const __grid_constant__
     const int z = rest / gy;
     const int x = bxi * tx + (int)(threadIdx.x % tx);
     const int y = byi * ty + (int)(threadIdx.x / tx);
-    if (x < D.d.nx && y < D.d.ny) step_cell<St, PAR, false, false, false, FAST>(D.d, D.P, D.U, x, y, z, nullptr, 0);
+    if (x < D.d.nx && y < D.d.ny) step_cell<St, PAR, false, false, false, FAST>(D.d, D.P, D.U, x, y, z);
   }
 }
 

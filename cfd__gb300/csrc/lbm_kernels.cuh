@@ -81,24 +81,18 @@ __device__ __forceinline__ int64_t eso_loc(int k, int p, int64_t cell, int x, in
 
 // Warp-level fp64 sum of three values; lane 0 adds them to dst atomically.
 // The fused force of one step accumulates into kForceSlots copies of
-// (fx, fy, fz), the block row picking the copy, so that the few thousand warps
-// that touch the body do not all serialise on the same three addresses; the
-// host sums the copies.
+// (fx, fy, fz), the block row picking the copy, so that the cells next to the
+// body do not all serialise on the same three addresses; the host (or
+// k_sum_slots) sums the copies.  Each such cell adds its own contribution
+// where it is computed: no value stays live through the collide and no warp
+// has to reconverge for a reduction.
 constexpr int kForceSlots = 32;
 
-__device__ __forceinline__ void warp_add3(double a, double b, double c, double* dst) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    a += __shfl_xor_sync(0xffffffffu, a, o);
-    b += __shfl_xor_sync(0xffffffffu, b, o);
-    c += __shfl_xor_sync(0xffffffffu, c, o);
-  }
-  if ((threadIdx.x & 31) == 0) {
-    double* slot = dst + 3 * ((blockIdx.y + blockIdx.z * gridDim.y) & (kForceSlots - 1));
-    atomicAdd(slot + 0, a);
-    atomicAdd(slot + 1, b);
-    atomicAdd(slot + 2, c);
-  }
+__device__ __forceinline__ void add_force(double* dst, double a, double b, double c) {
+  double* slot = dst + 3 * ((blockIdx.y + blockIdx.z * gridDim.y) & (kForceSlots - 1));
+  atomicAdd(slot + 0, a);
+  atomicAdd(slot + 1, b);
+  atomicAdd(slot + 2, c);
 }
 
 // ------------------------------------------------------------------ step
@@ -141,12 +135,10 @@ struct Deltas {
 // One cell of the in-place step (everything the step does for cell x, y, z).
 // Shared by the single-tunnel kernel and the batched kernel, so both run
 // the identical arithmetic.
-// FRC: the cell's momentum-exchange force is parked in shared memory
-// (park[0][t], park[1][t], park[2][t], volatile so it is not kept in
-// registers through the collide) for the warp reduction at the kernel's end.
+// FRC: the cell's momentum-exchange force goes to d.force (add_force).
 template <class St, int PAR, bool MAC, bool FRC, bool W64, bool FAST>
 __device__ __forceinline__ void step_cell(const Dev& d, const Params& P, const Uni<typename St::real>& U, int x, int y,
-                                          int z, volatile double (*park)[128], int t) {
+                                          int z) {
   double fx = 0.0, fy = 0.0, fz = 0.0;
   using R = typename St::real;
   using S = typename St::store_t;
@@ -208,7 +200,7 @@ __device__ __forceinline__ void step_cell(const Dev& d, const Params& P, const U
           }
         }
       }
-      if (FRC) { park[0][t] = fx; park[1][t] = fy; park[2][t] = fz; }
+      if (FRC && (fx != 0.0 || fy != 0.0 || fz != 0.0)) add_force(d.force, fx, fy, fz);
       R delta, rho, ux, uy, uz, uu, rinv = R(0.0);
       R sp[9], dp[9];
       if (FAST) moments_fast<R>(g, sp, dp, delta, rho, ux, uy, uz, uu, rinv);
@@ -231,23 +223,14 @@ __device__ __forceinline__ void step_cell(const Dev& d, const Params& P, const U
 
 // MINB: minimum resident 128-thread blocks per SM the register allocation
 // must allow (8 -> 64 registers, 6 -> 80); the autotuner picks per form.  The
-// fused force parks in shared memory, so the force variant fits 64 too.
+// fused force is added where it is computed, so the force variant fits 64 too.
 template <class St, int PAR, bool MAC, bool FRC, bool W64, bool FAST, int MINB>
 __global__ void __launch_bounds__(128, MINB)
 k_step_inplace(Dev d, Params P, Uni<typename St::real> U) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int z = blockIdx.z;
-  __shared__ double park[FRC ? 3 : 1][128];     // blocks have at most 128 threads
-  const int t = threadIdx.y * blockDim.x + threadIdx.x;
-  if (FRC) { park[0][t] = 0.0; park[1][t] = 0.0; park[2][t] = 0.0; }
-  if (x < d.nx && y < d.ny) step_cell<St, PAR, MAC, FRC, W64, FAST>(d, P, U, x, y, z, park, t);
-  if (FRC) {
-    const volatile double (*pk)[128] = park;
-    const double fx = pk[0][t], fy = pk[1][t], fz = pk[2][t];
-    const bool any = __any_sync(0xffffffffu, fx != 0.0 || fy != 0.0 || fz != 0.0);
-    if (any) warp_add3(fx, fy, fz, d.force);
-  }
+  if (x < d.nx && y < d.ny) step_cell<St, PAR, MAC, FRC, W64, FAST>(d, P, U, x, y, z);
 }
 
 // Arguments of the closure step.
@@ -365,6 +348,7 @@ k_step_closure(Dev d, Params P, Uni<float> U, CloArgs A) {
           }
         }
       }
+      if (FRC && (fx != 0.0 || fy != 0.0 || fz != 0.0)) add_force(d.force, fx, fy, fz);
       R sp[9], dp[9];
       moments_fast<R>(g, sp, dp, delta, rho, ux, uy, uz, uu, rinv);
       if (MAC) d.macros[cell] = make_float4(ux, uy, uz, delta);
@@ -451,10 +435,6 @@ k_step_closure(Dev d, Params P, Uni<float> U, CloArgs A) {
     if constexpr (ENG == 1)
       if (tid == 0 && SH.tc.err && A.err) atomicOr(A.err, 1u);
   }
-  if (FRC) {
-    const bool any = __any_sync(0xffffffffu, fx != 0.0 || fy != 0.0 || fz != 0.0);
-    if (any) warp_add3(fx, fy, fz, d.force);
-  }
 }
 
 // A/B ping-pong step: the reference's pull verbatim (tipo gathered per link).
@@ -506,10 +486,7 @@ __global__ void __launch_bounds__(128) k_step_ab(Dev d, Params P, Uni<typename S
                        [&](int i, R v) { St::st(dst + (int64_t)i * N + cell, v); });
     }
   }
-  if (FRC) {
-    const bool any = __any_sync(0xffffffffu, fx != 0.0 || fy != 0.0 || fz != 0.0);
-    if (any) warp_add3(fx, fy, fz, d.force);
-  }
+  if (FRC && (fx != 0.0 || fy != 0.0 || fz != 0.0)) add_force(d.force, fx, fy, fz);
 }
 
 // ------------------------------------------------------------------ init

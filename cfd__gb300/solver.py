@@ -187,6 +187,34 @@ class SolverCUDA:
         o = self.offsetForca if self.offsetForca is not None else [0.0, 0.0, 0.0]
         return f - np.asarray(o, dtype=np.float64)
 
+    def passoComForcasAssincrono(self, n, destino=None):
+        """passoComForcas enqueued (the reference's medirForcas is async):
+        returns a ticket at once; aguardarForcas(ticket) gives the n x 3
+        forces (rest offset subtracted) once they have landed.  destino:
+        3*n float64 the caller keeps alive (page-locked memory lets the copy
+        overlap the next steps)."""
+        if destino is None:
+            destino = np.empty(3 * n, dtype=np.float64)
+        t = C.c_int64()
+        nat.check(self._lib.lbm_step_forces_async(self._h, int(n), nat.ptr(destino), C.byref(t)))
+        self.passos += n
+        if not hasattr(self, "_forcas_async"):
+            self._forcas_async = {}
+        self._forcas_async[t.value] = destino
+        return t.value
+
+    def aguardarForcas(self, ticket, esperar=True):
+        """The n x 3 forces of an asynchronous call, or None if not landed
+        yet and esperar is False."""
+        d = C.c_int()
+        nat.check(self._lib.lbm_forces_done(self._h, int(ticket), 1 if esperar else 0, C.byref(d)))
+        if not d.value:
+            return None
+        destino = self._forcas_async.pop(ticket)
+        f = destino.reshape(-1, 3)
+        o = self.offsetForca if self.offsetForca is not None else [0.0, 0.0, 0.0]
+        return f - np.asarray(o, dtype=np.float64)
+
     # --------------------------------------------------------------- reading
     def lerMacros(self):
         """SolverWebGPU.lerMacros (src/backend/webgpu/solver.js:427-442):

@@ -153,6 +153,17 @@ int lbm_step(lbm_ctx* ctx, int n);
  * (3*n doubles, host).  One device->host copy at the end. */
 int lbm_step_forces(lbm_ctx* ctx, int n, double* out_f);
 
+/* The same, enqueued: returns at once with a ticket (> 0) in *ticket; out_f
+ * must stay valid until lbm_forces_done reports the ticket finished (with
+ * page-locked memory the copy overlaps the host and the next steps).  The
+ * asynchronous counterpart of medirForcas (an async method in the reference,
+ * src/backend/webgpu/solver.js:486-508).  Up to 16 calls may be in flight. */
+int lbm_step_forces_async(lbm_ctx* ctx, int n, double* out_f, int64_t* ticket);
+
+/* *done = 1 when the call that returned `ticket` has landed in its out_f;
+ * wait != 0 blocks until it has. */
+int lbm_forces_done(lbm_ctx* ctx, int64_t ticket, int wait, int* done);
+
 /* SolverWebGPU.atualizarMacros (src/backend/webgpu/solver.js:511-520) with
  * shaderMacros (src/core/emit/wgsl.js:442-476); solid cells report 0. */
 int lbm_update_macros(lbm_ctx* ctx);

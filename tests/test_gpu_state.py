@@ -115,3 +115,29 @@ def test_async_macros_match_sync(native):
     s.atualizarMacros()
     assert np.array_equal(dst, s.lerMacros().reshape(-1))
     s.destruir()
+
+
+def test_async_forces_match_sync(native):
+    """lbm_step_forces_async gives the forces lbm_step_forces gives, with
+    several calls in flight and tickets awaited out of order."""
+    from cfd__gb300._native import LbmError
+    grade, tipo, esp = all_types_tunnel()
+    g0 = random_state(int(np.prod(list(grade.values()))), seed=34)
+    a = _solver(grade, tipo, esp)
+    a.definirPopulacoes(g0)
+    ref = np.concatenate([a.passoComForcas(3), a.passoComForcas(1), a.passoComForcas(5)])
+    b = _solver(grade, tipo, esp)
+    b.definirPopulacoes(g0)
+    t1 = b.passoComForcasAssincrono(3)
+    t2 = b.passoComForcasAssincrono(1)
+    t3 = b.passoComForcasAssincrono(5)
+    f3 = b.aguardarForcas(t3)
+    f1 = b.aguardarForcas(t1, esperar=False)     # older than t3: landed
+    f2 = b.aguardarForcas(t2)
+    got = np.concatenate([f1, f2, f3])
+    np.testing.assert_allclose(got, ref, rtol=1e-12, atol=1e-15)
+    assert np.array_equal(a.lerPopulacoes(), b.lerPopulacoes())
+    with pytest.raises(LbmError, match="EINVAL"):
+        b.aguardarForcas(99)
+    a.destruir()
+    b.destruir()
