@@ -453,6 +453,20 @@ def run_ours(args):
             forms[st] = {"MLUPS": m2, "vs_f32": m2 / (mlups / world),
                          "roofline_frac": BYTES_PER_CELL[st] * N / (ms2 / args.steps / 1e3) / 1e9 / peak}
             s2.destruir()
+        # the step kernel's register-cap variants side by side (lbm_set_launch codes)
+        variants = {}
+        for st in ("f32", "f16s", "bf16s"):
+            row = {}
+            for name, code in (("64_registers", 8), ("80_registers", 6)):
+                s2 = make(st)
+                s2.definirBloco(64, code)
+                s2.passo(args.warmup)
+                ms2 = time_steps(s2, stream, args.steps)
+                row[name] = {"MLUPS": N * args.steps / (ms2 / 1e3) / 1e6,
+                             "roofline_frac": BYTES_PER_CELL[st] * N / (ms2 / args.steps / 1e3) / 1e9 / peak}
+                s2.destruir()
+            variants[st] = row
+        forms["step_variants"] = variants
         forms.update(closure_forms(make, stream, args.steps, args.warmup, ms_step, N))
         forms["visual"] = vis_timing(make, stream, N, peak)
 

@@ -140,7 +140,7 @@ __device__ __forceinline__ float fma_r<float>(float a, float b, float c) { retur
 // is used by FAST only.
 template <typename R, bool FAST>
 __device__ __forceinline__ R equilibrium(int i, R delta, R rho, R ux, R uy, R uz, R uu, R uu15) {
-  if (FAST) {
+  if constexpr (FAST) {
     if (i == 0) return Lit<R>::w(0) * fma_r<R>(-rho, uu15, delta);
     const R cu = dotc<R>(i, ux, uy, uz);
     const R a = fma_r<R>(cu, fma_r<R>(R(4.5), cu, R(3.0)), -uu15);
@@ -399,7 +399,7 @@ __device__ __forceinline__ void collide(const Params& P, const Uni<R>& U, uint32
     const R zc = R(z) + R(0.5);
     const R blf = zc < bl ? r_pow(zc / uInletBL, Lit<R>::bl_exp()) : R(1.0);
     const R ex = R(P.inlet[0]) * blf, ey = R(P.inlet[1]) * blf, ez = R(P.inlet[2]) * blf;
-    if (FAST) {
+    if constexpr (FAST) {
       const R uuIn = fma_r<R>(ez, ez, fma_r<R>(ey, ey, ex * ex));
       const R uu15 = R(1.5) * uuIn;
 #pragma unroll
@@ -419,7 +419,7 @@ __device__ __forceinline__ void collide(const Params& P, const Uni<R>& U, uint32
   const R uu15 = R(1.5) * uu;
   if (ct == SAIDA) {
     // blocoSaida with the pulled u (src/core/emit/ir.js:432-444, :512-515)
-    if (FAST) {
+    if constexpr (FAST) {
       emit(0, Lit<R>::w(0) * (-uu15));
 #pragma unroll
       for (int i = 1; i < Q; ++i) {
@@ -437,7 +437,7 @@ __device__ __forceinline__ void collide(const Params& P, const Uni<R>& U, uint32
     return;
   }
   // FLUIDO: equilibrium, Smagorinsky LES (src/core/emit/ir.js:262-301)
-  if (FAST) {
+  if constexpr (FAST) {
     R e0, ns[9], nd[9], omegaP, omegaM;
     fluid_neq_fast<R>(sp, dp, delta, rho, ux, uy, uz, uu, e0, ns, nd);
     smag_rates_fast<R>(P, U, ns, rinv, omegaP, omegaM);
