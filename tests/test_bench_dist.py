@@ -1,6 +1,7 @@
-"""The multi-rank host logic of bench.py on CPU: two gloo ranks reduce their
-step times to the slowest one (the value every rank then reports), and the
-reference arm's non-zero ranks leave without work."""
+"""The host logic of bench.py on CPU: two gloo ranks reduce their step times
+to the slowest one (the value every rank then reports), the reference arm's
+non-zero ranks leave without work, and its rank 0 prints the arm's JSON
+line."""
 import os
 import socket
 
@@ -58,3 +59,28 @@ def test_reference_arm_nonzero_rank_exits_without_work(monkeypatch):
         raise AssertionError("rank 1 must not build the workload")
     monkeypatch.setattr(bench, "workload", boom)
     assert bench.run_reference(A()) == 0
+
+
+def test_reference_arm_line_contract():
+    """`bench.py --impl reference` on rank 0 prints one JSON line with the
+    reference arm's contract: impl, the metric and unit of our arm, a value,
+    at least three warm-up steps, a cpu_baseline describing the run and an
+    e2e that moves no bytes between host and device."""
+    import json
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK")}
+    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "2", "--warmup", "1"],
+                       cwd=root, env=env, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["unit"] == "MLUPS" and d["metric"].startswith("MLUPS")
+    assert d["value"] > 0 and d["higher_is_better"] is True and d["steps"] == 2 and d["warmup"] >= 3
+    cb = d["cpu_baseline"]
+    assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["sample"] and cb["value"] == d["value"]
+    assert d["e2e"]["value"] == d["value"] and d["e2e"]["unit"] == d["unit"]
+    assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
+    assert d["config"]["workload"].startswith("320x160x128")
