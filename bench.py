@@ -1,18 +1,28 @@
 """Throughput of the D3Q19 wind-tunnel step on GB300 (MLUPS, % of HBM roofline).
 
-Default workload: the 320x160x128 mesh-body tunnel (6.55 M cells): no-slip
-floor (PAREDE), free-slip sides/top, equilibrium inlet, outlet + sponge, a
-seeded superellipsoid body; u_in = 0.06, Re 2000 on the 96-cell length
-(nu = 0.00288, omega+ = 1.98295), Smagorinsky Cs = 0.12, fp32 populations in
-the in-place layout.  One "step" = one D3Q19 step over every cell (MLUPS
-counts all nx*ny*nz cells, as the reference's tests/desempenho.html:67-70).
+Default workload (--grid 512x256x192): the precision workload, 25.2 M cells,
+a seeded superellipsoid mesh (semi-axes 80x32x22 cells, 20k triangles,
+0.3-cell jitter) voxelized on the GPU, free-slip walls, equilibrium inlet,
+outlet + sponge, u_in 0.05, nu 0.008 (omega+ 1.9084), Smagorinsky Cs 0.1.
+`value` is the fp32 step; the fp16 (g * 2^10) and bf16 storage forms are
+timed beside it, with the Cd and velocity errors against the fp64 run that
+the precision study recorded (results/precisao_512x256x192.json).
+--grid 320x160x128 selects the mesh-body tunnel (no-slip floor, u_in 0.06,
+Re 2000, Cs 0.12), where the learned closure and the visualisation compute
+are also timed.  One "step" = one D3Q19 step over every cell (MLUPS counts
+all nx*ny*nz cells, as the reference's tests/desempenho.html:67-70).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--grid 512x256x192|320x160x128] [--storage f32|f16s|bf16s|f64]
+
+Timing: W + 2W untimed warm-up steps, then K steps between CUDA events on
+the solver's stream, repeated R >= 5 times so the repeats span at least a
+second; the median is reported.
 
 --impl reference times the reference's step on the host cores instead: the
 reference has no runnable CPU step of its own (its step exists only as
 generated WGSL/GLSL), so that arm runs the CPU restatement in oracle/ with all
-host threads on a bounded sample of the same workload.
+host threads on the same workload.
 
 Multi-GPU: the tunnel does not shard here (replicas only): every rank runs its
 own copy and `value` sums the ranks' cells (weak scaling).
@@ -34,36 +44,25 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-GRID = {"nx": 320, "ny": 160, "nz": 128}
-U_IN, RE, LEN, CS = 0.06, 2000.0, 96.0, 0.12
+# The metric string both arms print (the driver compares the two lines).
+METRIC = "MLUPS & % HBM roofline on 1 GB300, FP16-store vs FP32 plain, Cd err \u22641% vs FP64"
+from cfd__gb300.cargas import GRIDS  # noqa: E402
+
+GRID = GRIDS["320x160x128"]
 BYTES_PER_CELL = {"f32": 152, "f16s": 76, "bf16s": 76, "f64": 304}
 
 
-def workload(body="mesh", cpu_voxelizer=False):
-    """Cell types and parameters of the 320x160x128 mesh-body tunnel.  The
-    reference arm voxelizes with the CPU restatement, ours on the GPU (the
-    two give identical masks)."""
-    from cfd__gb300.tunel import montarTipos
+def oracle_voxelizer(pos, idx, grade):
+    from oracle import oracle as O
+    return O.voxelize(pos, idx, (grade["nx"], grade["ny"], grade["nz"]), with_sdf=False)[0]
 
-    nu = U_IN * LEN / RE
-    omega = 1.0 / (3.0 * nu + 0.5)
-    if body == "mesh":
-        from cfd__gb300.geometry import corpo_config2
-        pos, idx = corpo_config2(GRID)
-        if cpu_voxelizer:
-            from oracle import oracle as O
-            corpo = O.voxelize(pos, idx, (GRID["nx"], GRID["ny"], GRID["nz"]), with_sdf=False)[0]
-        else:
-            from cfd__gb300.voxel import voxelizar
-            corpo = voxelizar(pos, idx, GRID, sdf=False)["tipo"]
-        desc = "voxelized superellipsoid mesh 48x20x14 cells, 20k triangles, 0.3-cell jitter"
-    else:
-        from cfd__gb300.geometry import mascara_analitica
-        corpo = mascara_analitica(GRID, 48, 20, 14, 2.5, 3.0, (0.28 * 320 + 48, 80, 3 + 14))
-        desc = "analytic superellipsoid 48x20x14 cells"
-    mt = montarTipos(GRID, corpo=corpo, esteira=False)
-    cfg = dict(omegaPlus=omega, lesCs=CS, inletU=[U_IN, 0.0, 0.0], beltU=[0.0, 0.0, 0.0], esponja=mt["esponja"])
-    return mt["tipo"], cfg, desc
+
+def workload(grid="512x256x192", cpu_voxelizer=False):
+    """(cell types, solver parameters, description) of a bench workload
+    (cfd__gb300/cargas.py).  The reference arm voxelizes with the CPU
+    restatement, ours on the GPU (the two give identical masks)."""
+    from cfd__gb300.cargas import carga
+    return carga(grid, oracle_voxelizer if cpu_voxelizer else None)
 
 
 def peaks():
@@ -75,9 +74,10 @@ def peaks():
     return 6800.0, "fallback 6.8 TB/s"
 
 
-def ncu_traffic(kernel="k_step_inplace", workload_key="320x160x128"):
-    """Per-launch DRAM bytes of the step kernel from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "lbm_step_f32_320x160x128.md")
+def ncu_traffic(storage="f32", grid="512x256x192"):
+    """Per-launch DRAM bytes (read + write) of the step kernel, from the
+    committed ncu summary of the same storage form and grid."""
+    p = os.path.join(ROOT, "profiles", f"lbm_step_{storage}_{grid}.md")
     if not os.path.exists(p):
         return None
     for line in open(p):
@@ -87,6 +87,20 @@ def ncu_traffic(kernel="k_step_inplace", workload_key="320x160x128"):
             except ValueError:
                 return None
     return None
+
+
+def precision_study(grid):
+    """The recorded result of the precision study (Cd and velocity error of
+    each storage form against the fp64 run), if one is committed."""
+    p = os.path.join(ROOT, "results", f"precisao_{grid}.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    out = {"recorded": True, "source": d.get("command"), "steps": d.get("steps"), "forms": {}}
+    for k, v in d.get("forms", {}).items():
+        out["forms"][k] = {kk: v[kk] for kk in ("cd", "cd_err_vs_f64", "u_l2_rel_err_vs_f64") if kk in v}
+    return out
 
 
 class Clocks:
@@ -203,15 +217,22 @@ def cpu_model():
     return f"Arm CPU implementer {','.join(impl)} part {','.join(parts)}" if parts else "unknown"
 
 
-def cpu_measure(tipo, cfg, target_s=10.0, threads=None):
-    """The oracle step on the host cores, bounded to ~target_s seconds."""
+def _oracle_lattice(grade, tipo, cfg, threads):
     from oracle import oracle as O
-    threads = threads or (os.cpu_count() or 1)
-    lat = O.Lattice((GRID["nx"], GRID["ny"], GRID["nz"]), nthreads=threads)
+    lat = O.Lattice((grade["nx"], grade["ny"], grade["nz"]), nthreads=threads)
     lat.set_types(tipo)
     lat.configure(omega_plus=cfg["omegaPlus"], les_cs=cfg["lesCs"], inlet_u=cfg["inletU"], belt_u=cfg["beltU"],
-                  sponge_start=cfg["esponja"]["inicio"], sponge_len=cfg["esponja"]["comprimento"])
+                  sponge_start=cfg["esponja"]["inicio"], sponge_len=cfg["esponja"]["comprimento"],
+                  bl_thickness=cfg.get("espessuraCL", 0.0))
     lat.init()
+    return lat
+
+
+def cpu_measure(grid, tipo, cfg, target_s=10.0, threads=None):
+    """The oracle step on the host cores, bounded to ~target_s seconds."""
+    threads = threads or (os.cpu_count() or 1)
+    grade = GRIDS[grid]
+    lat = _oracle_lattice(grade, tipo, cfg, threads)
     lat.run(1)  # warm-up
     t0 = time.perf_counter()
     lat.run(1)
@@ -220,37 +241,53 @@ def cpu_measure(tipo, cfg, target_s=10.0, threads=None):
     t0 = time.perf_counter()
     lat.run(n)
     dt = time.perf_counter() - t0
-    N = GRID["nx"] * GRID["ny"] * GRID["nz"]
+    N = int(tipo.size)
     return {"value": N * n / dt / 1e6, "unit": "MLUPS", "cores": threads, "kind": "port",
-            "sample": f"{n} steps of the 320x160x128 tunnel (fp32 oracle restatement, OpenMP)", "seconds": dt}
+            "sample": f"{n} full steps of the {grid} tunnel (fp32 oracle restatement, {threads} threads)",
+            "seconds": dt}
 
 
 def run_reference(args):
+    """The reference's step on the host cores.  The reference has no CPU step
+    of its own (its step exists only as generated WGSL/GLSL for a browser
+    GPU), so this arm times the CPU restatement in oracle/ on all host
+    threads: W untimed warm-up steps, then up to K timed steps of the same
+    workload (fewer when K steps would take over a minute; the line says how
+    many)."""
     world, rank, local = dist_setup()
     if rank != 0:
         return 0
-    tipo, cfg, desc = workload(body=args.body, cpu_voxelizer=True)
-    res = []
-    for _ in range(args.warmup):
-        pass
-    for _ in range(max(1, args.steps)):
-        res.append(cpu_measure(tipo, cfg, target_s=max(2.0, 20.0 / max(1, args.steps))))
-    v = statistics.median(r["value"] for r in res)
+    threads = os.cpu_count() or 1
+    tipo, cfg, desc = workload(args.grid, cpu_voxelizer=True)
+    grade = GRIDS[args.grid]
+    N = int(tipo.size)
+    lat = _oracle_lattice(grade, tipo, cfg, threads)
+    t0 = time.perf_counter()
+    lat.run(args.warmup)
+    per = (time.perf_counter() - t0) / max(1, args.warmup)
+    k = max(1, min(args.steps, int(60.0 / max(per, 1e-6))))
+    t0 = time.perf_counter()
+    lat.run(k)
+    dt = time.perf_counter() - t0
+    v = N * k / dt / 1e6
+    sample = f"{k} of the requested {args.steps} steps of the {args.grid} tunnel after {args.warmup} warm-up steps"
     line = {
-        "impl": "reference", "metric": "MLUPS (D3Q19 TRT+LES step, fp32)", "value": v, "unit": "MLUPS",
-        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"320x160x128 tunnel, {desc}", "cells": int(tipo.size)},
-        "cpu_baseline": {k: res[0][k] for k in ("kind", "cores", "sample")} | {"value": v, "unit": "MLUPS"},
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "MLUPS",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / k * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": desc, "cells": N, "storage": "f32"},
+        "cpu_baseline": {"kind": "port", "cores": threads, "sample": sample, "value": v, "unit": "MLUPS",
+                         "cpu_model": cpu_model()},
         "e2e": {"value": v, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference's step exists only as generated WGSL/GLSL for a browser GPU; this arm times its "
-                "CPU restatement (oracle/) on all host threads",
+                "CPU restatement (oracle/, fp32, A/B ping-pong) on all host threads",
     }
     print(json.dumps(line))
     return 0
 
 
 def time_steps(s, stream, K):
+    """K steps bracketed by CUDA events on the solver's stream (ms)."""
     import torch
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -260,6 +297,20 @@ def time_steps(s, stream, K):
     e1.record(stream)
     e1.synchronize()
     return e0.elapsed_time(e1)
+
+
+def timed(s, stream, K, barrier=None, min_total_ms=1000.0, min_repeats=5):
+    """K steps timed R >= min_repeats times, R large enough that the timed
+    repeats span at least min_total_ms: (median ms of K steps, R)."""
+    first = time_steps(s, stream, K)
+    R = max(min_repeats, int(math.ceil(min_total_ms / max(first, 1e-3))))
+    R = min(R, 5000)
+    times = []
+    for _ in range(R):
+        if barrier:
+            barrier()
+        times.append(time_steps(s, stream, K))
+    return statistics.median(times), R
 
 
 def reduce_max(value, world, device="cpu"):
@@ -273,7 +324,7 @@ def reduce_max(value, world, device="cpu"):
     return float(t.item())
 
 
-def closure_forms(make, stream, steps, warmup, ms_plain, N):
+def closure_forms(make, stream, steps, N, ms_plain):
     """Step time of the learned closure (coefficient form, weights trained by
     `python -m cfd__gb300.estudos fecho`) evaluated every step, every 8th and
     every 16th step (warp engine) and every step on the CTA tcgen05 engine,
@@ -284,21 +335,21 @@ def closure_forms(make, stream, steps, warmup, ms_plain, N):
     for every, motor in ((1, 0), (8, 0), (16, 0), (1, 1)):
         s = make("f32", closure=every, pesos=p)
         s.motorFecho(motor)
-        s.passo(warmup)
-        ms = time_steps(s, stream, steps)
+        s.passo(16)
+        ms, R = timed(s, stream, steps, min_total_ms=500.0)
         fb, fl = s.estatisticasFecho()
         name = f"closure_every_{every}" + ("_tcgen05" if motor else "")
         out[name] = {"MLUPS": N * steps / (ms / 1e3) / 1e6, "overhead_vs_smagorinsky": (ms / steps) / ms_plain - 1.0,
-                     "fallback_rate": fb / max(fl, 1),
+                     "fallback_rate": fb / max(fl, 1), "repeats": R,
                      "engine": "CTA tcgen05.mma, TMEM accumulators" if motor else "warp mma.sync"}
         s.destruir()
     return out
 
 
 def vis_timing(make, stream, N, peak):
-    """Visualisation compute on the bench tunnel (include/lbm_vis.h): one smoke
-    step (back-trace + MacCormack, fp16 volume; algorithmic bytes per voxel:
-    2 x 16 B macros + 2 x 1 B types + 2 B current x 3 reads + 2 B
+    """Visualisation compute on the 320x160x128 tunnel (include/lbm_vis.h): one
+    smoke step (back-trace + MacCormack, fp16 volume; algorithmic bytes per
+    voxel: 2 x 16 B macros + 2 x 1 B types + 2 B current x 3 reads + 2 B
     intermediate write + read + 2 B next write = 44 B), a 640x360 ray-march
     of the volume, and one frame of 65 536 streak particles in 8 sub-steps."""
     import torch
@@ -364,24 +415,25 @@ def run_ours(args):
     from cfd__gb300 import build as B
 
     B.build()
-    tipo, cfg, desc = workload(body=args.body)
+    grade = GRIDS[args.grid]
+    tipo, cfg, desc = workload(args.grid)
     N = int(tipo.size)
     stream = torch.cuda.Stream()
-    vox = voxelizer_timing() if args.body == "mesh" else None
+    vox = voxelizer_timing() if not args.no_forms else None
 
-    def make(storage, closure=0, pesos=None):
-        s = SolverCUDA(GRID, storage=storage, escrever_macros=False)
-        s.definirStream(stream.cuda_stream)
-        s.definirTipos(tipo)
-        s.configurar(**cfg, closure=closure)
-        if pesos is not None:
-            s.definirFecho(pesos)
-        s.inicializar()
-        return s
+    def maker(tp, cf, gr):
+        def make(storage, closure=0, pesos=None):
+            s = SolverCUDA(gr, storage=storage, escrever_macros=False)
+            s.definirStream(stream.cuda_stream)
+            s.definirTipos(tp)
+            s.configurar(**cf, closure=closure)
+            if pesos is not None:
+                s.definirFecho(pesos)
+            s.inicializar()
+            return s
+        return make
 
-    s = make(args.storage)
-    s.passo(args.warmup)
-    torch.cuda.synchronize()
+    make = maker(tipo, cfg, grade)
 
     def barrier():
         if world > 1:
@@ -389,13 +441,17 @@ def run_ours(args):
             dist.barrier()
         torch.cuda.synchronize()
 
+    peak, peak_src = peaks()
+    s = make(args.storage)
+    s.passo(args.warmup)
+    torch.cuda.synchronize()
     with Clocks(local) as clk:
         s.passo(2 * args.warmup)        # keeps the GPU busy while the sampler starts
         time.sleep(0.3)
         barrier()
         clk.start()
         t0 = time.perf_counter()
-        ms = time_steps(s, stream, args.steps)
+        ms, R = timed(s, stream, args.steps, barrier=barrier)
         wall = time.perf_counter() - t0
         clk.stop()
     barrier()
@@ -404,17 +460,16 @@ def run_ours(args):
     mlups = N * args.steps / (ms / 1e3) / 1e6 * world
 
     # roofline of the step kernel (one launch per step)
-    peak, peak_src = peaks()
     bpc = BYTES_PER_CELL[args.storage]
     achieved = bpc * N / (ms_step / 1e3) / 1e9
-    traffic = ncu_traffic()
+    traffic = ncu_traffic(args.storage, args.grid)
 
     # end to end through the public API: every step configures (parameters by
     # value in the launch) and its force (24 B) comes back to the host.  The
     # reference's medirForcas is asynchronous; the pipelined form reads step
     # k's force while step k+1 runs (page-locked double buffer), the
     # synchronous form waits for every step.
-    E = max(20, args.steps // 4)
+    E = max(200, min(2000, int(2000.0 / max(ms_step, 1e-3))))
     import torch as _t
     bufs = [_t.empty(3, dtype=_t.float64, pin_memory=True).numpy() for _ in range(2)]
     s.passoComForcas(1)
@@ -448,11 +503,14 @@ def run_ours(args):
         for st in ("f16s", "bf16s"):
             s2 = make(st)
             s2.passo(args.warmup)
-            ms2 = time_steps(s2, stream, args.steps)
+            ms2, R2 = timed(s2, stream, args.steps)
             m2 = N * args.steps / (ms2 / 1e3) / 1e6
-            forms[st] = {"MLUPS": m2, "vs_f32": m2 / (mlups / world),
-                         "roofline_frac": BYTES_PER_CELL[st] * N / (ms2 / args.steps / 1e3) / 1e9 / peak}
+            a2 = BYTES_PER_CELL[st] * N / (ms2 / args.steps / 1e3) / 1e9
+            forms[st] = {"MLUPS": m2, "vs_f32": m2 / (mlups / world), "repeats": R2,
+                         "roofline": {"bound": "hbm", "achieved": a2, "peak": peak, "unit": "GB/s", "frac": a2 / peak,
+                                      "traffic": ncu_traffic(st, args.grid), "algorithmic_bytes_per_cell": 76}}
             s2.destruir()
+        forms["precision_study"] = precision_study(args.grid)
         # the step kernel's register-cap variants side by side (lbm_set_launch codes)
         variants = {}
         for st in ("f32", "f16s", "bf16s"):
@@ -461,42 +519,56 @@ def run_ours(args):
                 s2 = make(st)
                 s2.definirBloco(64, code)
                 s2.passo(args.warmup)
-                ms2 = time_steps(s2, stream, args.steps)
+                ms2, _ = timed(s2, stream, args.steps, min_total_ms=300.0)
                 row[name] = {"MLUPS": N * args.steps / (ms2 / 1e3) / 1e6,
                              "roofline_frac": BYTES_PER_CELL[st] * N / (ms2 / args.steps / 1e3) / 1e9 / peak}
                 s2.destruir()
             variants[st] = row
         forms["step_variants"] = variants
-        forms.update(closure_forms(make, stream, args.steps, args.warmup, ms_step, N))
-        forms["visual"] = vis_timing(make, stream, N, peak)
+        # the mesh-body tunnel: its plain step, the learned closure (trained
+        # on that tunnel's body) and the visualisation compute
+        g2 = GRIDS["320x160x128"]
+        tipo2, cfg2, desc2 = workload("320x160x128")
+        N2 = int(tipo2.size)
+        make2 = maker(tipo2, cfg2, g2)
+        s2 = make2("f32")
+        s2.passo(args.warmup)
+        ms2, R2 = timed(s2, stream, args.steps)
+        s2.destruir()
+        forms["f32_320x160x128"] = {"MLUPS": N2 * args.steps / (ms2 / 1e3) / 1e6, "workload": desc2, "repeats": R2,
+                                    "roofline_frac": 152 * N2 / (ms2 / args.steps / 1e3) / 1e9 / peak}
+        forms.update(closure_forms(make2, stream, args.steps, N2, ms2 / args.steps))
+        forms["visual"] = vis_timing(make2, stream, N2, peak)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        cpu = cpu_measure(tipo, cfg, target_s=args.cpu_seconds)
+        cpu = cpu_measure(args.grid, tipo, cfg, target_s=args.cpu_seconds)
         cpu.pop("seconds", None)
-        one = cpu_measure(tipo, cfg, target_s=max(2.0, args.cpu_seconds / 4), threads=1)
+        one = cpu_measure(args.grid, tipo, cfg, target_s=max(2.0, args.cpu_seconds / 4), threads=1)
         cpu["single_thread_MLUPS"] = one["value"]
         cpu["cpu_model"] = cpu_model()
         if vox is not None:
-            cpu["voxelizer_ms_1_thread"] = cpu_voxelizer_ms()
+            cpu["voxelizer_320x160x128_ms_1_thread"] = cpu_voxelizer_ms()
     if rank == 0:
         line = {
-            "metric": "MLUPS (D3Q19 TRT+LES step, fp32 plain; 16-bit storage and learned-closure forms beside it)",
+            "metric": METRIC,
             "value": mlups, "unit": "MLUPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "ms_per_step": ms_step, "repeats": R, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": {"f32": "f32", "f16s": "f16 storage / f32 math", "bf16s": "bf16 storage / f32 math",
                       "f64": "f64"}[args.storage],
             "data": "synthetic",
-            "config": {"workload": f"320x160x128 tunnel, {desc}, u_in 0.06, Re 2000, Cs 0.12",
-                       "cells": N, "storage": args.storage, "layout": "in-place (esoteric pull)",
+            "config": {"workload": desc, "cells": N, "storage": args.storage, "layout": "in-place (esoteric pull)",
                        "parallelism": "replicas" if world > 1 else "single",
+                       "timing": f"median of {R} timed repeats of {args.steps} steps (CUDA events on the solver's "
+                                 f"stream), {args.warmup} + {2 * args.warmup} warm-up steps",
                        "l2": f"state {N * 19 * (bpc // 38) / 1e6:.0f} MB > 126 MB L2 (inputs larger than L2)"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
                          "kernel": "k_step_inplace", "algorithmic_bytes_per_cell": bpc},
             "cpu_baseline": cpu,
             "e2e": e2e,
-            "gpu_launches": args.steps,
+            "gpu_launches": args.steps * R,
+            "gpu_launches_note": f"{args.steps} step kernels per timed repeat, {R} repeats",
             "clocks": clk.summary(),
             "forms": forms,
             "voxelizer": vox,
@@ -512,11 +584,11 @@ def run_ours(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3000)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=40)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--storage", default="f32", choices=["f32", "f16s", "bf16s", "f64"])
-    ap.add_argument("--body", default="mesh", choices=["mesh", "analytic"])
+    ap.add_argument("--grid", default="512x256x192", choices=sorted(GRIDS))
     ap.add_argument("--no-forms", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)

@@ -4,10 +4,10 @@ Compiles every translation unit under cfd__gb300/csrc with nvcc in parallel
 and links cfd__gb300/_native/libcfdgb300.so.  No cmake, no torch extension
 machinery: plain nvcc, one -gencode (compute_103a/sm_103a).
 
-The lattice-Boltzmann units are built with -fmad=false and IEEE division and
-square root so each fp32 operation rounds where the reference's shader text
-writes it (bit-parity with the CPU oracle).  Units that do not restate the
-reference's arithmetic (learned closure, voxelizer prefilter) keep FMA.
+Every unit is built with -fmad=false and IEEE division and square root, so
+each fp32 operation rounds where the source writes it: the lattice-Boltzmann
+units then match the CPU oracle bit for bit, and the others (learned closure,
+voxelizer, visualisation) fuse a multiply-add only where they call fmaf().
 """
 from __future__ import annotations
 

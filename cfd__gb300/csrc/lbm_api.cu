@@ -114,6 +114,26 @@ cudaError_t launch_reduce3(const double* part, int64_t n, double* out, cudaStrea
   k_reduce3<<<1, 256, 0, s>>>(part, n, out);
   return cudaGetLastError();
 }
+// The nz inlet boundary-layer factors of thickness bl in the arithmetic type
+// of the storage form (double for the fp64 reference form, else float), as
+// raw bytes; returns whether any factor differs from 1.
+bool bl_table(float bl, int nz, bool f64, std::vector<unsigned char>& out) {
+  const size_t el = f64 ? sizeof(double) : sizeof(float);
+  out.assign(el * (size_t)nz, 0);
+  bool any = false;
+  for (int z = 0; z < nz; ++z) {
+    if (f64) {
+      const double v = bl_factor_host<double>(bl, z);
+      any |= v != 1.0;
+      memcpy(out.data() + el * z, &v, el);
+    } else {
+      const float v = bl_factor_host<float>(bl, z);
+      any |= v != 1.0f;
+      memcpy(out.data() + el * z, &v, el);
+    }
+  }
+  return any;
+}
 }  // namespace lbm
 
 struct lbm_ctx {
@@ -128,6 +148,10 @@ struct lbm_ctx {
   uint8_t* tipo = nullptr;
   uint32_t* link = nullptr;
   float4* macros = nullptr;
+  void* blf = nullptr;         // nz inlet boundary-layer factors (arithmetic type)
+  bool blf_on = false;         // some factor differs from 1
+  bool blf_set = false;        // blf holds the factors of thickness blf_bl
+  float blf_bl = 0.0f;
   double* partials = nullptr;
   int64_t npart = 0;
   double* red = nullptr;       // 3 doubles
@@ -206,6 +230,7 @@ Dev dev_of(const lbm_ctx* c) {
   d.tipo = c->tipo; d.link = c->link;
   d.macros = c->macros;
   d.force = nullptr;
+  d.blf = c->blf_on ? c->blf : nullptr;
   return d;
 }
 
@@ -337,6 +362,7 @@ int lbm_create(const lbm_dims* dims, int storage, int flags, lbm_ctx** out) {
   if (!r) r = dalloc(c, (void**)&c->tipo, (size_t)c->N, "cell types");
   if (!r && c->inplace) r = dalloc(c, (void**)&c->link, sizeof(uint32_t) * (size_t)c->N, "link words");
   if (!r) r = dalloc(c, (void**)&c->red, 3 * sizeof(double), "reduction result");
+  if (!r) r = dalloc(c, &c->blf, sizeof(double) * (size_t)dims->nz, "inlet boundary-layer factors");
   if (!r && (flags & LBM_FLAG_WRITE_MACROS)) r = ensure_macros(c);
   if (r) { lbm_destroy(c); return r; }
   cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
@@ -356,7 +382,7 @@ int lbm_destroy(lbm_ctx* c) {
   if (!c) return fail(LBM_EINVAL, "null context");
   if (c->stream) cudaStreamSynchronize(c->stream);
   void* ps[] = {c->pop, c->pop2, c->tipo, c->link, c->macros, c->partials, c->red, c->fbuf, c->stage, c->clo, c->clo_fb,
-                c->clo_nu};
+                c->clo_nu, c->blf};
   for (void* p : ps)
     if (p) cudaFree(p);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -386,6 +412,19 @@ int lbm_configure(lbm_ctx* c, const lbm_params* p) {
   for (int a = 0; a < 3; ++a) { P.belt[a] = p->belt_u[a]; P.inlet[a] = p->inlet_u[a]; }
   P.sponge_start = p->sponge_start; P.sponge_len = p->sponge_len; P.bl = p->bl_thickness;
   P.closure = p->closure;
+  // The boundary-layer table depends on the thickness alone: rebuilt only
+  // when it changes (a ramp re-configures the inlet before every step).
+  if (!c->blf_set || memcmp(&c->blf_bl, &p->bl_thickness, sizeof(float)) != 0) {
+    std::vector<unsigned char> tab;
+    const bool on = bl_table(p->bl_thickness, c->dims.nz, c->storage == LBM_F64, tab);
+    if (on) {
+      CK(cudaMemcpyAsync(c->blf, tab.data(), tab.size(), cudaMemcpyHostToDevice, c->stream), "boundary-layer table upload");
+      CK(cudaStreamSynchronize(c->stream), "boundary-layer table upload sync");
+    }
+    c->blf_on = on;
+    c->blf_bl = p->bl_thickness;
+    c->blf_set = true;
+  }
   c->P = P;
   c->configured = true;
   c->clo_since = -1;

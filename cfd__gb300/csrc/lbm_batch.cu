@@ -31,6 +31,7 @@ extern "C" int lbm_internal_fail(int code, const char* msg);
 namespace lbm {
 cudaError_t launch_links(const uint8_t* tipo, uint32_t* link, int nx, int ny, int nz, cudaStream_t s);
 cudaError_t launch_reduce3(const double* part, int64_t n, double* out, cudaStream_t s);
+bool bl_table(float bl, int nz, bool f64, std::vector<unsigned char>& out);
 }  // namespace lbm
 
 using namespace lbm;
@@ -143,6 +144,7 @@ struct lbm_batch {
   std::vector<cudaStream_t> lanes;   // capture-time streams, one per tunnel (mode 0)
   cudaEvent_t fork = nullptr;
   std::vector<cudaEvent_t> joins;
+  std::vector<void*> blf;            // per tunnel: nz inlet boundary-layer factors
 };
 
 namespace {
@@ -315,6 +317,8 @@ int lbm_batch_create(const lbm_dims* dims, int ntunnels, int storage, int flags,
     D.d.tipo = static_cast<uint8_t*>(p);
     if ((r = balloc(b, &p, sizeof(uint32_t) * (size_t)N, "link words"))) break;
     D.d.link = static_cast<uint32_t*>(p);
+    if ((r = balloc(b, &p, sizeof(float) * (size_t)d.nz, "inlet boundary-layer factors"))) break;
+    b->blf.push_back(p);
     b->cells += N;
   }
   void* p = nullptr;
@@ -373,8 +377,15 @@ int lbm_batch_configure(lbm_batch* b, int k, const lbm_params* p) {
   for (int a = 0; a < 3; ++a) { P.belt[a] = p->belt_u[a]; P.inlet[a] = p->inlet_u[a]; }
   P.sponge_start = p->sponge_start; P.sponge_len = p->sponge_len; P.bl = p->bl_thickness;
   P.closure = p->closure;
+  std::vector<unsigned char> tab;
+  const bool on = bl_table(p->bl_thickness, b->host[k].d.nz, false, tab);
+  if (on) {
+    BCK(cudaMemcpyAsync(b->blf[k], tab.data(), tab.size(), cudaMemcpyHostToDevice, b->stream), "boundary-layer table");
+    BCK(cudaStreamSynchronize(b->stream), "boundary-layer table sync");
+  }
+  b->host[k].d.blf = on ? b->blf[k] : nullptr;
   b->host[k].P = P;
-  b->host[k].U = make_uni<float>(P);
+  b->host[k].U = make_uni<float>(P, b->storage == LBM_F16S ? StF16S::kScale : 1.0f);
   b->configured[k] = true;
   b->desc_dirty = true;
   return LBM_OK;

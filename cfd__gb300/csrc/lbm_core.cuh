@@ -79,8 +79,21 @@ template <> struct Lit<double> {
 
 __device__ __forceinline__ float r_sqrt(float v) { return sqrtf(v); }
 __device__ __forceinline__ double r_sqrt(double v) { return sqrt(v); }
-__device__ __forceinline__ float r_pow(float a, float b) { return powf(a, b); }
-__device__ __forceinline__ double r_pow(double a, double b) { return pow(a, b); }
+
+// Inlet boundary-layer factor of row z (src/core/emit/wgsl.js:217-220):
+//   blf = zc < BL ? pow(zc / max(BL, 1), 1/7) : 1,  zc = z + 1/2.
+// It depends on z and BL only, so the library evaluates it on the host once
+// per configuration (bl_factor_host, the host's libm pow) and the kernels read
+// it from a per-z table: the power function leaves the device, and a host
+// restatement of the shader computes the same value bit for bit.
+template <typename R>
+inline R bl_factor_host(float bl_thickness, int z) {
+  const R bl = R(bl_thickness);
+  const R uInletBL = bl > R(1.0) ? bl : R(1.0);
+  const R zc = R(z) + R(0.5);
+  if (!(zc < bl)) return R(1.0);
+  return std::pow(zc / uInletBL, Lit<R>::bl_exp());
+}
 
 // Kernel-side copy of lbm_params (src/core/emit/wgsl.js:123-135).
 struct Params {
@@ -209,6 +222,36 @@ __device__ __forceinline__ void moments_fast(const R* g, R* sp, R* dp, R& delta,
   uu = fma_r<R>(uz, uz, fma_r<R>(uy, uy, ux * ux));
 }
 
+// FAST moments of populations held times a power-of-two scale S (the 16-bit
+// form stores S g_i): the pair sums, delta and rho u come out exactly S times
+// the unscaled ones (scaling by a power of two commutes with rounding), and
+//   rho = fma(S delta, 1/S, 1) = RN(1 + delta),
+//   u   = (S rho u) (RN(1/rho) / S) = RN((rho u) RN(1/rho))
+// round as the unscaled operations do: the results are bit-identical to
+// moments_fast on the unscaled values.  delta_s = S delta.
+template <typename R>
+__device__ __forceinline__ void moments_fast_scaled(const R* g, R inv_scale, R* sp, R* dp, R& delta_s, R& rho, R& ux,
+                                                    R& uy, R& uz, R& uu, R& rinv) {
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    sp[k] = g[2 * k + 1] + g[2 * k + 2];
+    dp[k] = g[2 * k + 1] - g[2 * k + 2];
+  }
+  delta_s = g[0];
+#pragma unroll
+  for (int k = 0; k < 9; ++k) delta_s = delta_s + sp[k];
+  rho = fma_r<R>(delta_s, inv_scale, R(1.0));
+  const R mx = pair_sum<R>(dp, [](int i) { return cx(i); });
+  const R my = pair_sum<R>(dp, [](int i) { return cy(i); });
+  const R mz = pair_sum<R>(dp, [](int i) { return cz(i); });
+  rinv = R(1.0) / rho;
+  const R rinvs = rinv * inv_scale;
+  ux = mx * rinvs;
+  uy = my * rinvs;
+  uz = mz * rinvs;
+  uu = fma_r<R>(uz, uz, fma_r<R>(uy, uy, ux * ux));
+}
+
 // Warp-uniform values derived from Params once per launch on the host (same
 // IEEE operations the per-cell code would do, so results do not change):
 //   tau0 = 1/omega+, tau0^2, 18 Cs^2 (src/core/emit/ir.js:290-293);
@@ -223,6 +266,7 @@ struct Uni {
   R sp_start, sp_len;
   R sp_t[Q];               // STRICT sponge targets
   R sp_tf[Q];              // FAST sponge targets
+  R sp_tfs[Q];             // FAST sponge targets times the storage scale
   int les_on;
 };
 
@@ -242,7 +286,7 @@ inline double fma_h(double a, double b, double c) { return std::fma(a, b, c); }
 
 // Host side (built with -ffp-contract=off; fusion only where fma_h is called).
 template <typename R>
-inline Uni<R> make_uni(const Params& P) {
+inline Uni<R> make_uni(const Params& P, R scale = R(1.0)) {
   Uni<R> u;
   const R cs = R(P.les_cs);
   const R magic = R(P.magic);
@@ -268,6 +312,7 @@ inline Uni<R> make_uni(const Params& P) {
     u.sp_t[i] = Lit<R>::w(i) * (R(3.0) * si + R(4.5) * si * si - R(1.5) * uuInf);
     u.sp_tf[i] = Lit<R>::w(i) * fma_h(si, fma_h(R(4.5), si, R(3.0)), -uu15f);
   }
+  for (int i = 0; i < Q; ++i) u.sp_tfs[i] = u.sp_tf[i] * scale;   // exact: scale is a power of two
   return u;
 }
 
@@ -348,27 +393,40 @@ __device__ __forceinline__ void smag_rates_c18(const Params& P, const Uni<R>& U,
 }
 
 // TRT per pair and the sponge blend (src/core/emit/ir.js:304-323, :458-478).
+// spt: the sponge targets in the units of g (U.sp_tf, or U.sp_tfs for
+// populations held times the storage scale).
 template <typename R, typename Emit>
 __device__ __forceinline__ void trt_emit_fast(const Uni<R>& U, int x, const R* g, R e0, const R* ns, const R* nd,
-                                              R omegaP, R omegaM, Emit&& emit) {
+                                              R omegaP, R omegaM, const R* spt, Emit&& emit) {
   R sig2 = R(0.0);
   if (R(x) > U.sp_start) {
     const R sx = (R(x) - U.sp_start) / U.sp_len;
     const R sigma = sx < R(1.0) ? sx : R(1.0);
     sig2 = sigma * sigma;
   }
-  const bool sponge = sig2 != R(0.0);
-  const R oms = R(1.0) - sig2;
-  auto blend = [&](int i, R o) -> R { return sponge ? fma_r<R>(U.sp_tf[i], sig2, o * oms) : o; };
-  emit(0, blend(0, fma_r<R>(-omegaP, g[0] - e0, g[0])));
+  const R o0 = fma_r<R>(-omegaP, g[0] - e0, g[0]);
   const R hP = R(0.5) * omegaP, hM = R(0.5) * omegaM;
+  // One branch per cell (warps run along x, so a warp is either inside the
+  // sponge or not) instead of a select per output.
+  if (sig2 != R(0.0)) {
+    const R oms = R(1.0) - sig2;
+    emit(0, fma_r<R>(spt[0], sig2, o0 * oms));
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      const int i = 2 * k + 1, j = i + 1;
+      const R oi = fma_r<R>(-hM, nd[k], fma_r<R>(-hP, ns[k], g[i]));
+      const R oj = fma_r<R>(hM, nd[k], fma_r<R>(-hP, ns[k], g[j]));
+      emit(i, fma_r<R>(spt[i], sig2, oi * oms));
+      emit(j, fma_r<R>(spt[j], sig2, oj * oms));
+    }
+    return;
+  }
+  emit(0, o0);
 #pragma unroll
   for (int k = 0; k < 9; ++k) {
     const int i = 2 * k + 1, j = i + 1;
-    const R oi = fma_r<R>(-hM, nd[k], fma_r<R>(-hP, ns[k], g[i]));
-    const R oj = fma_r<R>(hM, nd[k], fma_r<R>(-hP, ns[k], g[j]));
-    emit(i, blend(i, oi));
-    emit(j, blend(j, oj));
+    emit(i, fma_r<R>(-hM, nd[k], fma_r<R>(-hP, ns[k], g[i])));
+    emit(j, fma_r<R>(hM, nd[k], fma_r<R>(-hP, ns[k], g[j])));
   }
 }
 
@@ -376,11 +434,16 @@ __device__ __forceinline__ void trt_emit_fast(const Uni<R>& U, int x, const R* g
 // the fluid collide with LES, TRT and sponge (src/core/emit/ir.js:505-530).
 // g: pulled populations.  Each post-collision population is handed to
 // emit(i, value) as soon as it exists (i is a compile-time constant after
-// unrolling), so no output array stays live.
-template <typename R, bool FAST, typename Emit>
+// unrolling), so no output array stays live.  blf: the per-z inlet
+// boundary-layer factors (bl_factor_host), null when every factor is 1.
+// SC (FAST only): g, sp, dp and delta are held times the power-of-two `scale`
+// (moments_fast_scaled) and the emitted values are too; every operation on
+// them is the unscaled one times the scale, exactly.
+template <typename R, bool FAST, bool SC = false, typename Emit>
 __device__ __forceinline__ void collide(const Params& P, const Uni<R>& U, uint32_t ct, int x, int z, const R* g,
                                         const R* sp, const R* dp, R delta, R rho, R ux, R uy, R uz, R uu, R rinv,
-                                        Emit&& emit) {
+                                        const R* blf_tab, Emit&& emit, R scale = R(1.0)) {
+  static_assert(FAST || !SC, "the scaled form is a FAST restatement");
   if (ct == ESPELHO_Y) {
 #pragma unroll
     for (int i = 0; i < Q; ++i) emit(i, g[mirror_idx(i, 1)]);
@@ -394,16 +457,16 @@ __device__ __forceinline__ void collide(const Params& P, const Uni<R>& U, uint32
   if (ct == ENTRADA) {
     // blocoEntrada with the boundary-layer factor of the kernel header
     // (src/core/emit/ir.js:405-422; src/core/emit/wgsl.js:217-220)
-    const R bl = R(P.bl);
-    const R uInletBL = bl > R(1.0) ? bl : R(1.0);
-    const R zc = R(z) + R(0.5);
-    const R blf = zc < bl ? r_pow(zc / uInletBL, Lit<R>::bl_exp()) : R(1.0);
+    const R blf = blf_tab ? blf_tab[z] : R(1.0);
     const R ex = R(P.inlet[0]) * blf, ey = R(P.inlet[1]) * blf, ez = R(P.inlet[2]) * blf;
     if constexpr (FAST) {
       const R uuIn = fma_r<R>(ez, ez, fma_r<R>(ey, ey, ex * ex));
       const R uu15 = R(1.5) * uuIn;
 #pragma unroll
-      for (int i = 0; i < Q; ++i) emit(i, equilibrium<R, true>(i, R(0.0), R(1.0), ex, ey, ez, uuIn, uu15));
+      for (int i = 0; i < Q; ++i) {
+        const R e = equilibrium<R, true>(i, R(0.0), R(1.0), ex, ey, ez, uuIn, uu15);
+        emit(i, SC ? e * scale : e);
+      }
       return;
     }
     const R deltaIn = R(0.0), rhoIn = R(1.0);
@@ -420,11 +483,13 @@ __device__ __forceinline__ void collide(const Params& P, const Uni<R>& U, uint32
   if (ct == SAIDA) {
     // blocoSaida with the pulled u (src/core/emit/ir.js:432-444, :512-515)
     if constexpr (FAST) {
-      emit(0, Lit<R>::w(0) * (-uu15));
+      const R o0 = Lit<R>::w(0) * (-uu15);
+      emit(0, SC ? o0 * scale : o0);
 #pragma unroll
       for (int i = 1; i < Q; ++i) {
         const R c = dotc<R>(i, ux, uy, uz);
-        emit(i, Lit<R>::w(i) * fma_r<R>(c, fma_r<R>(R(4.5), c, R(3.0)), -uu15));
+        const R o = Lit<R>::w(i) * fma_r<R>(c, fma_r<R>(R(4.5), c, R(3.0)), -uu15);
+        emit(i, SC ? o * scale : o);
       }
       return;
     }
@@ -439,9 +504,17 @@ __device__ __forceinline__ void collide(const Params& P, const Uni<R>& U, uint32
   // FLUIDO: equilibrium, Smagorinsky LES (src/core/emit/ir.js:262-301)
   if constexpr (FAST) {
     R e0, ns[9], nd[9], omegaP, omegaM;
-    fluid_neq_fast<R>(sp, dp, delta, rho, ux, uy, uz, uu, e0, ns, nd);
-    smag_rates_fast<R>(P, U, ns, rinv, omegaP, omegaM);
-    trt_emit_fast<R>(U, x, g, e0, ns, nd, omegaP, omegaM, emit);
+    if constexpr (SC) {
+      // scaled: e = (S rho) a + S delta and the LES term's (S c18 qs) (rinv / S)
+      // are S times / exactly the unscaled operations
+      fluid_neq_fast<R>(sp, dp, delta, rho * scale, ux, uy, uz, uu, e0, ns, nd);
+      smag_rates_fast<R>(P, U, ns, rinv * (R(1.0) / scale), omegaP, omegaM);
+      trt_emit_fast<R>(U, x, g, e0, ns, nd, omegaP, omegaM, U.sp_tfs, emit);
+    } else {
+      fluid_neq_fast<R>(sp, dp, delta, rho, ux, uy, uz, uu, e0, ns, nd);
+      smag_rates_fast<R>(P, U, ns, rinv, omegaP, omegaM);
+      trt_emit_fast<R>(U, x, g, e0, ns, nd, omegaP, omegaM, U.sp_tf, emit);
+    }
     return;
   }
   R e[Q];
@@ -472,27 +545,44 @@ __device__ __forceinline__ void collide(const Params& P, const Uni<R>& U, uint32
     const R sigma = sx < R(1.0) ? sx : R(1.0);
     sig2 = sigma * sigma;
   }
-  const bool sponge = sig2 != R(0.0);
-  const R oms = R(1.0) - sig2;
-  auto blend = [&](int i, R o) -> R { return sponge ? o * oms + U.sp_t[i] * sig2 : o; };
-  // TRT per opposite pair (src/core/emit/ir.js:304-323), mix(a, b, t) = a (1 - t) + b t
-  emit(0, blend(0, g[0] - omegaP * (g[0] - e[0])));
+  // TRT per opposite pair (src/core/emit/ir.js:304-323), mix(a, b, t) = a (1 - t) + b t;
+  // one branch per cell for the sponge, as in trt_emit_fast
+  if (sig2 != R(0.0)) {
+    const R oms = R(1.0) - sig2;
+    emit(0, (g[0] - omegaP * (g[0] - e[0])) * oms + U.sp_t[0] * sig2);
+#pragma unroll
+    for (int i = 1; i < Q; i += 2) {
+      const int j = i + 1;
+      const R p = R(0.5) * ((g[i] + g[j]) - (e[i] + e[j]));
+      const R m = R(0.5) * ((g[i] - g[j]) - (e[i] - e[j]));
+      emit(i, (g[i] - omegaP * p - omegaM * m) * oms + U.sp_t[i] * sig2);
+      emit(j, (g[j] - omegaP * p + omegaM * m) * oms + U.sp_t[j] * sig2);
+    }
+    return;
+  }
+  emit(0, g[0] - omegaP * (g[0] - e[0]));
 #pragma unroll
   for (int i = 1; i < Q; i += 2) {
     const int j = i + 1;
     const R p = R(0.5) * ((g[i] + g[j]) - (e[i] + e[j]));
     const R m = R(0.5) * ((g[i] - g[j]) - (e[i] - e[j]));
-    emit(i, blend(i, g[i] - omegaP * p - omegaM * m));
-    emit(j, blend(j, g[j] - omegaP * p + omegaM * m));
+    emit(i, g[i] - omegaP * p - omegaM * m);
+    emit(j, g[j] - omegaP * p + omegaM * m);
   }
 }
 
 // ---------------------------------------------------------------- storage
 // Population storage forms.  Arithmetic is float (or double for the fp64 reference form).
+// kScaled: the stored value is the population times kScale (a power of two);
+// ld_raw / st_raw move the stored value without the scale.
 struct StF32 {
   using store_t = float;
   using real = float;
+  static constexpr bool kScaled = false;
+  static constexpr float kScale = 1.0f;
   static __device__ __forceinline__ float ld(const float* p) { return *p; }
+  static __device__ __forceinline__ float ld_raw(const float* p) { return *p; }
+  static __device__ __forceinline__ void st_raw(float* p, float v) { *p = v; }
   static __device__ __forceinline__ void st(float* p, float v) { *p = v; }
   static __device__ __forceinline__ float from_double(double v) { return (float)v; }
   // value from the aligned 32-bit word a pipelined copy brought in
@@ -501,7 +591,11 @@ struct StF32 {
 struct StF64 {
   using store_t = double;
   using real = double;
+  static constexpr bool kScaled = false;
+  static constexpr double kScale = 1.0;
   static __device__ __forceinline__ double ld(const double* p) { return *p; }
+  static __device__ __forceinline__ double ld_raw(const double* p) { return *p; }
+  static __device__ __forceinline__ void st_raw(double* p, double v) { *p = v; }
   static __device__ __forceinline__ void st(double* p, double v) { *p = v; }
   static __device__ __forceinline__ double from_double(double v) { return v; }
 };
@@ -510,9 +604,13 @@ struct StF64 {
 struct StF16S {
   using store_t = uint16_t;
   using real = float;
+  static constexpr bool kScaled = true;
+  static constexpr float kScale = 1024.0f;
   static __device__ __forceinline__ float ld(const uint16_t* p) {
     return __half2float(__ushort_as_half(*p)) * (1.0f / 1024.0f);
   }
+  static __device__ __forceinline__ float ld_raw(const uint16_t* p) { return __half2float(__ushort_as_half(*p)); }
+  static __device__ __forceinline__ void st_raw(uint16_t* p, float v) { *p = __half_as_ushort(__float2half_rn(v)); }
   static __device__ __forceinline__ float from_word(uint32_t w, uint32_t shift) {
     return __half2float(__ushort_as_half((unsigned short)(w >> shift))) * (1.0f / 1024.0f);
   }
@@ -524,9 +622,13 @@ struct StF16S {
 struct StBF16S {
   using store_t = uint16_t;
   using real = float;
+  static constexpr bool kScaled = false;
+  static constexpr float kScale = 1.0f;
   static __device__ __forceinline__ float ld(const uint16_t* p) {
     return __bfloat162float(__ushort_as_bfloat16(*p));
   }
+  static __device__ __forceinline__ float ld_raw(const uint16_t* p) { return ld(p); }
+  static __device__ __forceinline__ void st_raw(uint16_t* p, float v) { *p = __bfloat16_as_ushort(__float2bfloat16_rn(v)); }
   static __device__ __forceinline__ float from_word(uint32_t w, uint32_t shift) {
     return __bfloat162float(__ushort_as_bfloat16((unsigned short)(w >> shift)));
   }

@@ -41,6 +41,7 @@ struct Dev {
   const uint32_t* link;  // link words (in-place layout)
   float4* macros;        // nullable
   double* force;         // nullable: kForceSlots x 3 doubles accumulated by the fused force
+  const void* blf;       // nullable: nz inlet boundary-layer factors in the arithmetic type
 };
 
 struct Wrap {
@@ -143,6 +144,13 @@ __device__ __forceinline__ void step_cell(const Dev& d, const Params& P, const U
   using R = typename St::real;
   using S = typename St::store_t;
   using Off = typename OffT<W64>::type;
+  // SC: a form stored times a power-of-two scale (fp16) runs the FAST collide
+  // on the stored values themselves (moments_fast_scaled): bit-identical
+  // results without a multiply per loaded and per stored population.
+  constexpr bool SC = FAST && St::kScaled;
+  const R scale = R(St::kScale), inv_scale = R(1.0) / R(St::kScale);
+  auto ld = [](const S* p) -> R { return SC ? St::ld_raw(p) : St::ld(p); };
+  auto st = [](S* p, R v) { if (SC) St::st_raw(p, v); else St::st(p, v); };
   const int nx = d.nx, ny = d.ny;
   {
     const Off N = (Off)d.N;
@@ -154,11 +162,11 @@ __device__ __forceinline__ void step_cell(const Dev& d, const Params& P, const U
     const Deltas<Off> D(x, y, z, nx, ny, d.nz);
     constexpr bool E = (PAR == 0);
     R g[Q];
-    g[0] = St::ld(Fc);
+    g[0] = ld(Fc);
 #pragma unroll
     for (int i = 1; i < Q; i += 2) {
-      g[i] = St::ld(Fc + (Off)(E ? i + 1 : i) * N);
-      g[i + 1] = St::ld(Fc + D.odd(i) + (Off)(E ? i : i + 1) * N);
+      g[i] = ld(Fc + (Off)(E ? i + 1 : i) * N);
+      g[i + 1] = ld(Fc + D.odd(i) + (Off)(E ? i : i + 1) * N);
     }
     const uint32_t ct = (lw >> LINK_CLASS_SHIFT) & 7u;
     if (is_solid(ct)) {
@@ -169,12 +177,16 @@ __device__ __forceinline__ void step_cell(const Dev& d, const Params& P, const U
         if (bb) {
 #pragma unroll
           for (int i = 1; i < Q; i += 2) {
-            if ((bb >> (i - 1)) & 1u) g[i] = St::ld(Fc + (Off)(E ? i : i + 1) * N);
-            if ((bb >> i) & 1u) g[i + 1] = St::ld(Fc + D.odd(i) + (Off)(E ? i + 1 : i) * N);
+            if ((bb >> (i - 1)) & 1u) g[i] = ld(Fc + (Off)(E ? i : i + 1) * N);
+            if ((bb >> i) & 1u) g[i + 1] = ld(Fc + D.odd(i) + (Off)(E ? i + 1 : i) * N);
           }
         }
       }
-      // Bounce-back links: moving-wall term and the fused force.
+      // Bounce-back links: moving-wall term and the fused force (the force
+      // uses the unscaled g: fma(S g, 1/S, w) = RN(g + w)).
+      auto link_q = [&](int k) -> R {
+        return R(2.0) * (SC ? fma_r<R>(g[k], inv_scale, Lit<R>::w(k)) : g[k] + Lit<R>::w(k));
+      };
       const uint32_t bbmask = lw & 0x3ffffu;
       if (bbmask) {
         if (lw & LINK_SLOW) {
@@ -184,10 +196,11 @@ __device__ __forceinline__ void step_cell(const Dev& d, const Params& P, const U
             if (!((bbmask >> (k - 1)) & 1u)) continue;
             const uint32_t t = d.tipo[nbr(k, -1, x, y, z, w, nx, ny)];
             if (t == SOLIDO_MOVEL) {
-              g[k] = g[k] + Lit<R>::sixw(k) * (dotc<R>(k, R(P.belt[0]), R(P.belt[1]), R(P.belt[2])));
+              const R mw = Lit<R>::sixw(k) * (dotc<R>(k, R(P.belt[0]), R(P.belt[1]), R(P.belt[2])));
+              g[k] = g[k] + (SC ? mw * scale : mw);
             }
             if (FRC && ct == FLUIDO && t == SOLIDO) {
-              const R q = R(2.0) * (g[k] + Lit<R>::w(k));
+              const R q = link_q(k);
               fx -= (double)(cx(k) * q); fy -= (double)(cy(k) * q); fz -= (double)(cz(k) * q);
             }
           }
@@ -195,7 +208,7 @@ __device__ __forceinline__ void step_cell(const Dev& d, const Params& P, const U
 #pragma unroll
           for (int k = 1; k < Q; ++k) {
             if (!((bbmask >> (k - 1)) & 1u)) continue;
-            const R q = R(2.0) * (g[k] + Lit<R>::w(k));
+            const R q = link_q(k);
             fx -= (double)(cx(k) * q); fy -= (double)(cy(k) * q); fz -= (double)(cz(k) * q);
           }
         }
@@ -203,20 +216,22 @@ __device__ __forceinline__ void step_cell(const Dev& d, const Params& P, const U
       if (FRC && (fx != 0.0 || fy != 0.0 || fz != 0.0)) add_force(d.force, fx, fy, fz);
       R delta, rho, ux, uy, uz, uu, rinv = R(0.0);
       R sp[9], dp[9];
-      if (FAST) moments_fast<R>(g, sp, dp, delta, rho, ux, uy, uz, uu, rinv);
+      if (SC) moments_fast_scaled<R>(g, inv_scale, sp, dp, delta, rho, ux, uy, uz, uu, rinv);
+      else if (FAST) moments_fast<R>(g, sp, dp, delta, rho, ux, uy, uz, uu, rinv);
       else moments_strict<R>(g, delta, rho, ux, uy, uz, uu);
-      if (MAC) d.macros[cell] = make_float4((float)ux, (float)uy, (float)uz, (float)delta);
+      if (MAC) d.macros[cell] = make_float4((float)ux, (float)uy, (float)uz, (float)(SC ? delta * inv_scale : delta));
       // g*_i of an odd i goes to the neighbour's slot (E ? i : i+1); g*_{i+1}
       // stays local in slot (E ? i+1 : i); the rest population stays put.
-      collide<R, FAST>(P, U, ct, x, z, g, sp, dp, delta, rho, ux, uy, uz, uu, rinv, [&](int i, R v) {
+      collide<R, FAST, SC>(P, U, ct, x, z, g, sp, dp, delta, rho, ux, uy, uz, uu, rinv, static_cast<const R*>(d.blf),
+                           [&](int i, R v) {
         if (i == 0) {
-          St::st(Fc, v);
+          st(Fc, v);
         } else if (i & 1) {
-          St::st(Fc + D.odd(i) + (Off)(E ? i : i + 1) * N, v);
+          st(Fc + D.odd(i) + (Off)(E ? i : i + 1) * N, v);
         } else {
-          St::st(Fc + (Off)(E ? i : i - 1) * N, v);
+          st(Fc + (Off)(E ? i : i - 1) * N, v);
         }
-      });
+      }, scale);
     }
     }
 }
@@ -375,7 +390,8 @@ k_step_closure(Dev d, Params P, Uni<float> U, CloArgs A) {
           }
         }
       } else {
-        collide<R, true>(P, U, ct, x, z, g, sp, dp, delta, rho, ux, uy, uz, uu, rinv, emit);
+        collide<R, true>(P, U, ct, x, z, g, sp, dp, delta, rho, ux, uy, uz, uu, rinv, static_cast<const R*>(d.blf),
+                         emit);
       }
     }
   }
@@ -427,7 +443,7 @@ k_step_closure(Dev d, Params P, Uni<float> U, CloArgs A) {
       fell_back = true;
       smag_rates_fast<R>(P, U, ns, rinv, omegaP, omegaM);
     }
-    trt_emit_fast<R>(U, x, g, e0, ns, nd, omegaP, omegaM, emit);
+    trt_emit_fast<R>(U, x, g, e0, ns, nd, omegaP, omegaM, U.sp_tf, emit);
   }
   if constexpr (NET) {
     const unsigned fb = __ballot_sync(0xffffffffu, fell_back);
@@ -482,7 +498,7 @@ __global__ void __launch_bounds__(128) k_step_ab(Dev d, Params P, Uni<typename S
       if (FAST) moments_fast<R>(g, sp, dp, delta, rho, ux, uy, uz, uu, rinv);
       else moments_strict<R>(g, delta, rho, ux, uy, uz, uu);
       if (MAC) d.macros[cell] = make_float4((float)ux, (float)uy, (float)uz, (float)delta);
-      collide<R, FAST>(P, U, ct, x, z, g, sp, dp, delta, rho, ux, uy, uz, uu, rinv,
+      collide<R, FAST>(P, U, ct, x, z, g, sp, dp, delta, rho, ux, uy, uz, uu, rinv, static_cast<const R*>(d.blf),
                        [&](int i, R v) { St::st(dst + (int64_t)i * N + cell, v); });
     }
   }
@@ -768,7 +784,8 @@ __global__ void __launch_bounds__(BX, 768 / BX) k_step_pipe(Dev d, Params P, Uni
     if (FAST) moments_fast<R>(g, sp, dp, delta, rho, ux, uy, uz, uu, rinv);
     else moments_strict<R>(g, delta, rho, ux, uy, uz, uu);
     S* const Fc = F + cell;
-    collide<R, FAST>(P, U, ct, x, z, g, sp, dp, delta, rho, ux, uy, uz, uu, rinv, [&](int i, R v) {
+    collide<R, FAST>(P, U, ct, x, z, g, sp, dp, delta, rho, ux, uy, uz, uu, rinv, static_cast<const R*>(d.blf),
+                     [&](int i, R v) {
       if (i == 0) {
         St::st(Fc, v);
       } else if (i & 1) {
@@ -849,7 +866,7 @@ struct OpsImpl {
   }
   static cudaError_t step(const Dev& d, const Params& P, int parity, bool inplace, bool mac, bool frc, bool fast,
                           Launch L, cudaStream_t s) {
-    const Uni<R> U = make_uni<R>(P);
+    const Uni<R> U = make_uni<R>(P, R(St::kScale));
     if (fast && kFastOK) go<kFastOK>(d, P, U, parity, inplace, mac, frc, L, s);
     else go<false>(d, P, U, parity, inplace, mac, frc, L, s);
     return cudaGetLastError();

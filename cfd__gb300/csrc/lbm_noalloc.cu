@@ -2,13 +2,13 @@
 //
 // lbm_forces() sums per-block partial forces in a scratch buffer the solver
 // context allocates with cudaMalloc.  Some callers cannot allocate device
-// memory at the point where they need a force: code running while a stream is
-// being captured into a CUDA graph, real-time loops that must not take the
-// implicit device synchronisation of cudaMalloc/cudaFree, and hosts that hand
-// the library memory from their own pool (a JavaScript/N-API host owning its
-// buffers, a framework allocator).  lbm_forces_noalloc() gives them the same
-// force from buffers they already own, with its scratch in the file-scope
-// device array below.
+// memory at the point where they need a force: real-time loops that must not
+// take the implicit device synchronisation of cudaMalloc/cudaFree, and hosts
+// that hand the library memory from their own pool (a JavaScript/N-API host
+// owning its buffers, a framework allocator).  lbm_forces_noalloc() gives
+// them the same force from buffers they already own, with its scratch in the
+// file-scope device array below.  Its address is looked up per device
+// ordinal, so the device's primary context is the one supported.
 //
 // Scratch: g_noalloc_partials holds one partial force (3 doubles) per
 // (y, z) row of cells, for at most kNoAllocMaxRows rows (1.5 MiB, held by every

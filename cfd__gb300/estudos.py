@@ -3,6 +3,7 @@
     python -m cfd__gb300.estudos precisao [--steps 10000] [--grid 512,256,192]
     python -m cfd__gb300.estudos lote [--steps 256]
     python -m cfd__gb300.estudos fecho [--steps 24000] [--pesos w.npz]
+    python -m cfd__gb300.estudos casos
 
 precisao: the 512x256x192 precision workload (25.2 M cells): the seeded
 superellipsoid (semi-axes 80x32x22 cells, 20k triangles, 0.3-cell jitter)
@@ -21,6 +22,7 @@ from __future__ import annotations
 import argparse
 import json
 import math
+import sys
 import time
 
 import numpy as np
@@ -37,19 +39,32 @@ def _peak():
         return 6800.0
 
 
-def caso_precisao(grade):
+def malha_precisao(grade):
+    """Mesh of the precision workload: the seeded superellipsoid (semi-axes
+    80x32x22 cells, 20k triangles, 0.3-cell jitter), nose at 0.28 nx, centred
+    in y and z."""
     from .geometry import colocar, superelipsoide
-    from .tunel import areaFrontalCorpo, montarTipos
-    from .voxel import voxelizar
     pos, idx = superelipsoide(80.0, 32.0, 22.0, 2.5, 3.0, 20000, 0.3, 2027)
     pos = colocar(pos, grade, nariz=0.28, folga_piso=0.0)
     dz = 0.5 * grade["nz"] - 0.5 * (pos[:, 2].min() + pos[:, 2].max())
     pos[:, 2] += np.float32(dz)
-    vox = voxelizar(pos, idx, grade, sdf=False)
-    mt = montarTipos(grade, corpo=vox["tipo"], esteira=False)
+    return pos, idx
+
+
+def caso_precisao(grade, voxelizador=None):
+    """Cell types, parameters and frontal area of the precision workload.
+    voxelizador(pos, idx, grade) -> VOXEL codes; default: the GPU voxelizer."""
+    from .tunel import areaFrontalCorpo, montarTipos
+    pos, idx = malha_precisao(grade)
+    if voxelizador is None:
+        from .voxel import voxelizar
+        corpo = voxelizar(pos, idx, grade, sdf=False)["tipo"]
+    else:
+        corpo = voxelizador(pos, idx, grade)
+    mt = montarTipos(grade, corpo=corpo, esteira=False)
     t = mt["tipo"].reshape(grade["nz"], grade["ny"], grade["nx"])
     t[0, :, 1:grade["nx"] - 1] = 6          # free-slip floor as well
-    area = areaFrontalCorpo(vox["tipo"], grade)
+    area = areaFrontalCorpo(corpo, grade)
     nu = 0.008
     cfg = dict(omegaPlus=1.0 / (3.0 * nu + 0.5), lesCs=0.1, inletU=[0.05, 0.0, 0.0], esponja=mt["esponja"])
     return mt["tipo"], cfg, area
@@ -387,13 +402,135 @@ def fecho(re_treino=(2000, 5000, 20000), re_teste=10000, passos_finos=24000, sna
     return out
 
 
+def estavel(s, u_ref, fator=6.0, passo_amostra=11):
+    """The stability check of tests/estabilidade.html:49-72: recompute the
+    macros, read them back and sample every 11th cell; the run has diverged
+    if a sampled |u| is not finite or exceeds 6 times the free stream.
+    Returns (stable, max sampled |u|)."""
+    s.atualizarMacros()
+    m = s.lerMacros().reshape(-1, 4)[::passo_amostra, :3].astype(np.float64)
+    u = np.sqrt((m * m).sum(1))
+    if not np.isfinite(u).all():
+        return False, float("nan")
+    mu = float(u.max())
+    return mu <= fator * u_ref, mu
+
+
+def rodar_caso(grade, tipo, cfg, area, passos, u, janela, storage="f32", bloco=1000, checar=True):
+    """Run `passos` steps with the fused force of every step; Cd / Cl per step
+    (Maskell, theta 2.5, src/core/forces.js:55-95); the stability check every
+    `bloco` steps.  Returns the per-step coefficients and the window means."""
+    from .forces import coeficientes
+    from .solver import SolverCUDA
+    from .units import LatticeUnits
+    s = SolverCUDA(grade, storage=storage, escrever_macros=False)
+    s.definirTipos(tipo)
+    s.configurar(**cfg)
+    s.calibrarRepouso()
+    s.inicializar()
+    units = LatticeUnits(u)
+    cd, cl, feito, maxu, divergiu = [], [], 0, [], None
+    t0 = time.time()
+    while feito < passos:
+        n = min(bloco, passos - feito)
+        f = s.passoComForcas(n)
+        for k in range(n):
+            c = coeficientes(list(f[k]), units, area, grade)
+            cd.append(c["cd"])
+            cl.append(c["cl"])
+        feito += n
+        if checar:
+            ok, mu = estavel(s, u)
+            maxu.append(mu)
+            if not ok:
+                divergiu = feito
+                break
+    wall = time.time() - t0
+    s.destruir()
+    cd, cl = np.asarray(cd), np.asarray(cl)
+    a, b = janela
+    rec = {"storage": storage, "steps_run": feito, "diverged_at": divergiu, "max_u_per_check": maxu, "wall_s": wall}
+    if divergiu is None and len(cd) >= b:
+        w = slice(a, b)
+        rec.update(cd_mean=float(cd[w].mean()), cd_std=float(cd[w].std(ddof=1)), cl_mean=float(cl[w].mean()),
+                   cl_std=float(cl[w].std(ddof=1)), window=[a, b])
+    return rec, cd, cl
+
+
+def casos(storage_judge="f64"):
+    """The stated outputs of the plain-method workloads.
+
+    Mesh body, 320x160x128 (no-slip floor, u_in 0.06, Cs 0.12): Re 2000 on
+    the 96-cell length gives omega+ = 1.98295, above the reference's
+    stability ceiling omega_max = 1.90 (src/core/units.js:60-92).  10 000
+    steps with the stability check of tests/estabilidade.html every 1000;
+    Cd / Cl averaged over steps 5000-10000 if it survives; then the run at
+    the clamped viscosity (omega+ = 1.90, as Units does,
+    src/core/units.js:157-164), with its fp64 run as the accuracy judge.
+
+    Sphere, 128x64x64 (D = 16 at (40, 32, 32), Re 100, Cs 0.1): the Cd series
+    over 4000 steps in fp32 and fp64, and the fp32 error against fp64."""
+    from .cargas import GRIDS, carga
+    from .lattice import nu_from_omega, omega_from_nu
+    from .tunel import areaFrontalCorpo, corpoAnalitico, montarTipos
+    from .voxel import voxelizar
+    out = {"mesh_body": {}, "sphere": {}}
+    g2 = GRIDS["320x160x128"]
+    tipo, cfg, desc = carga("320x160x128")
+    from .geometry import corpo_config2
+    pos, idx = corpo_config2(g2)
+    corpo = voxelizar(pos, idx, g2, sdf=False)["tipo"]
+    area = areaFrontalCorpo(corpo, g2)
+    out["mesh_body"]["workload"] = desc
+    out["mesh_body"]["frontal_area"] = area
+    for nome, omega in (("re2000", cfg["omegaPlus"]), ("clamped_omega_1.90", 1.90)):
+        c = dict(cfg, omegaPlus=omega)
+        rec, cd, _ = rodar_caso(g2, tipo, c, area, 10000, 0.06, (5000, 10000))
+        rec["omega_plus"] = omega
+        rec["nu"] = nu_from_omega(omega)
+        rec["Re_length_96"] = 0.06 * 96 / rec["nu"]
+        rec["cd_series_every_100"] = [float(v) for v in cd[::100]]
+        out["mesh_body"][nome] = rec
+    judge = dict(cfg, omegaPlus=1.90)
+    rj, cdj, _ = rodar_caso(g2, tipo, judge, area, 10000, 0.06, (5000, 10000), storage=storage_judge)
+    out["mesh_body"]["clamped_omega_1.90_" + storage_judge] = {k: v for k, v in rj.items() if k != "max_u_per_check"}
+    c32 = out["mesh_body"]["clamped_omega_1.90"]
+    if "cd_mean" in c32 and "cd_mean" in rj:
+        c32["cd_err_vs_" + storage_judge] = (c32["cd_mean"] - rj["cd_mean"]) / rj["cd_mean"]
+        c32["cl_abs_err_vs_" + storage_judge] = c32["cl_mean"] - rj["cl_mean"]
+
+    g1 = {"nx": 128, "ny": 64, "nz": 64}
+    corpo1 = corpoAnalitico(g1, {"tipo": "esfera", "cx": 40, "cy": 32, "cz": 32, "raio": 8})
+    mt = montarTipos(g1, corpo=corpo1, esteira=False)
+    t1 = mt["tipo"].reshape(64, 64, 128)
+    t1[0, :, 1:127] = 6
+    nu = 0.05 * 16 / 100
+    cfg1 = dict(omegaPlus=omega_from_nu(nu), lesCs=0.1, inletU=[0.05, 0.0, 0.0], beltU=[0.0, 0.0, 0.0],
+                esponja=mt["esponja"])
+    area1 = areaFrontalCorpo(corpo1, g1)
+    series = {}
+    for st in ("f32", storage_judge):
+        rec, cd, cl = rodar_caso(g1, mt["tipo"], cfg1, area1, 4000, 0.05, (3000, 4000), storage=st, checar=False)
+        series[st] = cd
+        out["sphere"][st] = {k: v for k, v in rec.items() if k != "max_u_per_check"}
+        out["sphere"][st]["cd_series_every_10"] = [float(v) for v in cd[::10]]
+    d = series["f32"] - series[storage_judge]
+    out["sphere"]["frontal_area"] = area1
+    out["sphere"]["cd_final_err_vs_" + storage_judge] = float(d[-1] / series[storage_judge][-1])
+    out["sphere"]["cd_series_max_abs_err_vs_" + storage_judge] = float(np.abs(d).max())
+    out["sphere"]["cd_series_max_rel_err_after_500_vs_" + storage_judge] = float(
+        np.abs(d[500:] / series[storage_judge][500:]).max())
+    return out
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("study", choices=["precisao", "lote", "fecho"])
+    ap.add_argument("study", choices=["precisao", "lote", "fecho", "casos"])
     ap.add_argument("--pesos", default=None, help="fecho: write the trained weights (.npz) here")
     ap.add_argument("--cada", type=int, default=8, help="fecho: the held form's evaluation period (calibration)")
     ap.add_argument("--steps", type=int, default=10000)
     ap.add_argument("--grid", default="512,256,192")
+    ap.add_argument("--out", default=None, help="also write the result (JSON) to this file")
     a = ap.parse_args(argv)
     nx, ny, nz = (int(v) for v in a.grid.split(","))
     t0 = time.time()
@@ -401,10 +538,17 @@ def main(argv=None):
         r = lote(steps=a.steps)
     elif a.study == "fecho":
         r = fecho(passos_finos=a.steps, pesos_saida=a.pesos, cada=a.cada)
+    elif a.study == "casos":
+        r = casos()
     else:
         r = precisao(a.steps, {"nx": nx, "ny": ny, "nz": nz})
     r["wall_s"] = time.time() - t0
+    r["command"] = "python -m cfd__gb300.estudos " + " ".join(argv if argv is not None else sys.argv[1:])
     print(json.dumps(r))
+    if a.out:
+        with open(a.out, "w") as f:
+            json.dump(r, f, indent=1)
+            f.write("\n")
 
 
 if __name__ == "__main__":

@@ -1,0 +1,57 @@
+"""Run a few steps of a benchmark workload on cuda:0 — the program the
+committed ncu summaries under profiles/ capture.
+
+    python -m cfd__gb300.perfil [--grid 512x256x192|320x160x128]
+                                [--storage f32|f16s|bf16s|f64] [--steps K] [--warmup W]
+                                [--closure K] [--engine 0|1] [--block BX] [--variant MINB]
+
+W warm-up steps, then K steps, then a synchronize; prints the wall time.
+The step kernel runs once per step (k_step_inplace, or k_step_closure with
+--closure), so `ncu -k regex:k_step -s W -c C` captures steps W .. W+C-1.
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import time
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--grid", default="512x256x192")
+    ap.add_argument("--storage", default="f32", choices=["f32", "f16s", "bf16s", "f64"])
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--closure", type=int, default=0, help="learned closure evaluated every K steps (0: off)")
+    ap.add_argument("--engine", type=int, default=0)
+    ap.add_argument("--block", type=int, default=0)
+    ap.add_argument("--variant", type=int, default=0, help="lbm_set_launch min_blocks code")
+    a = ap.parse_args(argv)
+    from . import build as B
+    B.build()
+    from .cargas import GRIDS, carga
+    from .solver import SolverCUDA
+    tipo, cfg, desc = carga(a.grid)
+    s = SolverCUDA(GRIDS[a.grid], storage=a.storage, escrever_macros=False)
+    s.definirTipos(tipo)
+    s.configurar(**cfg, closure=a.closure)
+    if a.closure:
+        from .fecho import carregar
+        s.definirFecho(carregar(os.path.join(os.path.dirname(os.path.abspath(__file__)), "pesos", "fecho_coef.npz")))
+        s.motorFecho(a.engine)
+    if a.block or a.variant:
+        s.definirBloco(a.block or 64, a.variant)
+    s.inicializar()
+    s.passo(a.warmup)
+    s.sincronizar()
+    t0 = time.perf_counter()
+    s.passo(a.steps)
+    s.sincronizar()
+    dt = time.perf_counter() - t0
+    N = int(tipo.size)
+    print(f"{desc}: {a.storage}, {a.steps} steps in {dt * 1e3:.2f} ms ({N * a.steps / dt / 1e6:.0f} MLUPS wall)")
+    s.destruir()
+
+
+if __name__ == "__main__":
+    main()

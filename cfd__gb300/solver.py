@@ -176,6 +176,8 @@ class SolverCUDA:
                 r["aplicar"](self.fatorRampa)
         nat.check(self._lib.lbm_step(self._h, int(n)))
         self.passos += n
+        if n % 2:   # the reference swaps its A/B sets once per dispatched step
+            self._frente = "B" if self._frente == "A" else "A"
 
     def passoComForcas(self, n):
         """n steps that also return the force of the state each step streams

@@ -199,19 +199,24 @@ int lbm_set_block(lbm_ctx* ctx, int block_x);
 int lbm_set_launch(lbm_ctx* ctx, int block_x, int min_blocks);
 
 /* Momentum-exchange force for callers that cannot allocate device memory when
- * they need it: work being captured into a CUDA graph, real-time loops that
- * must not take cudaMalloc's implicit synchronisation, hosts that own every
- * buffer through their own pool.  No counterpart in the reference.  Same value
- * as lbm_forces (raw, before the rest offset), computed from buffers the
- * caller owns: pop = 19*N fp32 populations on the device, direction-major,
- * natural layout g[i*N + cell]; tipo = N cell classes (uint8) on the device;
- * f_out = 3 doubles on the device, written when the work on `stream` (a
- * cudaStream_t, NULL = legacy default stream) completes.  Enqueues only; no
- * synchronisation.  Allocates nothing: its per-row partial sums live in a
- * 1.5 MiB array built into the library, so ny*nz may be at most 65536
- * (LBM_EINVAL beyond).  The first call on a device looks up that array's
- * device address; make it before any stream capture.  Calls that overlap on
- * the GPU share the array and race. */
+ * they need it: real-time loops that must not take cudaMalloc's implicit
+ * device synchronisation, and hosts that own every device buffer through
+ * their own pool or allocator (a JavaScript/N-API host, a framework's
+ * caching allocator).  No counterpart in the reference.  Same value as
+ * lbm_forces (raw, before the rest offset), computed from buffers the caller
+ * owns: pop = 19*N fp32 populations on the device, direction-major, natural
+ * layout g[i*N + cell]; tipo = N cell classes on the device, ONE BYTE each
+ * (uint8; lbm_set_types takes uint32 on the host, so narrow that array
+ * before passing it here); f_out = 3 doubles on the device, written when the
+ * work on `stream` (a cudaStream_t, NULL = legacy default stream) completes.
+ * Enqueues only; no synchronisation.  Allocates nothing: its per-row partial
+ * sums live in a 1.5 MiB array built into the library, so ny*nz may be at
+ * most 65536 (LBM_EINVAL beyond).  The first call on a device looks up that
+ * array's device address with the device current; make it before any stream
+ * capture.  The address is kept per device ordinal, so only the device's
+ * primary context (the CUDA runtime's default) is supported.  Every call
+ * shares the one array: calls that overlap on the GPU (other streams, other
+ * host threads) race, so callers must order them. */
 int lbm_forces_noalloc(const float* pop, const uint8_t* tipo, const lbm_dims* dims, double* f_out, void* stream);
 
 #ifdef __cplusplus

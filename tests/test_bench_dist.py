@@ -53,7 +53,7 @@ def test_reference_arm_nonzero_rank_exits_without_work(monkeypatch):
     monkeypatch.setenv("LOCAL_RANK", "1")
 
     class A:
-        steps, warmup, gpus, body = 1, 0, 2, "mesh"
+        steps, warmup, gpus, grid = 1, 0, 2, "320x160x128"
 
     def boom(*a, **k):
         raise AssertionError("rank 1 must not build the workload")
@@ -71,16 +71,33 @@ def test_reference_arm_line_contract():
     import sys
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
     env = {k: v for k, v in os.environ.items() if k not in ("RANK", "WORLD_SIZE", "LOCAL_RANK")}
-    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "2", "--warmup", "1"],
-                       cwd=root, env=env, capture_output=True, text=True, timeout=600)
+    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "2", "--warmup", "1",
+                        "--grid", "320x160x128"], cwd=root, env=env, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
     assert len(lines) == 1
     d = json.loads(lines[0])
-    assert d["impl"] == "reference" and d["unit"] == "MLUPS" and d["metric"].startswith("MLUPS")
+    import bench
+    assert d["impl"] == "reference" and d["unit"] == "MLUPS" and d["metric"] == bench.METRIC
     assert d["value"] > 0 and d["higher_is_better"] is True and d["steps"] == 2 and d["warmup"] >= 3
     cb = d["cpu_baseline"]
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["sample"] and cb["value"] == d["value"]
     assert d["e2e"]["value"] == d["value"] and d["e2e"]["unit"] == d["unit"]
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
     assert d["config"]["workload"].startswith("320x160x128")
+
+
+def test_both_arms_print_the_baseline_metric():
+    """The two arms' lines carry the same metric string, the benchmark's own,
+    so that their values can be divided."""
+    import inspect
+    import json
+
+    import bench
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    with open(os.path.join(root, "BASELINE.json")) as f:
+        assert json.load(f)["metric"] == bench.METRIC
+    for fn in (bench.run_ours, bench.run_reference):
+        src = inspect.getsource(fn)
+        assert '"metric": METRIC' in src, fn.__name__
+        assert '"metric": "' not in src, fn.__name__

@@ -1,5 +1,5 @@
 """lbm_forces_noalloc: the force entry point for callers that cannot allocate
-device memory (graph capture, real-time loops, hosts that own every buffer).
+device memory (real-time loops, hosts that own every buffer).
 
 Collected last on purpose (test_zz_*): if it fails, a run that stops at the
 first failure has already run every other test.  It passes alone in a fresh
