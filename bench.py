@@ -500,6 +500,21 @@ def run_ours(args):
 
     forms = {}
     if not args.no_forms:
+        # the fused-force variant of the step on the device (what e2e runs),
+        # without the host: K steps of passoComForcas between CUDA events
+        s2 = make(args.storage)
+        s2.passoComForcas(args.warmup)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        s2.passoComForcas(args.steps)
+        e1.record(stream)
+        e1.synchronize()
+        msf = e0.elapsed_time(e1)
+        forms["fused_force_step_device"] = {"MLUPS": N * args.steps / (msf / 1e3) / 1e6,
+                                            "note": "passoComForcas(K): step with the fused force, its per-step "
+                                                    "slot clear and one read-back of the K forces"}
+        s2.destruir()
         for st in ("f16s", "bf16s"):
             s2 = make(st)
             s2.passo(args.warmup)

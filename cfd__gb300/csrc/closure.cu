@@ -12,6 +12,8 @@
 // Evaluation uses the tensor-core MLP the fused step uses (closure_mlp.cuh).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -188,23 +190,29 @@ __global__ void __launch_bounds__(128) k_eval(const float* __restrict__ feats, l
   if (i < m) nu[i] = inside ? closure_nu(*F, y) : __int_as_float(0x7fc00000);
 }
 
-// The same through the CTA-wide tcgen05 MLP (128 rows per block).
+// The same through the CTA-wide tcgen05 MLP: persistent CTAs walk tiles of
+// 128 rows (set up once per CTA, closure_tc.cuh).
 __global__ void __launch_bounds__(128) k_eval_tc(const float* __restrict__ feats, long long m,
                                                  const MlpFrag* __restrict__ F, float* __restrict__ nu,
                                                  unsigned* __restrict__ err) {
-  __shared__ TcShared S;
+  __shared__ TcPersist S;
   const int tid = threadIdx.x;
-  const long long i = (long long)blockIdx.x * TC_ROWS + tid;
-  float x[6];
+  const uint32_t tmem = tcp_setup(S, F->tcb, tid);
+  uint32_t phase = 0;
+  bool dead = false;
+  const long long ntiles = (m + TC_ROWS - 1) / TC_ROWS;
+  for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const long long i = t * TC_ROWS + tid;
+    float x[6];
 #pragma unroll
-  for (int a = 0; a < 6; ++a) x[a] = i < m ? feats[i * 6 + a] : 0.0f;
-  const bool inside = closure_in_range(*F, x);
+    for (int a = 0; a < 6; ++a) x[a] = i < m ? feats[i * 6 + a] : 0.0f;
+    const bool inside = closure_in_range(*F, x);
 #pragma unroll
-  for (int a = 0; a < 6; ++a) x[a] = i < m ? (x[a] - F->mean[a]) * F->inv_std[a] : 0.0f;
-  const uint32_t tmem = tc_begin(S, F->tcb, tid);
-  const float y = tc_mlp(S, tmem, tid, x);
-  tc_end(S, tmem, tid);
-  if (i < m) nu[i] = inside ? closure_nu(*F, y) : __int_as_float(0x7fc00000);
+    for (int a = 0; a < 6; ++a) x[a] = i < m ? (x[a] - F->mean[a]) * F->inv_std[a] : 0.0f;
+    const float y = tcp_mlp(S, tmem, tid, x, phase, dead);
+    if (i < m) nu[i] = inside ? closure_nu(*F, y) : __int_as_float(0x7fc00000);
+  }
+  tcp_teardown(S, tmem, tid, phase, dead);
   if (tid == 0 && S.err) atomicOr(err, 1u);
 }
 
@@ -528,7 +536,14 @@ int closure_eval(const closure_weights* w, const float* feats, size_t m, int eng
   CCK(cudaMemcpy(d_f, feats, sizeof(float) * m * NI, cudaMemcpyHostToDevice), "upload");
   CCK(cudaMemcpy(d_F, &F, sizeof F, cudaMemcpyHostToDevice), "upload");
   CCK(cudaMemset(d_err, 0, sizeof(unsigned)), "clear");
-  if (engine == 1) k_eval_tc<<<(unsigned)((m + TC_ROWS - 1) / TC_ROWS), TC_ROWS>>>(d_f, (long long)m, d_F, d_nu, d_err);
+  if (engine == 1) {
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long tiles = ((long long)m + TC_ROWS - 1) / TC_ROWS;
+    const unsigned grid = (unsigned)std::max<long long>(1, std::min<long long>(tiles, 4LL * sms));
+    k_eval_tc<<<grid, TC_ROWS>>>(d_f, (long long)m, d_F, d_nu, d_err);
+  }
   else k_eval<<<(unsigned)((m + 127) / 128), 128>>>(d_f, (long long)m, d_F, d_nu);
   CCK(cudaGetLastError(), "eval kernel");
   unsigned err = 0;

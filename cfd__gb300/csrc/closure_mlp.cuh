@@ -32,6 +32,21 @@ struct MlpFrag {
   int coef;                     // output is Cs^2 (1) or nu_t (0)
 };
 
+// The network's per-feature constants and output bounds, passed by value in
+// the step kernels' parameters (read from the constant bank, no loads).
+struct CloConst {
+  float lo[6], hi[6], mean[6], inv_std[6];
+  float nu_scale, nu_max;
+};
+
+// Raw features inside the trained range (false also for NaN features).
+__device__ __forceinline__ bool closure_in_range(const CloConst& K, const float (&f)[6]) {
+  bool ok = true;
+#pragma unroll
+  for (int a = 0; a < 6; ++a) ok = ok && f[a] >= K.lo[a] && f[a] <= K.hi[a];
+  return ok;
+}
+
 // Raw features inside the trained range (false also for NaN features).
 __device__ __forceinline__ bool closure_in_range(const MlpFrag& F, const float (&f)[6]) {
   bool ok = true;
@@ -180,10 +195,12 @@ __device__ __forceinline__ void closure_features(float xx, float yy, float zz, f
 
 // nu_t from the network output: nu_scale * softplus(y); NaN when the cell
 // must fall back (not finite, negative or above nu_max).
-__device__ __forceinline__ float closure_nu(const MlpFrag& F, float y) {
+__device__ __forceinline__ float closure_nu(float nu_scale, float nu_max, float y) {
   const float sp = y > 20.0f ? y : __logf(1.0f + __expf(y));
-  const float nu = F.nu_scale * sp;
-  return (nu >= 0.0f && nu <= F.nu_max) ? nu : __int_as_float(0x7fc00000);
+  const float nu = nu_scale * sp;
+  return (nu >= 0.0f && nu <= nu_max) ? nu : __int_as_float(0x7fc00000);
 }
+__device__ __forceinline__ float closure_nu(const MlpFrag& F, float y) { return closure_nu(F.nu_scale, F.nu_max, y); }
+__device__ __forceinline__ float closure_nu(const CloConst& K, float y) { return closure_nu(K.nu_scale, K.nu_max, y); }
 
 }  // namespace lbm

@@ -2,11 +2,11 @@
 // of 128 cells on the 5th-generation tensor cores (tcgen05.mma, kind::f16,
 // bf16 operands from shared memory, fp32 accumulators in tensor memory).
 //
-// One tile = the CTA's 128 cells (thread tid <-> MMA row tid <-> TMEM lane
+// One tile = a CTA's 128 cells (thread tid <-> MMA row tid <-> TMEM lane
 // tid).  Per layer: every thread writes its row of the A operand to shared
 // memory, one thread issues the MMA(s) and commits them to an mbarrier, every
 // thread waits on it and reads its row of the accumulator back with
-// tcgen05.ld.  Biases ride in the K dimension: A carries a constant 1 in
+// tcgen05.ld.  A CTA sets up once and then walks many tiles (persistent).  Biases ride in the K dimension: A carries a constant 1 in
 // column kb and B holds the bias there (layer 1: K = 16 = 6 features + 1 +
 // 9 zeros; layers 2, 3: K = 48 = 32 hidden + 1 + 15 zeros), so the
 // accumulators start at zero and no bias add is needed.
@@ -36,7 +36,6 @@ constexpr int TC_B1_BYTES = 32 * TC_K1 * 2;      // 1024
 constexpr int TC_B2_BYTES = 32 * TC_K2 * 2;      // 3072
 constexpr int TC_B3_BYTES = 16 * TC_K2 * 2;      // 1536
 constexpr int TC_B_BYTES = TC_B1_BYTES + TC_B2_BYTES + TC_B3_BYTES;   // 5632
-constexpr int TC_A_BYTES = TC_ROWS * TC_K2 * 2;  // 12288 (layer-1 A uses the first 4096)
 constexpr uint32_t TC_TMEM_COLS = 32;
 constexpr uint32_t TC_WAIT_LIMIT = 1u << 20;     // mbarrier polls (~0.5 us apart) before giving up
 
@@ -45,14 +44,6 @@ constexpr uint32_t TC_WAIT_LIMIT = 1u << 20;     // mbarrier polls (~0.5 us apar
 __host__ __device__ constexpr uint32_t tc_off(int r, int k, int K) {
   return (uint32_t)((r >> 3) * (K / 8) * 128 + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
 }
-
-struct TcShared {
-  alignas(128) uint8_t a[TC_A_BYTES];
-  alignas(128) uint8_t b[TC_B_BYTES];
-  alignas(8) uint64_t mbar;
-  uint32_t tmem;
-  uint32_t err;
-};
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -141,11 +132,32 @@ __device__ __forceinline__ void sts128(uint8_t* base, uint32_t off, uint32_t a, 
   *reinterpret_cast<uint4*>(base + off) = make_uint4(a, b, c, d);
 }
 
-// Start of a tile: warp 0 allocates TC_TMEM_COLS columns of tensor memory,
-// thread 0 initialises the mbarrier, all threads copy the packed B operands
-// (bw: TC_B_BYTES, 16-byte aligned).  Every thread of the 128-thread CTA
-// calls it; returns the TMEM base address.
-__device__ __forceinline__ uint32_t tc_begin(TcShared& S, const uint4* __restrict__ bw, int tid) {
+// ------------------------------------------------------------------ persistent
+// The engine of the persistent closure step (k_step_closure_tc): a CTA sets
+// up once (TMEM columns, the mbarrier, the B operands, the constant columns
+// of the A operands) and then walks many 128-cell tiles; per tile it pays one
+// CTA barrier and one MMA round trip per layer.
+//
+// A operands live in two buffers so that the constant columns never need
+// rewriting: a1 (K = 16: features 0..5, the bias 1 at element 6, zeros to
+// 15 -- elements 8..15 are a separate core matrix, written once) and a2
+// (K = 48: 32 hidden values, the bias 1 at element 32, zeros to 47 -- the
+// core matrices of elements 32..47 are written once).
+struct TcPersist {
+  alignas(128) uint8_t a1[TC_ROWS * TC_K1 * 2];
+  alignas(128) uint8_t a2[TC_ROWS * TC_K2 * 2];
+  alignas(128) uint8_t b[TC_B_BYTES];
+  alignas(8) uint64_t mbar;
+  uint32_t tmem;
+  uint32_t err;      // a wait gave up: no further MMA is issued
+};
+
+__device__ __forceinline__ void mbar_init_fence() {
+  asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+
+// Set-up of a persistent CTA (128 threads, every thread calls it).
+__device__ __forceinline__ uint32_t tcp_setup(TcPersist& S, const uint4* __restrict__ bw, int tid) {
   if (tid < 32) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_addr(&S.tmem)),
                  "r"(TC_TMEM_COLS)
@@ -154,90 +166,108 @@ __device__ __forceinline__ uint32_t tc_begin(TcShared& S, const uint4* __restric
   }
   if (tid == 0) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(smem_addr(&S.mbar)) : "memory");
+    mbar_init_fence();
     S.err = 0;
   }
   uint4* bd = reinterpret_cast<uint4*>(S.b);
   for (int i = tid; i < TC_B_BYTES / 16; i += TC_ROWS) bd[i] = __ldg(bw + i);
+  // constant columns of this thread's rows
+  sts128(S.a1, tc_off(tid, 8, TC_K1), 0u, 0u, 0u, 0u);
+  sts128(S.a2, tc_off(tid, 32, TC_K2), 0x3F80u, 0u, 0u, 0u);   // bf16 1.0 at element 32
+  sts128(S.a2, tc_off(tid, 40, TC_K2), 0u, 0u, 0u, 0u);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   return S.tmem;
 }
 
-// End of a tile: every thread calls it after its last tcgen05.ld.
-__device__ __forceinline__ void tc_end(TcShared& S, uint32_t tmem, int tid) {
+// Make this thread's A row visible to the tensor core, meet the CTA, and let
+// thread 0 issue `nk` K-steps of 16 from `a` (K elements per row) against the
+// B operand at b_off into TMEM columns [0, N), committed to the mbarrier.
+// `dead`: this thread has seen a wait give up.  The barrier ORs it over the
+// CTA, so every thread takes the same decision: once any wait has given up,
+// no further MMA is issued.  Returns whether the MMA was issued.
+__device__ __forceinline__ bool tcp_issue(TcPersist& S, const uint8_t* a, uint32_t tmem, int tid, int K, int N,
+                                          int nk, uint32_t b_off, bool& dead) {
+  proxy_fence();
+  tc_fence_before();
+  dead = __syncthreads_or(dead ? 1 : 0) != 0;
+  const bool go = !dead;
+  if (go && tid == 0) {
+    tc_fence_after();
+    const uint32_t a0 = smem_addr(a), b0 = smem_addr(S.b) + b_off;
+    const uint32_t idesc = tc_idesc(TC_ROWS, N);
+    for (int k = 0; k < nk; ++k)
+      tc_mma(tmem, tc_desc(a0 + (uint32_t)k * 256u, K), tc_desc(b0 + (uint32_t)k * 256u, K), idesc, k > 0);
+    tc_commit(&S.mbar);
+  }
+  return go;
+}
+
+// Bounded wait for the committed MMAs of the phase with parity `par`; a
+// thread that gives up sets `dead` and records it in S.err for the report.
+__device__ __forceinline__ bool tcp_wait(TcPersist& S, uint32_t par, bool& dead) {
+  const bool ok = mbar_wait(&S.mbar, par);
+  if (!ok) { dead = true; S.err = 1; }
+  tc_fence_after();
+  return ok;
+}
+
+// Layer epilogue of a hidden layer: this thread's 32 accumulator columns ->
+// ReLU -> bf16 -> elements 0..31 of its row of a2.
+__device__ __forceinline__ void tcp_hidden_to_a2(TcPersist& S, uint32_t tmem, int tid) {
+  const uint32_t lane_addr = tmem + ((uint32_t)(tid & ~31) << 16);
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    float v[16];
+    tc_ld16(lane_addr + 16u * h, v);
+    uint32_t q[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) q[i] = tc_relu_pack(v[2 * i], v[2 * i + 1]);
+    sts128(S.a2, tc_off(tid, 16 * h, TC_K2), q[0], q[1], q[2], q[3]);
+    sts128(S.a2, tc_off(tid, 16 * h + 8, TC_K2), q[4], q[5], q[6], q[7]);
+  }
+}
+
+// The network for the CTA's current tile: x = this thread's normalised
+// features (zeros for threads without a fluid cell).  All 128 threads call
+// it.  `phase` is the parity of the mbarrier's next phase (three phases per
+// tile), `dead` the give-up state (tcp_issue).  NaN when the network was not
+// run or a wait gave up.
+__device__ __forceinline__ float tcp_mlp(TcPersist& S, uint32_t tmem, int tid, const float (&x)[6], uint32_t& phase,
+                                         bool& dead) {
+  const float nan = __int_as_float(0x7fc00000);
+  sts128(S.a1, tc_off(tid, 0, TC_K1), tc_pack(x[0], x[1]), tc_pack(x[2], x[3]), tc_pack(x[4], x[5]), 0x3F80u);
+  bool ok = true;
+  if (!tcp_issue(S, S.a1, tmem, tid, TC_K1, 32, 1, 0, dead)) return nan;
+  ok = tcp_wait(S, phase, dead) && ok;
+  phase ^= 1u;
+  tcp_hidden_to_a2(S, tmem, tid);
+  if (!tcp_issue(S, S.a2, tmem, tid, TC_K2, 32, 3, TC_B1_BYTES, dead)) return nan;
+  ok = tcp_wait(S, phase, dead) && ok;
+  phase ^= 1u;
+  tcp_hidden_to_a2(S, tmem, tid);
+  if (!tcp_issue(S, S.a2, tmem, tid, TC_K2, 16, 3, TC_B1_BYTES + TC_B2_BYTES, dead)) return nan;
+  ok = tcp_wait(S, phase, dead) && ok;
+  phase ^= 1u;
+  const float y = tc_ld1(tmem + ((uint32_t)(tid & ~31) << 16));
+  return ok ? y : nan;
+}
+
+// End of a persistent CTA.  If a wait gave up (in any thread: ORed over the
+// CTA), the last committed MMAs may still be running: wait for that phase
+// once more (bounded) before the TMEM columns are released.  `phase` is the
+// parity of the next phase, so the last committed one has parity phase ^ 1.
+__device__ __forceinline__ void tcp_teardown(TcPersist& S, uint32_t tmem, int tid, uint32_t phase, bool dead) {
+  tc_fence_before();
+  dead = __syncthreads_or(dead ? 1 : 0) != 0;
+  if (dead) (void)mbar_wait(&S.mbar, phase ^ 1u);
   tc_fence_before();
   __syncthreads();
   if (tid < 32) {
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem), "r"(TC_TMEM_COLS) : "memory");
   }
-}
-
-// Make this thread's shared-memory operand row visible to the tensor core,
-// wait for every row, and let thread 0 issue `nk` K-steps of 16 into
-// columns [0, N) and commit them.
-__device__ __forceinline__ void tc_issue(TcShared& S, uint32_t tmem, int tid, int K, int N, int nk,
-                                         uint32_t b_off) {
-  proxy_fence();
-  tc_fence_before();
-  __syncthreads();
-  if (tid == 0) {
-    tc_fence_after();
-    const uint32_t a0 = smem_addr(S.a), b0 = smem_addr(S.b) + b_off;
-    const uint32_t idesc = tc_idesc(TC_ROWS, N);
-    for (int k = 0; k < nk; ++k)   // K-step k covers elements 16k..16k+15: two core matrices
-      tc_mma(tmem, tc_desc(a0 + (uint32_t)k * 256u, K), tc_desc(b0 + (uint32_t)k * 256u, K), idesc, k > 0);
-    tc_commit(&S.mbar);
-  }
-}
-
-// Wait for the committed MMAs; on a timeout record it and return false.
-__device__ __forceinline__ bool tc_wait(TcShared& S, uint32_t parity) {
-  const bool ok = mbar_wait(&S.mbar, parity);
-  if (!ok) S.err = 1;
-  tc_fence_after();
-  return ok;
-}
-
-// Hidden layer epilogue: this thread's 32 accumulator columns -> ReLU ->
-// bf16 -> its row of the next A operand (K = 48, constant 1 at element 32).
-__device__ __forceinline__ void tc_hidden_to_a(TcShared& S, uint32_t tmem, int tid) {
-  const uint32_t lane_addr = tmem + ((uint32_t)(tid & ~31) << 16);
-#pragma unroll
-  for (int h = 0; h < 2; ++h) {
-    float v[16];
-    tc_ld16(lane_addr + 16u * h, v);
-    uint32_t p[8];
-#pragma unroll
-    for (int i = 0; i < 8; ++i) p[i] = tc_relu_pack(v[2 * i], v[2 * i + 1]);
-    sts128(S.a, tc_off(tid, 16 * h, TC_K2), p[0], p[1], p[2], p[3]);
-    sts128(S.a, tc_off(tid, 16 * h + 8, TC_K2), p[4], p[5], p[6], p[7]);
-  }
-  const uint32_t one = 0x3F80u;   // bf16 1.0 in the low half
-  sts128(S.a, tc_off(tid, 32, TC_K2), one, 0u, 0u, 0u);
-  sts128(S.a, tc_off(tid, 40, TC_K2), 0u, 0u, 0u, 0u);
-}
-
-// y (pre-softplus) of this thread's cell; x: normalised features (zeros for
-// threads without a cell).  All 128 threads of the CTA must call it, between
-// tc_begin and tc_end.  NaN when a wait gave up.
-__device__ __forceinline__ float tc_mlp(TcShared& S, uint32_t tmem, int tid, const float (&x)[6]) {
-  // layer 1: A row = [x0..x5, 1, 0 x 9]
-  sts128(S.a, tc_off(tid, 0, TC_K1), tc_pack(x[0], x[1]), tc_pack(x[2], x[3]), tc_pack(x[4], x[5]), 0x3F80u);
-  sts128(S.a, tc_off(tid, 8, TC_K1), 0u, 0u, 0u, 0u);
-  tc_issue(S, tmem, tid, TC_K1, 32, 1, 0);
-  bool ok = tc_wait(S, 0);
-  tc_hidden_to_a(S, tmem, tid);
-  // layer 2
-  tc_issue(S, tmem, tid, TC_K2, 32, 3, TC_B1_BYTES);
-  ok = tc_wait(S, 1) && ok;
-  tc_hidden_to_a(S, tmem, tid);
-  // layer 3 (N = 16, output in column 0)
-  tc_issue(S, tmem, tid, TC_K2, 16, 3, TC_B1_BYTES + TC_B2_BYTES);
-  ok = tc_wait(S, 0) && ok;
-  const float y = tc_ld1(tmem + ((uint32_t)(tid & ~31) << 16));
-  return ok ? y : __int_as_float(0x7fc00000);
 }
 
 }  // namespace lbm

@@ -185,6 +185,7 @@ struct lbm_ctx {
   float* clo_nu = nullptr;                // held nu_t per cell (closure evaluated every k > 1 steps)
   int clo_since = -1;                     // steps since the last evaluation; -1: evaluate next
   int clo_coef = 0;                       // the network gives Cs^2 (1) or nu_t (0)
+  lbm::CloConst clo_k{};                  // feature range, normalisation, output bounds
 };
 
 namespace lbm {
@@ -317,6 +318,7 @@ int launch_step(lbm_ctx* c, bool mac, double* force) {
     A.nu = c->clo_nu;
     A.omega0 = 1.0f / make_uni<float>(c->P).tau0;
     A.coef = c->clo_coef;
+    A.K = c->clo_k;
     cudaError_t e = c->ops.step_closure(d, c->P, parity(c), mac, force != nullptr, c->clo_engine, mode, A,
                                         cell_launch(c), c->stream);
     if (e != cudaSuccess) return cuda_fail(e, "closure step kernel launch");
@@ -774,6 +776,14 @@ int lbm_set_closure(lbm_ctx* c, const closure_weights* w) {
   lbm::MlpFrag F;
   lbm::closure_pack(w, &F);
   c->clo_coef = w->coef != 0;
+  for (int a = 0; a < 6; ++a) {
+    c->clo_k.lo[a] = F.lo[a];
+    c->clo_k.hi[a] = F.hi[a];
+    c->clo_k.mean[a] = F.mean[a];
+    c->clo_k.inv_std[a] = F.inv_std[a];
+  }
+  c->clo_k.nu_scale = F.nu_scale;
+  c->clo_k.nu_max = F.nu_max;
   if (!c->clo) {
     int r = dalloc(c, (void**)&c->clo, sizeof(lbm::MlpFrag), "closure network");
     if (r) return r;

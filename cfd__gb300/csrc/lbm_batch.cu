@@ -60,12 +60,12 @@ struct BatchArgs {
 };
 static_assert(sizeof(BatchArgs) < 32000, "kernel parameter space");
 
-template <class St, int PAR, bool FAST>
-__global__ void __launch_bounds__(kTile, 8) k_batch_step(const __grid_constant__ BatchArgs A) {
-  // The current tunnel's descriptor, staged in shared memory when a CTA
-  // moves to a tile of another tunnel.
-  __shared__ TunnelDesc D;
-  int cur = -1;
+template <class St, int PAR, bool FAST, int MINB>
+__global__ void __launch_bounds__(kTile, MINB) k_batch_step(const __grid_constant__ BatchArgs A) {
+  // The tunnel of a tile is found by a search over the launch's first-tile
+  // prefix; the index is the same for the whole CTA, so the search and the
+  // descriptor reads (straight from the parameter bank, no staging) run on
+  // the uniform datapath.
   for (int t = blockIdx.x; t < A.ntiles; t += gridDim.x) {
     int lo = 0, hi = A.ntun;
     while (hi - lo > 1) {
@@ -73,22 +73,15 @@ __global__ void __launch_bounds__(kTile, 8) k_batch_step(const __grid_constant__
       if (A.first[mid] <= t) lo = mid;
       else hi = mid;
     }
-    if (lo != cur) {
-      __syncthreads();
-      const uint32_t* src = reinterpret_cast<const uint32_t*>(&A.t[lo]);
-      uint32_t* dst = reinterpret_cast<uint32_t*>(&D);
-      for (int w = threadIdx.x; w < (int)(sizeof(TunnelDesc) / 4); w += kTile) dst[w] = src[w];
-      __syncthreads();
-      cur = lo;
-    }
-    const int tx = D.tx, ty = D.ty, gx = D.gx, gy = D.gy;
+    const TunnelDesc& D = A.t[lo];
+    const int tx = D.tx, gx = D.gx, gy = D.gy;
     const int local = t - A.first[lo];
     const int bxi = local % gx;
     const int rest = local / gx;
     const int byi = rest % gy;
     const int z = rest / gy;
     const int x = bxi * tx + (int)(threadIdx.x % tx);
-    const int y = byi * ty + (int)(threadIdx.x / tx);
+    const int y = byi * D.ty + (int)(threadIdx.x / tx);
     if (x < D.d.nx && y < D.d.ny) step_cell<St, PAR, false, false, false, FAST>(D.d, D.P, D.U, x, y, z);
   }
 }
@@ -125,7 +118,8 @@ struct lbm_batch {
   std::vector<void*> allocs;
   std::vector<BatchArgs> args;       // one per launch of a step (64 tunnels each)
   long long ntiles = 0;
-  int grid = 0;
+  int sms = 1;                       // multiprocessors of the device
+  int minb = 8;                      // resident CTAs per SM the persistent kernel is built for (8 or 6)
   Ops ops{};
   double* partials = nullptr;
   int64_t npart = 0;
@@ -189,12 +183,19 @@ int sync_desc(lbm_batch* b) {
   drop_graphs(b);
   b->args.clear();
   long long total = 0;
+  // tiles of the largest tunnels first: the persistent CTAs then finish with
+  // the small ones, which evens out the tail
+  std::vector<size_t> order(b->host.size());
+  for (size_t k = 0; k < order.size(); ++k) order[k] = k;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](size_t p, size_t q) { return b->host[p].d.N > b->host[q].d.N; });
   for (size_t k0 = 0; k0 < b->host.size(); k0 += kPerLaunch) {
     BatchArgs A;
     memset(&A, 0, sizeof A);
     const size_t k1 = std::min(b->host.size(), k0 + kPerLaunch);
     long long t = 0;
-    for (size_t k = k0; k < k1; ++k) {
+    for (size_t kk = k0; kk < k1; ++kk) {
+      const size_t k = order[kk];
       TunnelDesc& D = b->host[k];
       const int tx = b->tile_req[k] ? b->tile_req[k] : pick_tile(D.d.nx, D.d.ny);
       D.tx = tx;
@@ -202,8 +203,8 @@ int sync_desc(lbm_batch* b) {
       D.gx = (D.d.nx + tx - 1) / tx;
       D.gy = (D.d.ny + D.ty - 1) / D.ty;
       D.tile0 = t;
-      A.first[k - k0] = (int)t;
-      A.t[k - k0] = D;
+      A.first[kk - k0] = (int)t;
+      A.t[kk - k0] = D;
       t += (long long)D.gx * D.gy * D.d.nz;
     }
     if (t >= INT32_MAX) return bfail(LBM_EINVAL, "too many tiles in one launch (keep a batch under 2^31 tiles)");
@@ -218,16 +219,23 @@ int sync_desc(lbm_batch* b) {
   return LBM_OK;
 }
 
+template <class St, bool FAST, int MINB>
+void launch_batch_m(lbm_batch* b, const BatchArgs& A, int parity, int grid) {
+  if (parity == 0) k_batch_step<St, 0, FAST, MINB><<<grid, kTile, 0, b->stream>>>(A);
+  else k_batch_step<St, 1, FAST, MINB><<<grid, kTile, 0, b->stream>>>(A);
+}
+
 template <class St>
 void launch_batch(lbm_batch* b, int parity) {
   for (const BatchArgs& A : b->args) {
-    const int grid = std::min(b->grid, std::max(1, A.ntiles));
+    const int per_sm = b->minb;
+    const int grid = std::min(b->sms * per_sm, std::max(1, A.ntiles));
     if (b->fast) {
-      if (parity == 0) k_batch_step<St, 0, true><<<grid, kTile, 0, b->stream>>>(A);
-      else k_batch_step<St, 1, true><<<grid, kTile, 0, b->stream>>>(A);
+      if (per_sm == 6) launch_batch_m<St, true, 6>(b, A, parity, grid);
+      else launch_batch_m<St, true, 8>(b, A, parity, grid);
     } else {
-      if (parity == 0) k_batch_step<St, 0, false><<<grid, kTile, 0, b->stream>>>(A);
-      else k_batch_step<St, 1, false><<<grid, kTile, 0, b->stream>>>(A);
+      if (per_sm == 6) launch_batch_m<St, false, 6>(b, A, parity, grid);
+      else launch_batch_m<St, false, 8>(b, A, parity, grid);
     }
   }
 }
@@ -336,7 +344,7 @@ int lbm_batch_create(const lbm_dims* dims, int ntunnels, int storage, int flags,
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  b->grid = std::max(1, sms) * 8;   // persistent: 8 resident 128-thread CTAs per SM
+  b->sms = std::max(1, sms);   // persistent: minb resident 128-thread CTAs per SM
   e = cudaStreamSynchronize(b->stream);
   if (e != cudaSuccess) { lbm_batch_destroy(b); return bfail(LBM_ECUDA, "initial clear failed"); }
   *out = b;

@@ -24,6 +24,8 @@
 //    neighbours of src into dst, types gathered per direction.  Kept as the
 //    faithful debug path; both layouts give bit-identical states.
 #pragma once
+#include <algorithm>
+
 #include "closure_mlp.cuh"
 #include "lbm_core.cuh"
 
@@ -130,6 +132,75 @@ struct Deltas {
   }
 };
 
+// Where the in-place step of parity PAR finds the two slots of pair k
+// (i = 2k + 1): slot A = (E ? i + 1 : i) holds, at the cell itself, the
+// pulled g_i and receives g*_{i+1}; slot B = (E ? i : i + 1) holds, at the
+// neighbour x + c_i, the pulled g_{i+1} and receives g*_i.  A bounce-back
+// link re-reads the other slot of the same location (B at the cell, A at
+// the neighbour).
+__host__ __device__ constexpr int slot_a(int k, int par) { return par == 0 ? 2 * k + 2 : 2 * k + 1; }
+__host__ __device__ constexpr int slot_b(int k, int par) { return par == 0 ? 2 * k + 1 : 2 * k + 2; }
+
+// Base pointers of the population slots for one launch of the in-place step
+// (parity-dependent), passed by value in the kernel parameters: an access is
+// then base + element index, formed in one multiply-add with the base read
+// from the constant bank.
+struct SlotPtrs {
+  void* a[9];
+  void* b[9];
+  void* rest;
+};
+
+template <class St>
+inline SlotPtrs make_slots(const Dev& d, int par) {
+  using S = typename St::store_t;
+  SlotPtrs t;
+  S* F = static_cast<S*>(d.pop);
+  for (int k = 0; k < 9; ++k) {
+    t.a[k] = F + (int64_t)slot_a(k, par) * d.N;
+    t.b[k] = F + (int64_t)slot_b(k, par) * d.N;
+  }
+  t.rest = F;
+  return t;
+}
+
+// Addressing of one cell's accesses: from the set's base, the slot offset
+// and the neighbour displacement (AddrSet), or from the launch's slot
+// pointers and the cell / neighbour element indices (AddrSlots).
+template <class St, int PAR, class Off>
+struct AddrSet {
+  using S = typename St::store_t;
+  S* Fc;
+  Off N;
+  Deltas<Off> D;
+  __device__ __forceinline__ AddrSet(const Dev& d, Off cell, int x, int y, int z)
+      : Fc(static_cast<S*>(d.pop) + cell), N((Off)d.N), D(x, y, z, d.nx, d.ny, d.nz) {}
+  __device__ __forceinline__ S* rest() const { return Fc; }
+  __device__ __forceinline__ S* a(int k, bool nb) const {
+    return Fc + (nb ? D.odd(2 * k + 1) : (Off)0) + (Off)slot_a(k, PAR) * N;
+  }
+  __device__ __forceinline__ S* b(int k, bool nb) const {
+    return Fc + (nb ? D.odd(2 * k + 1) : (Off)0) + (Off)slot_b(k, PAR) * N;
+  }
+};
+
+template <class St, int PAR, class Off>
+struct AddrSlots {
+  using S = typename St::store_t;
+  const SlotPtrs& T;
+  Off cell;
+  Deltas<Off> D;
+  __device__ __forceinline__ AddrSlots(const Dev& d, const SlotPtrs& t, Off c, int x, int y, int z)
+      : T(t), cell(c), D(x, y, z, d.nx, d.ny, d.nz) {}
+  __device__ __forceinline__ S* rest() const { return static_cast<S*>(T.rest) + cell; }
+  __device__ __forceinline__ S* a(int k, bool nb) const {
+    return static_cast<S*>(T.a[k]) + (nb ? cell + D.odd(2 * k + 1) : cell);
+  }
+  __device__ __forceinline__ S* b(int k, bool nb) const {
+    return static_cast<S*>(T.b[k]) + (nb ? cell + D.odd(2 * k + 1) : cell);
+  }
+};
+
 // In-place step.  Grid: (ceil(nx/bx), ceil(ny/by), nz), block (bx, by).
 // PAR: step parity (0 even).  MAC: write (u, delta).  FRC: accumulate the
 // momentum-exchange force of the state being streamed.
@@ -137,13 +208,12 @@ struct Deltas {
 // Shared by the single-tunnel kernel and the batched kernel, so both run
 // the identical arithmetic.
 // FRC: the cell's momentum-exchange force goes to d.force (add_force).
-template <class St, int PAR, bool MAC, bool FRC, bool W64, bool FAST>
-__device__ __forceinline__ void step_cell(const Dev& d, const Params& P, const Uni<typename St::real>& U, int x, int y,
-                                          int z) {
+template <class St, int PAR, bool MAC, bool FRC, bool W64, bool FAST, class Addr>
+__device__ __forceinline__ void step_cell_at(const Dev& d, const Params& P, const Uni<typename St::real>& U, int x,
+                                             int y, int z, typename OffT<W64>::type cell, const Addr& ad) {
   double fx = 0.0, fy = 0.0, fz = 0.0;
   using R = typename St::real;
   using S = typename St::store_t;
-  using Off = typename OffT<W64>::type;
   // SC: a form stored times a power-of-two scale (fp16) runs the FAST collide
   // on the stored values themselves (moments_fast_scaled): bit-identical
   // results without a multiply per loaded and per stored population.
@@ -152,88 +222,84 @@ __device__ __forceinline__ void step_cell(const Dev& d, const Params& P, const U
   auto ld = [](const S* p) -> R { return SC ? St::ld_raw(p) : St::ld(p); };
   auto st = [](S* p, R v) { if (SC) St::st_raw(p, v); else St::st(p, v); };
   const int nx = d.nx, ny = d.ny;
-  {
-    const Off N = (Off)d.N;
-    const Off cell = ((Off)z * ny + y) * nx + x;
-    // The normal-slot loads do not wait for the link word: they are issued
-    // together with it, and the rare bounce-back links are re-read below.
-    const uint32_t lw = __ldg(d.link + cell);
-    S* const Fc = static_cast<S*>(d.pop) + cell;
-    const Deltas<Off> D(x, y, z, nx, ny, d.nz);
-    constexpr bool E = (PAR == 0);
-    R g[Q];
-    g[0] = ld(Fc);
+  // The normal-slot loads do not wait for the link word: they are issued
+  // together with it, and the rare bounce-back links are re-read below.
+  const uint32_t lw = __ldg(d.link + cell);
+  R g[Q];
+  g[0] = ld(ad.rest());
 #pragma unroll
-    for (int i = 1; i < Q; i += 2) {
-      g[i] = ld(Fc + (Off)(E ? i + 1 : i) * N);
-      g[i + 1] = ld(Fc + D.odd(i) + (Off)(E ? i : i + 1) * N);
+  for (int k = 0; k < 9; ++k) {
+    g[2 * k + 1] = ld(ad.a(k, false));
+    g[2 * k + 2] = ld(ad.b(k, true));
+  }
+  const uint32_t ct = (lw >> LINK_CLASS_SHIFT) & 7u;
+  if (is_solid(ct)) {
+    if (MAC) d.macros[cell] = make_float4(0.f, 0.f, 0.f, 0.f);
+    return;
+  }
+  const uint32_t bbmask = lw & 0x3ffffu;
+  if (bbmask) {
+#pragma unroll
+    for (int k = 0; k < 9; ++k) {
+      if ((bbmask >> (2 * k)) & 1u) g[2 * k + 1] = ld(ad.b(k, false));
+      if ((bbmask >> (2 * k + 1)) & 1u) g[2 * k + 2] = ld(ad.a(k, true));
     }
-    const uint32_t ct = (lw >> LINK_CLASS_SHIFT) & 7u;
-    if (is_solid(ct)) {
-      if (MAC) d.macros[cell] = make_float4(0.f, 0.f, 0.f, 0.f);
-    } else {
-      {
-        const uint32_t bb = lw & 0x3ffffu;
-        if (bb) {
+    // Bounce-back links: moving-wall term and the fused force (the force
+    // uses the unscaled g: fma(S g, 1/S, w) = RN(g + w)).
+    auto link_q = [&](int k) -> R {
+      return R(2.0) * (SC ? fma_r<R>(g[k], inv_scale, Lit<R>::w(k)) : g[k] + Lit<R>::w(k));
+    };
+    if (lw & LINK_SLOW) {
+      const Wrap w = wrap3(x, y, z, nx, ny, d.nz);
 #pragma unroll
-          for (int i = 1; i < Q; i += 2) {
-            if ((bb >> (i - 1)) & 1u) g[i] = ld(Fc + (Off)(E ? i : i + 1) * N);
-            if ((bb >> i) & 1u) g[i + 1] = ld(Fc + D.odd(i) + (Off)(E ? i + 1 : i) * N);
-          }
+      for (int k = 1; k < Q; ++k) {
+        if (!((bbmask >> (k - 1)) & 1u)) continue;
+        const uint32_t t = d.tipo[nbr(k, -1, x, y, z, w, nx, ny)];
+        if (t == SOLIDO_MOVEL) {
+          const R mw = Lit<R>::sixw(k) * (dotc<R>(k, R(P.belt[0]), R(P.belt[1]), R(P.belt[2])));
+          g[k] = g[k] + (SC ? mw * scale : mw);
+        }
+        if (FRC && ct == FLUIDO && t == SOLIDO) {
+          const R q = link_q(k);
+          fx -= (double)(cx(k) * q); fy -= (double)(cy(k) * q); fz -= (double)(cz(k) * q);
         }
       }
-      // Bounce-back links: moving-wall term and the fused force (the force
-      // uses the unscaled g: fma(S g, 1/S, w) = RN(g + w)).
-      auto link_q = [&](int k) -> R {
-        return R(2.0) * (SC ? fma_r<R>(g[k], inv_scale, Lit<R>::w(k)) : g[k] + Lit<R>::w(k));
-      };
-      const uint32_t bbmask = lw & 0x3ffffu;
-      if (bbmask) {
-        if (lw & LINK_SLOW) {
-          const Wrap w = wrap3(x, y, z, nx, ny, d.nz);
+    } else if (FRC && ct == FLUIDO && (lw & LINK_BODY)) {
 #pragma unroll
-          for (int k = 1; k < Q; ++k) {
-            if (!((bbmask >> (k - 1)) & 1u)) continue;
-            const uint32_t t = d.tipo[nbr(k, -1, x, y, z, w, nx, ny)];
-            if (t == SOLIDO_MOVEL) {
-              const R mw = Lit<R>::sixw(k) * (dotc<R>(k, R(P.belt[0]), R(P.belt[1]), R(P.belt[2])));
-              g[k] = g[k] + (SC ? mw * scale : mw);
-            }
-            if (FRC && ct == FLUIDO && t == SOLIDO) {
-              const R q = link_q(k);
-              fx -= (double)(cx(k) * q); fy -= (double)(cy(k) * q); fz -= (double)(cz(k) * q);
-            }
-          }
-        } else if (FRC && ct == FLUIDO && (lw & LINK_BODY)) {
-#pragma unroll
-          for (int k = 1; k < Q; ++k) {
-            if (!((bbmask >> (k - 1)) & 1u)) continue;
-            const R q = link_q(k);
-            fx -= (double)(cx(k) * q); fy -= (double)(cy(k) * q); fz -= (double)(cz(k) * q);
-          }
-        }
+      for (int k = 1; k < Q; ++k) {
+        if (!((bbmask >> (k - 1)) & 1u)) continue;
+        const R q = link_q(k);
+        fx -= (double)(cx(k) * q); fy -= (double)(cy(k) * q); fz -= (double)(cz(k) * q);
       }
-      if (FRC && (fx != 0.0 || fy != 0.0 || fz != 0.0)) add_force(d.force, fx, fy, fz);
-      R delta, rho, ux, uy, uz, uu, rinv = R(0.0);
-      R sp[9], dp[9];
-      if (SC) moments_fast_scaled<R>(g, inv_scale, sp, dp, delta, rho, ux, uy, uz, uu, rinv);
-      else if (FAST) moments_fast<R>(g, sp, dp, delta, rho, ux, uy, uz, uu, rinv);
-      else moments_strict<R>(g, delta, rho, ux, uy, uz, uu);
-      if (MAC) d.macros[cell] = make_float4((float)ux, (float)uy, (float)uz, (float)(SC ? delta * inv_scale : delta));
-      // g*_i of an odd i goes to the neighbour's slot (E ? i : i+1); g*_{i+1}
-      // stays local in slot (E ? i+1 : i); the rest population stays put.
-      collide<R, FAST, SC>(P, U, ct, x, z, g, sp, dp, delta, rho, ux, uy, uz, uu, rinv, static_cast<const R*>(d.blf),
-                           [&](int i, R v) {
-        if (i == 0) {
-          st(Fc, v);
-        } else if (i & 1) {
-          st(Fc + D.odd(i) + (Off)(E ? i : i + 1) * N, v);
-        } else {
-          st(Fc + (Off)(E ? i : i - 1) * N, v);
-        }
-      }, scale);
     }
-    }
+    if (FRC && (fx != 0.0 || fy != 0.0 || fz != 0.0)) add_force(d.force, fx, fy, fz);
+  }
+  R delta, rho, ux, uy, uz, uu, rinv = R(0.0);
+  R sp[9], dp[9];
+  if (SC) moments_fast_scaled<R>(g, inv_scale, sp, dp, delta, rho, ux, uy, uz, uu, rinv);
+  else if (FAST) moments_fast<R>(g, sp, dp, delta, rho, ux, uy, uz, uu, rinv);
+  else moments_strict<R>(g, delta, rho, ux, uy, uz, uu);
+  if (MAC) d.macros[cell] = make_float4((float)ux, (float)uy, (float)uz, (float)(SC ? delta * inv_scale : delta));
+  // g*_i of an odd i goes to the neighbour's slot B; g*_{i+1} stays local in
+  // slot A; the rest population stays put.
+  collide<R, FAST, SC>(P, U, ct, x, z, g, sp, dp, delta, rho, ux, uy, uz, uu, rinv, static_cast<const R*>(d.blf),
+                       [&](int i, R v) {
+    if (i == 0) st(ad.rest(), v);
+    else if (i & 1) st(ad.b((i - 1) >> 1, true), v);
+    else st(ad.a((i - 2) >> 1, false), v);
+  }, scale);
+}
+
+// One cell of the in-place step (everything the step does for cell x, y, z),
+// addressing from the set's base.  Shared by the batched kernel, so it runs
+// the identical arithmetic.  FRC: the cell's momentum-exchange force goes to
+// d.force (add_force).
+template <class St, int PAR, bool MAC, bool FRC, bool W64, bool FAST>
+__device__ __forceinline__ void step_cell(const Dev& d, const Params& P, const Uni<typename St::real>& U, int x, int y,
+                                          int z) {
+  using Off = typename OffT<W64>::type;
+  const Off cell = ((Off)z * d.ny + y) * d.nx + x;
+  step_cell_at<St, PAR, MAC, FRC, W64, FAST>(d, P, U, x, y, z, cell, AddrSet<St, PAR, Off>(d, cell, x, y, z));
 }
 
 // MINB: minimum resident 128-thread blocks per SM the register allocation
@@ -241,11 +307,15 @@ __device__ __forceinline__ void step_cell(const Dev& d, const Params& P, const U
 // fused force is added where it is computed, so the force variant fits 64 too.
 template <class St, int PAR, bool MAC, bool FRC, bool W64, bool FAST, int MINB>
 __global__ void __launch_bounds__(128, MINB)
-k_step_inplace(Dev d, Params P, Uni<typename St::real> U) {
+k_step_inplace(Dev d, Params P, Uni<typename St::real> U, SlotPtrs T) {
+  using Off = typename OffT<W64>::type;
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int z = blockIdx.z;
-  if (x < d.nx && y < d.ny) step_cell<St, PAR, MAC, FRC, W64, FAST>(d, P, U, x, y, z);
+  if (x < d.nx && y < d.ny) {
+    const Off cell = ((Off)z * d.ny + y) * d.nx + x;
+    step_cell_at<St, PAR, MAC, FRC, W64, FAST>(d, P, U, x, y, z, cell, AddrSlots<St, PAR, Off>(d, T, cell, x, y, z));
+  }
 }
 
 // Arguments of the closure step.
@@ -256,19 +326,14 @@ struct CloArgs {
   float* nu;                    // per-cell output: written by mode 1, read by mode 2
   float omega0;                 // feature x4 = 1 / tau0
   int coef;                     // 1: the output is a Smagorinsky Cs^2, 0: nu_t
+  CloConst K;                   // feature range, normalisation, output bounds
 };
 
-// Shared memory of the two network engines: the warp engine parks a fluid
-// cell's pulled g and moments (a column per thread) while the network runs,
-// so that the registers of the pull and of the network are not live at the
-// same time; the CTA engine holds its MMA operands (closure_tc.cuh).
-template <int ENG>
+// Shared memory of the warp engine: it parks a fluid cell's pulled g and
+// moments (a column per thread) while the network runs, so that the
+// registers of the pull and of the network are not live at the same time.
 struct CloShared {
   float stash[Q + 7][128];
-};
-template <>
-struct CloShared<1> {
-  TcShared tc;
 };
 
 // In-place step with the learned eddy-viscosity closure (fp32 arithmetic,
@@ -283,10 +348,10 @@ struct CloShared<1> {
 // MODE 2: no network: the rates come from the stored nu_t (Smagorinsky where
 //   it is NaN) -- the steps between two network evaluations of a closure
 //   that is evaluated every k-th step.
-// ENG 0: warp engine (closure_mlp.cuh, mma.sync per 32 cells); ENG 1: CTA
-// engine (closure_tc.cuh, tcgen05.mma per 128 cells).  Every other class goes
-// through collide() unchanged, before the network.  Modes 0 and 1 run 64 x 2
-// threads per block; mode 2 any shape.
+// This kernel is the warp engine (closure_mlp.cuh, mma.sync per 32 cells);
+// the CTA engine is k_step_closure_tc below.  Every other class goes through
+// collide() unchanged, before the network.  Modes 0 and 1 run 64 x 2 threads
+// per block; mode 2 any shape.
 template <class St, int PAR, bool MAC, bool FRC, bool W64, int ENG, int MODE>
 __global__ void __launch_bounds__(128, MODE == 2 ? 8 : 6)
 k_step_closure(Dev d, Params P, Uni<float> U, CloArgs A) {
@@ -294,8 +359,9 @@ k_step_closure(Dev d, Params P, Uni<float> U, CloArgs A) {
   using S = typename St::store_t;
   using Off = typename OffT<W64>::type;
   static_assert(sizeof(typename St::real) == 4, "closure step is fp32 arithmetic");
+  static_assert(ENG == 0, "the CTA engine is k_step_closure_tc");
   constexpr bool NET = MODE != 2;
-  __shared__ CloShared<NET ? ENG : 0> SH;
+  __shared__ CloShared SH;
   const int tid = threadIdx.y * blockDim.x + threadIdx.x;
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y * blockDim.y + threadIdx.y;
@@ -307,8 +373,6 @@ k_step_closure(Dev d, Params P, Uni<float> U, CloArgs A) {
   S* const Fc = static_cast<S*>(d.pop) + cell;
   const Deltas<Off> D(x, y, z, nx, ny, d.nz);
   constexpr bool E = (PAR == 0);
-  uint32_t tmem = 0;
-  if constexpr (NET && ENG == 1) tmem = tc_begin(SH.tc, A.F->tcb, tid);
   double fx = 0.0, fy = 0.0, fz = 0.0;
   auto emit = [&](int i, R v) {
     if (i == 0) {
@@ -378,16 +442,14 @@ k_step_closure(Dev d, Params P, Uni<float> U, CloArgs A) {
           closure_features(m.xx - d3 - rux * ux, m.yy - d3 - ruy * uy, m.zz - d3 - ruz * uz, m.xy - rux * uy,
                            m.xz - rux * uz, m.yz - ruy * uz, rinv, delta, feat);
           feat[4] = A.omega0;
-          inside = closure_in_range(*A.F, feat);
+          inside = closure_in_range(A.K, feat);
 #pragma unroll
-          for (int a = 0; a < 6; ++a) feat[a] = (feat[a] - __ldg(&A.F->mean[a])) * __ldg(&A.F->inv_std[a]);
-          if constexpr (ENG == 0) {
+          for (int a = 0; a < 6; ++a) feat[a] = (feat[a] - A.K.mean[a]) * A.K.inv_std[a];
 #pragma unroll
-            for (int i = 0; i < Q; ++i) SH.stash[i][tid] = g[i];
-            SH.stash[Q + 0][tid] = delta; SH.stash[Q + 1][tid] = rho; SH.stash[Q + 2][tid] = ux;
-            SH.stash[Q + 3][tid] = uy; SH.stash[Q + 4][tid] = uz; SH.stash[Q + 5][tid] = uu;
-            SH.stash[Q + 6][tid] = rinv;
-          }
+          for (int i = 0; i < Q; ++i) SH.stash[i][tid] = g[i];
+          SH.stash[Q + 0][tid] = delta; SH.stash[Q + 1][tid] = rho; SH.stash[Q + 2][tid] = ux;
+          SH.stash[Q + 3][tid] = uy; SH.stash[Q + 4][tid] = uz; SH.stash[Q + 5][tid] = uu;
+          SH.stash[Q + 6][tid] = rinv;
         }
       } else {
         collide<R, true>(P, U, ct, x, z, g, sp, dp, delta, rho, ux, uy, uz, uu, rinv, static_cast<const R*>(d.blf),
@@ -397,23 +459,15 @@ k_step_closure(Dev d, Params P, Uni<float> U, CloArgs A) {
   }
   float nu = 0.0f;
   if constexpr (NET) {
-    float yv;
-    if constexpr (ENG == 0) {
-      __syncwarp();
-      yv = warp_mlp(*A.F, feat);
-    } else {
-      yv = tc_mlp(SH.tc, tmem, tid, feat);
-      tc_end(SH.tc, tmem, tid);
-    }
+    __syncwarp();
+    const float yv = warp_mlp(*A.F, feat);
     if (fluid) {
-      if constexpr (ENG == 0) {
 #pragma unroll
-        for (int i = 0; i < Q; ++i) g[i] = SH.stash[i][tid];
-        delta = SH.stash[Q + 0][tid]; rho = SH.stash[Q + 1][tid]; ux = SH.stash[Q + 2][tid];
-        uy = SH.stash[Q + 3][tid]; uz = SH.stash[Q + 4][tid]; uu = SH.stash[Q + 5][tid];
-        rinv = SH.stash[Q + 6][tid];
-      }
-      nu = inside ? closure_nu(*A.F, yv) : __int_as_float(0x7fc00000);
+      for (int i = 0; i < Q; ++i) g[i] = SH.stash[i][tid];
+      delta = SH.stash[Q + 0][tid]; rho = SH.stash[Q + 1][tid]; ux = SH.stash[Q + 2][tid];
+      uy = SH.stash[Q + 3][tid]; uz = SH.stash[Q + 4][tid]; uu = SH.stash[Q + 5][tid];
+      rinv = SH.stash[Q + 6][tid];
+      nu = inside ? closure_nu(A.K, yv) : __int_as_float(0x7fc00000);
       if (MODE == 1) A.nu[cell] = nu;
     }
   } else {
@@ -448,9 +502,155 @@ k_step_closure(Dev d, Params P, Uni<float> U, CloArgs A) {
   if constexpr (NET) {
     const unsigned fb = __ballot_sync(0xffffffffu, fell_back);
     if (fb && (threadIdx.x & 31) == 0 && A.nfb) atomicAdd(A.nfb, (unsigned long long)__popc(fb));
-    if constexpr (ENG == 1)
-      if (tid == 0 && SH.tc.err && A.err) atomicOr(A.err, 1u);
   }
+}
+
+// The learned-closure step on the CTA engine (closure_tc.cuh): persistent
+// CTAs of 128 threads walk tiles of 64 x 2 cells (x, y) of one z plane; a CTA
+// sets up its tensor memory, mbarrier and B operands once.  Per tile every
+// thread pulls its cell exactly as k_step_closure does, collides the
+// boundary classes at once, and for a FLUIDO cell keeps the pulled g and its
+// moments in registers while the three layers run (one CTA barrier and one
+// tcgen05.mma round trip per layer); then the rates and TRT as in
+// k_step_closure.  MODE 0 or 1 (mode 2 has no network: k_step_closure).
+constexpr int kClosureTcPerSm = 4;
+template <class St, int PAR, bool MAC, bool FRC, bool W64, int MODE>
+__global__ void __launch_bounds__(128, kClosureTcPerSm)
+k_step_closure_tc(Dev d, Params P, Uni<float> U, CloArgs A, int gx, int gy, long long ntiles) {
+  using R = float;
+  using S = typename St::store_t;
+  using Off = typename OffT<W64>::type;
+  static_assert(sizeof(typename St::real) == 4, "closure step is fp32 arithmetic");
+  static_assert(MODE != 2, "held steps have no network");
+  __shared__ TcPersist SH;
+  const int tid = threadIdx.x;
+  const uint32_t tmem = tcp_setup(SH, A.F->tcb, tid);
+  uint32_t phase = 0;
+  bool dead = false;
+  unsigned nfb = 0;
+  const int nx = d.nx, ny = d.ny;
+  const Off N = (Off)d.N;
+  constexpr bool E = (PAR == 0);
+  for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int bxi = (int)(t % gx);
+    const long long rest = t / gx;
+    const int byi = (int)(rest % gy);
+    const int z = (int)(rest / gy);
+    const int x = bxi * 64 + (tid & 63), y = byi * 2 + (tid >> 6);
+    const bool inr = x < nx && y < ny;
+    const Off cell = ((Off)z * ny + (inr ? y : 0)) * nx + (inr ? x : 0);
+    S* const Fc = static_cast<S*>(d.pop) + cell;
+    const Deltas<Off> D(inr ? x : 0, inr ? y : 0, z, nx, ny, d.nz);
+    auto emit = [&](int i, R v) {
+      if (i == 0) {
+        St::st(Fc, v);
+      } else if (i & 1) {
+        St::st(Fc + D.odd(i) + (Off)(E ? i : i + 1) * N, v);
+      } else {
+        St::st(Fc + (Off)(E ? i : i - 1) * N, v);
+      }
+    };
+    R g[Q];
+    R delta = R(0.0), rho = R(1.0), ux = R(0.0), uy = R(0.0), uz = R(0.0), uu = R(0.0), rinv = R(1.0);
+    float feat[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    bool fluid = false, inside = false;
+    if (inr) {
+      double fx = 0.0, fy = 0.0, fz = 0.0;
+      const uint32_t lw = __ldg(d.link + cell);
+      g[0] = St::ld(Fc);
+#pragma unroll
+      for (int i = 1; i < Q; i += 2) {
+        g[i] = St::ld(Fc + (Off)(E ? i + 1 : i) * N);
+        g[i + 1] = St::ld(Fc + D.odd(i) + (Off)(E ? i : i + 1) * N);
+      }
+      const uint32_t ct = (lw >> LINK_CLASS_SHIFT) & 7u;
+      if (is_solid(ct)) {
+        if (MAC) d.macros[cell] = make_float4(0.f, 0.f, 0.f, 0.f);
+      } else {
+        const uint32_t bb = lw & 0x3ffffu;
+        if (bb) {
+#pragma unroll
+          for (int i = 1; i < Q; i += 2) {
+            if ((bb >> (i - 1)) & 1u) g[i] = St::ld(Fc + (Off)(E ? i : i + 1) * N);
+            if ((bb >> i) & 1u) g[i + 1] = St::ld(Fc + D.odd(i) + (Off)(E ? i + 1 : i) * N);
+          }
+          if (lw & LINK_SLOW) {
+            const Wrap w = wrap3(x, y, z, nx, ny, d.nz);
+#pragma unroll
+            for (int k = 1; k < Q; ++k) {
+              if (!((bb >> (k - 1)) & 1u)) continue;
+              const uint32_t tk = d.tipo[nbr(k, -1, x, y, z, w, nx, ny)];
+              if (tk == SOLIDO_MOVEL)
+                g[k] = g[k] + Lit<R>::sixw(k) * (dotc<R>(k, R(P.belt[0]), R(P.belt[1]), R(P.belt[2])));
+              if (FRC && ct == FLUIDO && tk == SOLIDO) {
+                const R q = R(2.0) * (g[k] + Lit<R>::w(k));
+                fx -= (double)(cx(k) * q); fy -= (double)(cy(k) * q); fz -= (double)(cz(k) * q);
+              }
+            }
+          } else if (FRC && ct == FLUIDO && (lw & LINK_BODY)) {
+#pragma unroll
+            for (int k = 1; k < Q; ++k) {
+              if (!((bb >> (k - 1)) & 1u)) continue;
+              const R q = R(2.0) * (g[k] + Lit<R>::w(k));
+              fx -= (double)(cx(k) * q); fy -= (double)(cy(k) * q); fz -= (double)(cz(k) * q);
+            }
+          }
+        }
+        if (FRC && (fx != 0.0 || fy != 0.0 || fz != 0.0)) add_force(d.force, fx, fy, fz);
+        R sp[9], dp[9];
+        moments_fast<R>(g, sp, dp, delta, rho, ux, uy, uz, uu, rinv);
+        if (MAC) d.macros[cell] = make_float4(ux, uy, uz, delta);
+        if (ct == FLUIDO) {
+          fluid = true;
+          const PiT<R> m = pi_fast<R>(sp);
+          const R d3 = delta * R(1.0 / 3.0);
+          const R rux = rho * ux, ruy = rho * uy, ruz = rho * uz;
+          closure_features(m.xx - d3 - rux * ux, m.yy - d3 - ruy * uy, m.zz - d3 - ruz * uz, m.xy - rux * uy,
+                           m.xz - rux * uz, m.yz - ruy * uz, rinv, delta, feat);
+          feat[4] = A.omega0;
+          inside = closure_in_range(A.K, feat);
+#pragma unroll
+          for (int a = 0; a < 6; ++a) feat[a] = (feat[a] - A.K.mean[a]) * A.K.inv_std[a];
+        } else {
+          collide<R, true>(P, U, ct, x, z, g, sp, dp, delta, rho, ux, uy, uz, uu, rinv,
+                           static_cast<const R*>(d.blf), emit);
+        }
+      }
+    }
+    const float yv = tcp_mlp(SH, tmem, tid, feat, phase, dead);
+    if (fluid) {
+      const float nu = inside ? closure_nu(A.K, yv) : __int_as_float(0x7fc00000);
+      if (MODE == 1) A.nu[cell] = nu;
+      R sp[9], dp[9];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) {
+        sp[k] = g[2 * k + 1] + g[2 * k + 2];
+        dp[k] = g[2 * k + 1] - g[2 * k + 2];
+      }
+      R e0, ns[9], nd[9];
+      fluid_neq_fast<R>(sp, dp, delta, rho, ux, uy, uz, uu, e0, ns, nd);
+      R omegaP, omegaM;
+      if (nu == nu) {
+        if (A.coef) {
+          smag_rates_c18<R>(P, U, ns, rinv, 18.0f * nu, omegaP, omegaM);
+        } else {
+          const float tauT = U.tau0 + 3.0f * nu, tm = tauT - 0.5f;
+          omegaP = __frcp_rn(tauT);
+          omegaM = __fdividef(tm, fmaf(0.5f, tm, P.magic));
+        }
+      } else {
+        ++nfb;
+        smag_rates_fast<R>(P, U, ns, rinv, omegaP, omegaM);
+      }
+      trt_emit_fast<R>(U, x, g, e0, ns, nd, omegaP, omegaM, U.sp_tf, emit);
+    }
+  }
+  tcp_teardown(SH, tmem, tid, phase, dead);
+  // fallback count: one atomic per warp for the whole kernel
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) nfb += __shfl_down_sync(0xffffffffu, nfb, o);
+  if ((tid & 31) == 0 && nfb && A.nfb) atomicAdd(A.nfb, (unsigned long long)nfb);
+  if (tid == 0 && SH.err && A.err) atomicOr(A.err, 1u);
 }
 
 // A/B ping-pong step: the reference's pull verbatim (tipo gathered per link).
@@ -839,14 +1039,15 @@ struct OpsImpl {
         return;
       }
     }
+    const SlotPtrs T = make_slots<St>(d, PAR);
     // the plain hot-loop variant also exists with a looser register cap
     if (!MAC && !FRC && sizeof(R) == 4 && L.occ == 6) {
-      if (w64) k_step_inplace<St, PAR, MAC, FRC, true, FAST, 6><<<L.grid, L.block, 0, s>>>(d, P, U);
-      else k_step_inplace<St, PAR, MAC, FRC, false, FAST, 6><<<L.grid, L.block, 0, s>>>(d, P, U);
+      if (w64) k_step_inplace<St, PAR, MAC, FRC, true, FAST, 6><<<L.grid, L.block, 0, s>>>(d, P, U, T);
+      else k_step_inplace<St, PAR, MAC, FRC, false, FAST, 6><<<L.grid, L.block, 0, s>>>(d, P, U, T);
       return;
     }
-    if (w64) k_step_inplace<St, PAR, MAC, FRC, true, FAST, kDefault><<<L.grid, L.block, 0, s>>>(d, P, U);
-    else k_step_inplace<St, PAR, MAC, FRC, false, FAST, kDefault><<<L.grid, L.block, 0, s>>>(d, P, U);
+    if (w64) k_step_inplace<St, PAR, MAC, FRC, true, FAST, kDefault><<<L.grid, L.block, 0, s>>>(d, P, U, T);
+    else k_step_inplace<St, PAR, MAC, FRC, false, FAST, kDefault><<<L.grid, L.block, 0, s>>>(d, P, U, T);
   }
   template <bool FAST>
   static void go(const Dev& d, const Params& P, const Uni<R>& U, int parity, bool inplace, bool mac, bool frc,
@@ -901,10 +1102,32 @@ struct OpsImpl {
     else k_mass<St, false><<<L.grid, L.block, 0, s>>>(d, parity, part);
     return cudaGetLastError();
   }
+  // Persistent CTA engine: as many CTAs as fit at once, at most one per tile.
+  template <int PAR, bool MAC, bool FRC, bool W64, int MODE>
+  static void go_closure_tc(const Dev& d, const Params& P, const Uni<float>& U, const CloArgs& A, cudaStream_t s) {
+    if constexpr (sizeof(R) == 4) {
+      auto* k = &k_step_closure_tc<St, PAR, MAC, FRC, W64, MODE>;
+      // the kernel is built for kClosureTcPerSm resident CTAs per SM
+      // (launch bounds), each holding 32 of the SM's 512 TMEM columns
+      int dev = 0, sms = 1;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      const int per_sm = kClosureTcPerSm;
+      const int gx = (d.nx + 63) / 64, gy = (d.ny + 1) / 2;
+      const long long ntiles = (long long)gx * gy * d.nz;
+      const unsigned grid = (unsigned)std::max<long long>(1, std::min<long long>(ntiles, (long long)per_sm * sms));
+      k<<<grid, 128, 0, s>>>(d, P, U, A, gx, gy, ntiles);
+    }
+  }
   template <int PAR, bool MAC, bool FRC, int ENG, int MODE>
   static void go_closure(const Dev& d, const Params& P, const Uni<float>& U, const CloArgs& A, Launch L,
                          cudaStream_t s) {
-    if constexpr (sizeof(R) == 4) {
+    if constexpr (ENG == 1 && MODE != 2) {
+      if ((int64_t)Q * d.N >= (int64_t)INT32_MAX) go_closure_tc<PAR, MAC, FRC, true, MODE>(d, P, U, A, s);
+      else go_closure_tc<PAR, MAC, FRC, false, MODE>(d, P, U, A, s);
+      return;
+    }
+    if constexpr (sizeof(R) == 4 && ENG == 0) {
       // network steps: 64 x 2 threads, four warps (one 128-row MMA tile for
       // engine 1); held steps: the plain step's launch shape
       dim3 block(64, 2), grid((d.nx + 63) / 64, (d.ny + 1) / 2, d.nz);

@@ -203,6 +203,68 @@ def tuneis_fecho(seed=2026):
     return out[0], out[1]
 
 
+def rodar_fecho(g, tipo, esp, area, re, passos, bloco, u=0.06, comprimento=96.0, cs=0.12, closure=None, cada_k=1,
+                colher=None, snapshots=4, intervalo=1000, cronometrar=False, stream=None, motor=0):
+    """One run of the learned-closure workload's tunnel: Re on `comprimento`
+    cells, u_in u, Smagorinsky Cs cs, or the network `closure` (weights
+    dict) evaluated every `cada_k` steps on engine `motor`.  Cd (Maskell,
+    src/core/forces.js:55-95) of the force averaged over each block of
+    `bloco` steps; reported: the mean and std of the second half of the
+    blocks.  colher(s): called at the last `snapshots` states `intervalo`
+    steps apart (training samples)."""
+    import torch
+
+    from .forces import coeficientes
+    from .solver import SolverCUDA
+    from .units import LatticeUnits
+    units = LatticeUnits(u)
+    nu = u * comprimento / re
+    s = SolverCUDA(g, escrever_macros=False)
+    if stream is not None:
+        s.definirStream(stream.cuda_stream)
+    s.definirTipos(tipo)
+    s.configurar(omegaPlus=1.0 / (3.0 * nu + 0.5), lesCs=cs, inletU=[u, 0.0, 0.0], esponja=esp,
+                 closure=cada_k if closure is not None else 0)
+    if closure is not None:
+        s.definirFecho(closure)
+        s.motorFecho(motor)
+        s.estatisticasFecho()
+    s.inicializar()
+    cds, feito, amos = [], 0, []
+    t0 = time.time()
+    while feito < passos:
+        n = min(bloco, passos - feito)
+        f = s.passoComForcas(n)
+        feito += n
+        c = coeficientes(f.mean(axis=0), units, area, g)["cd"]
+        cds.append(c)
+        if not np.isfinite(c) or abs(c) > 100:
+            break
+        if colher is not None and feito > passos - snapshots * intervalo and (passos - feito) % intervalo == 0:
+            amos.append(colher(s))
+    rec = {"Re": re, "omega_plus": 1.0 / (3.0 * nu + 0.5), "steps": feito, "diverged": bool(feito < passos),
+           "wall_s": time.time() - t0}
+    tail = cds[len(cds) // 2:]
+    rec["cd"] = float(np.mean(tail)) if tail and not rec["diverged"] else float("nan")
+    rec["cd_std"] = float(np.std(tail)) if tail and not rec["diverged"] else float("nan")
+    if closure is not None:
+        fb, fl = s.estatisticasFecho()
+        rec["fallback_cells"], rec["network_cell_evaluations"] = fb, fl
+        rec["fallback_rate"] = fb / max(fl, 1)
+    if cronometrar and not rec["diverged"]:
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        st = stream if stream is not None else torch.cuda.current_stream()
+        e0.record(st)
+        s.passo(400)
+        e1.record(st)
+        e1.synchronize()
+        rec["ms_per_step"] = e0.elapsed_time(e1) / 400
+        rec["MLUPS"] = s.N / rec["ms_per_step"] / 1e3
+    s.destruir()
+    return rec, amos
+
+
 def fecho(re_treino=(2000, 5000, 20000), re_teste=10000, passos_finos=24000, snapshots=4, intervalo=1000,
           por_snapshot=300000, passos_treino=3000, cs=0.12, u=0.06, comprimento=96.0, semente=2026,
           s_min=2e-4, escalas=(2.0, 1.0, 0.5, 0.25, 0.125), cada=8, forma="coef", pesos_saida=None):
@@ -236,11 +298,7 @@ def fecho(re_treino=(2000, 5000, 20000), re_teste=10000, passos_finos=24000, sna
     import torch
 
     from .fecho import amostras, avaliar, normalizacao, pesos_vazios, salvar, treinar
-    from .forces import coeficientes
-    from .solver import SolverCUDA
-    from .units import LatticeUnits
     (gc, tc, ec, ac), (gf, tf, ef, af) = tuneis_fecho(semente)
-    units = LatticeUnits(u)
     stream = torch.cuda.Stream()
     rng = np.random.default_rng(semente)
     cx = gc["nx"]
@@ -250,49 +308,9 @@ def fecho(re_treino=(2000, 5000, 20000), re_teste=10000, passos_finos=24000, sna
 
     def rodar(g, tipo, esp, area, re, passos, bloco, closure=None, cada_k=1, colher=None, cs_run=cs,
               cronometrar=False):
-        L = comprimento * g["nx"] / cx
-        nu = u * L / re
-        s = SolverCUDA(g, escrever_macros=False)
-        s.definirStream(stream.cuda_stream)
-        s.definirTipos(tipo)
-        s.configurar(omegaPlus=1.0 / (3.0 * nu + 0.5), lesCs=cs_run, inletU=[u, 0.0, 0.0], esponja=esp,
-                     closure=cada_k if closure is not None else 0)
-        if closure is not None:
-            s.definirFecho(closure)
-            s.estatisticasFecho()
-        s.inicializar()
-        cds, feito, amos = [], 0, []
-        t0 = time.time()
-        while feito < passos:
-            n = min(bloco, passos - feito)
-            f = s.passoComForcas(n)
-            feito += n
-            c = coeficientes(f.mean(axis=0), units, area, g)["cd"]
-            cds.append(c)
-            if not np.isfinite(c) or abs(c) > 100:
-                break
-            if colher is not None and feito > passos - snapshots * intervalo and (passos - feito) % intervalo == 0:
-                amos.append(colher(s))
-        rec = {"Re": re, "omega_plus": 1.0 / (3.0 * nu + 0.5), "steps": feito, "diverged": bool(feito < passos),
-               "wall_s": time.time() - t0}
-        tail = cds[len(cds) // 2:]
-        rec["cd"] = float(np.mean(tail)) if tail and not rec["diverged"] else float("nan")
-        rec["cd_std"] = float(np.std(tail)) if tail and not rec["diverged"] else float("nan")
-        if closure is not None:
-            fb, fl = s.estatisticasFecho()
-            rec["fallback_cells"], rec["network_cell_evaluations"] = fb, fl
-            rec["fallback_rate"] = fb / max(fl, 1)
-        if cronometrar and not rec["diverged"]:
-            torch.cuda.synchronize()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            s.passo(400)
-            e1.record(stream)
-            e1.synchronize()
-            rec["ms_per_step"] = e0.elapsed_time(e1) / 400
-            rec["MLUPS"] = s.N / rec["ms_per_step"] / 1e3
-        s.destruir()
-        return rec, amos
+        return rodar_fecho(g, tipo, esp, area, re, passos, bloco, u=u, comprimento=comprimento * g["nx"] / cx,
+                           cs=cs_run, closure=closure, cada_k=cada_k, colher=colher, snapshots=snapshots,
+                           intervalo=intervalo, cronometrar=cronometrar, stream=stream)
 
     def colhedor(re):
         tau0c = 3.0 * u * comprimento / re + 0.5
