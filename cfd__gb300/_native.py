@@ -13,7 +13,7 @@ import threading
 from . import build as _build
 
 F32, F16S, BF16S, F64 = 0, 1, 2, 3
-FLAG_WRITE_MACROS, FLAG_PINGPONG, FLAG_STRICT = 1, 2, 4
+FLAG_WRITE_MACROS, FLAG_PINGPONG, FLAG_STRICT, FLAG_SOA = 1, 2, 4, 8
 
 OK, EINVAL, ENOMEM, ECUDA, ETIMEDOUT, ESTATE, ENOTSUP = 0, -1, -2, -3, -4, -5, -6
 _NAMES = {EINVAL: "EINVAL", ENOMEM: "ENOMEM", ECUDA: "ECUDA", ETIMEDOUT: "ETIMEDOUT",
@@ -45,7 +45,8 @@ class Params(C.Structure):
 
 class Info(C.Structure):
     _fields_ = [("n_cells", C.c_int64), ("device_bytes", C.c_int64), ("storage", C.c_int32),
-                ("flags", C.c_int32), ("steps", C.c_int64), ("parity", C.c_int32), ("block_x", C.c_int32)]
+                ("flags", C.c_int32), ("steps", C.c_int64), ("parity", C.c_int32), ("block_x", C.c_int32),
+                ("layout", C.c_int32)]
 
 
 class VoxStats(C.Structure):

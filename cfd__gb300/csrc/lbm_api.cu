@@ -142,6 +142,7 @@ struct lbm_ctx {
   int storage = LBM_F32;
   int flags = 0;
   bool inplace = true;
+  bool aos = false;       // in-place set in the AoSoA layout (lbm_kernels.cuh, elem_off)
   Ops ops{};
   void* pop = nullptr;    // in-place set, or ping-pong front
   void* pop2 = nullptr;   // ping-pong back
@@ -232,6 +233,7 @@ Dev dev_of(const lbm_ctx* c) {
   d.macros = c->macros;
   d.force = nullptr;
   d.blf = c->blf_on ? c->blf : nullptr;
+  d.aos = c->aos ? 1 : 0;
   return d;
 }
 
@@ -350,13 +352,18 @@ int lbm_create(const lbm_dims* dims, int storage, int flags, lbm_ctx** out) {
   if (dims->nx < 1 || dims->ny < 1 || dims->nz < 1) return fail(LBM_EINVAL, "grid dimensions must be >= 1");
   if (dims->ny > 65535 * 256 || dims->nz > 65535) return fail(LBM_EINVAL, "grid too large for the launch shape");
   if (storage < LBM_F32 || storage > LBM_F64) return fail(LBM_EINVAL, "unknown storage form");
-  if (flags & ~(LBM_FLAG_WRITE_MACROS | LBM_FLAG_PINGPONG | LBM_FLAG_STRICT)) return fail(LBM_EINVAL, "unknown flag bits");
+  if (flags & ~(LBM_FLAG_WRITE_MACROS | LBM_FLAG_PINGPONG | LBM_FLAG_STRICT | LBM_FLAG_SOA))
+    return fail(LBM_EINVAL, "unknown flag bits");
   lbm_ctx* c = new lbm_ctx();
   c->dims = *dims;
   c->N = (int64_t)dims->nx * dims->ny * dims->nz;
   c->storage = storage;
   c->flags = flags;
   c->inplace = !(flags & LBM_FLAG_PINGPONG);
+  // AoSoA when the in-place FAST step can use it: nx a multiple of the
+  // 32-cell block, fp32 arithmetic, 32-bit element offsets
+  c->aos = c->inplace && !(flags & (LBM_FLAG_SOA | LBM_FLAG_STRICT)) && storage != LBM_F64 && dims->nx % 32 == 0 &&
+           (int64_t)Q * c->N < (int64_t)INT32_MAX;
   c->ops = ops_for(storage);
   const size_t set_bytes = (size_t)c->N * Q * c->ops.elem_bytes;
   int r = dalloc(c, &c->pop, set_bytes, "populations");
@@ -686,7 +693,7 @@ int lbm_save_state(lbm_ctx* c, void* dst, size_t bytes) {
   h.version = LBM_STATE_VERSION;
   h.nx = c->dims.nx; h.ny = c->dims.ny; h.nz = c->dims.nz;
   h.storage = c->storage;
-  h.layout = c->inplace ? 0 : 1;
+  h.layout = c->inplace ? (c->aos ? 2 : 0) : 1;
   h.parity = parity(c);
   h.steps = c->steps;
   h.payload_bytes = need - sizeof h;
@@ -708,7 +715,8 @@ int lbm_load_state(lbm_ctx* c, const void* src, size_t bytes) {
   if (h.nx != c->dims.nx || h.ny != c->dims.ny || h.nz != c->dims.nz)
     return fail(LBM_EINVAL, "checkpoint grid differs from the context's");
   if (h.storage != c->storage) return fail(LBM_EINVAL, "checkpoint storage form differs from the context's");
-  if (h.layout != (c->inplace ? 0 : 1)) return fail(LBM_EINVAL, "checkpoint layout differs from the context's");
+  if (h.layout != (c->inplace ? (c->aos ? 2 : 0) : 1))
+    return fail(LBM_EINVAL, "checkpoint layout differs from the context's");
   if (h.payload_bytes + sizeof h != need || bytes < need) return fail(LBM_EINVAL, "checkpoint size does not match");
   if (c->inplace && h.parity != (int)(h.steps & 1)) return fail(LBM_EINVAL, "checkpoint parity and step count disagree");
   CK(cudaMemcpyAsync(c->pop, static_cast<const char*>(src) + sizeof h, h.payload_bytes, cudaMemcpyHostToDevice, c->stream),
@@ -858,6 +866,7 @@ int lbm_get_info(lbm_ctx* c, lbm_info* info) {
   info->steps = c->steps;
   info->parity = (int)(c->steps & 1);
   info->block_x = (int)cell_launch(c).block.x;
+  info->layout = c->inplace ? (c->aos ? 2 : 0) : 1;
   return LBM_OK;
 }
 

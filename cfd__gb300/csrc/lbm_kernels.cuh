@@ -44,7 +44,21 @@ struct Dev {
   float4* macros;        // nullable
   double* force;         // nullable: kForceSlots x 3 doubles accumulated by the fused force
   const void* blf;       // nullable: nz inlet boundary-layer factors in the arithmetic type
+  int aos;               // in-place set in the AoSoA layout (elem_off) instead of SoA
 };
+
+// The in-place set's two layouts.  SoA: slot k of location c at k N + c.
+// AoSoA (nx a multiple of 32): the cells are cut into blocks of 32 along x;
+// a block holds its 19 slots one after the other, 32 elements each, so
+// slot k of location c sits at (c / 32) 19 * 32 + 32 k + c % 32 =
+// (c & ~31) 19 + 32 k + (c & 31).  A warp's access to one slot still
+// covers 32 consecutive elements, and every slot of a location is a
+// constant offset (32 k elements) from the location's slot 0.
+constexpr int kAosB = 32;
+__host__ __device__ __forceinline__ int64_t aos_base(int64_t c) { return (c & ~(int64_t)(kAosB - 1)) * 19 + (c & (kAosB - 1)); }
+__device__ __forceinline__ int64_t elem_off(const Dev& d, int k, int64_t c) {
+  return d.aos ? aos_base(c) + (int64_t)kAosB * k : (int64_t)k * d.N + c;
+}
 
 struct Wrap {
   int xm, xp, ym, yp, zm, zp;
@@ -72,14 +86,14 @@ __device__ __forceinline__ int64_t nbr(int k, int s, int x, int y, int z, const 
 
 // Where post-collision population k of cell `cell` lives in the in-place
 // layout at parity p (0: before an even step).  Returns the element offset.
-__device__ __forceinline__ int64_t eso_loc(int k, int p, int64_t cell, int x, int y, int z, const Wrap& w,
-                                           int nx, int ny, int64_t N) {
-  if (k == 0) return cell;
+__device__ __forceinline__ int64_t eso_loc(const Dev& d, int k, int p, int64_t cell, int x, int y, int z,
+                                           const Wrap& w) {
+  if (k == 0) return elem_off(d, 0, cell);
   if (k & 1) {  // + member of the pair, stored at the downstream neighbour
-    const int64_t nb = nbr(k, +1, x, y, z, w, nx, ny);
-    return (int64_t)(p == 0 ? k + 1 : k) * N + nb;
+    const int64_t nb = nbr(k, +1, x, y, z, w, d.nx, d.ny);
+    return elem_off(d, p == 0 ? k + 1 : k, nb);
   }
-  return (int64_t)(p == 0 ? k - 1 : k) * N + cell;  // - member, stored locally
+  return elem_off(d, p == 0 ? k - 1 : k, cell);  // - member, stored locally
 }
 
 // Warp-level fp64 sum of three values; lane 0 adds them to dst atomically.
@@ -132,6 +146,11 @@ struct Deltas {
   }
 };
 
+// An integer the compiler must treat as changed here (an empty asm): values
+// derived from it are formed again afterwards instead of being kept live.
+__device__ __forceinline__ void opaque(int32_t& v) { asm volatile("" : "+r"(v)); }
+__device__ __forceinline__ void opaque(int64_t& v) { asm volatile("" : "+l"(v)); }
+
 // Where the in-place step of parity PAR finds the two slots of pair k
 // (i = 2k + 1): slot A = (E ? i + 1 : i) holds, at the cell itself, the
 // pulled g_i and receives g*_{i+1}; slot B = (E ? i : i + 1) holds, at the
@@ -175,6 +194,7 @@ struct AddrSet {
   Deltas<Off> D;
   __device__ __forceinline__ AddrSet(const Dev& d, Off cell, int x, int y, int z)
       : Fc(static_cast<S*>(d.pop) + cell), N((Off)d.N), D(x, y, z, d.nx, d.ny, d.nz) {}
+  __device__ __forceinline__ void refresh() {}
   __device__ __forceinline__ S* rest() const { return Fc; }
   __device__ __forceinline__ S* a(int k, bool nb) const {
     return Fc + (nb ? D.odd(2 * k + 1) : (Off)0) + (Off)slot_a(k, PAR) * N;
@@ -192,6 +212,10 @@ struct AddrSlots {
   Deltas<Off> D;
   __device__ __forceinline__ AddrSlots(const Dev& d, const SlotPtrs& t, Off c, int x, int y, int z)
       : T(t), cell(c), D(x, y, z, d.nx, d.ny, d.nz) {}
+  // Make the index state opaque to the compiler, so that the store addresses
+  // are formed again after the collide instead of being kept in registers
+  // since the loads.
+  __device__ __forceinline__ void refresh() { opaque(cell); }
   __device__ __forceinline__ S* rest() const { return static_cast<S*>(T.rest) + cell; }
   __device__ __forceinline__ S* a(int k, bool nb) const {
     return static_cast<S*>(T.a[k]) + (nb ? cell + D.odd(2 * k + 1) : cell);
@@ -199,6 +223,82 @@ struct AddrSlots {
   __device__ __forceinline__ S* b(int k, bool nb) const {
     return static_cast<S*>(T.b[k]) + (nb ? cell + D.odd(2 * k + 1) : cell);
   }
+};
+
+// Neighbour displacements in AoSoA elements (aos_base(c + d) - aos_base(c)):
+// a y or z displacement is a whole number of blocks, so it is 19 times the
+// cell displacement; +1 in x is +1 inside a block, the next block's lane 0
+// (19 * 32 - 31) from lane 31, and the row's first block from x = nx - 1.
+template <class Off>
+struct DeltasAos {
+  Off xp, yp, ym, zp, zm;
+  __device__ __forceinline__ DeltasAos(int x, int y, int z, int nx, int ny, int nz) {
+    const Deltas<Off> D(x, y, z, nx, ny, nz);
+    constexpr Off next = (Off)(19 * kAosB - (kAosB - 1));
+    xp = (x & (kAosB - 1)) != kAosB - 1 ? (Off)1 : (x == nx - 1 ? next - (Off)19 * (Off)nx : next);
+    yp = (Off)19 * D.yp;
+    ym = (Off)19 * D.ym;
+    zp = (Off)19 * D.zp;
+    zm = (Off)19 * D.zm;
+  }
+  __device__ __forceinline__ Off odd(int i) const {
+    switch (i) {
+      case 1: return xp;
+      case 3: return yp;
+      case 5: return zp;
+      case 7: return xp + yp;
+      case 9: return xp + ym;
+      case 11: return xp + zp;
+      case 13: return xp + zm;
+      case 15: return yp + zp;
+      default: return yp + zm;   // 17
+    }
+  }
+};
+
+// AoSoA addressing: the location's slot-0 element (own cell, or a
+// neighbour's) plus the slot as a constant 32 k elements.
+template <class St, int PAR, class Off>
+struct AddrAos {
+  using S = typename St::store_t;
+  S* F;
+  Off ob;
+  DeltasAos<Off> D;
+  __device__ __forceinline__ AddrAos(const Dev& d, Off cell, int x, int y, int z)
+      : F(static_cast<S*>(d.pop)), ob((Off)aos_base(cell)), D(x, y, z, d.nx, d.ny, d.nz) {}
+  __device__ __forceinline__ void refresh() {
+    opaque(ob); opaque(D.xp); opaque(D.yp); opaque(D.ym); opaque(D.zp); opaque(D.zm);
+  }
+  __device__ __forceinline__ S* rest() const { return F + ob; }
+  __device__ __forceinline__ S* a(int k, bool nb) const {
+    return (F + (nb ? ob + D.odd(2 * k + 1) : ob)) + kAosB * slot_a(k, PAR);
+  }
+  __device__ __forceinline__ S* b(int k, bool nb) const {
+    return (F + (nb ? ob + D.odd(2 * k + 1) : ob)) + kAosB * slot_b(k, PAR);
+  }
+};
+
+// Either layout, chosen per context at run time (d.aos is the same for every
+// thread): the closure steps, whose time goes to the network, not to
+// addressing.
+template <class St, int PAR, class Off>
+struct AddrRt {
+  using S = typename St::store_t;
+  S* F;
+  Off N, own;
+  bool aos;
+  Deltas<Off> D;
+  DeltasAos<Off> DA;
+  __device__ __forceinline__ AddrRt(const Dev& d, Off cell, int x, int y, int z)
+      : F(static_cast<S*>(d.pop)), N((Off)d.N), own(d.aos ? (Off)aos_base(cell) : cell), aos(d.aos != 0),
+        D(x, y, z, d.nx, d.ny, d.nz), DA(x, y, z, d.nx, d.ny, d.nz) {}
+  __device__ __forceinline__ Off at(int slot, int k, bool nb) const {
+    if (aos) return (nb ? own + DA.odd(2 * k + 1) : own) + (Off)(kAosB * slot);
+    return (nb ? own + D.odd(2 * k + 1) : own) + (Off)slot * N;
+  }
+  __device__ __forceinline__ S* rest() const { return F + own; }
+  __device__ __forceinline__ S* a(int k, bool nb) const { return F + at(slot_a(k, PAR), k, nb); }
+  __device__ __forceinline__ S* b(int k, bool nb) const { return F + at(slot_b(k, PAR), k, nb); }
 };
 
 // In-place step.  Grid: (ceil(nx/bx), ceil(ny/by), nz), block (bx, by).
@@ -210,7 +310,7 @@ struct AddrSlots {
 // FRC: the cell's momentum-exchange force goes to d.force (add_force).
 template <class St, int PAR, bool MAC, bool FRC, bool W64, bool FAST, class Addr>
 __device__ __forceinline__ void step_cell_at(const Dev& d, const Params& P, const Uni<typename St::real>& U, int x,
-                                             int y, int z, typename OffT<W64>::type cell, const Addr& ad) {
+                                             int y, int z, typename OffT<W64>::type cell, Addr ad) {
   double fx = 0.0, fy = 0.0, fz = 0.0;
   using R = typename St::real;
   using S = typename St::store_t;
@@ -282,6 +382,7 @@ __device__ __forceinline__ void step_cell_at(const Dev& d, const Params& P, cons
   if (MAC) d.macros[cell] = make_float4((float)ux, (float)uy, (float)uz, (float)(SC ? delta * inv_scale : delta));
   // g*_i of an odd i goes to the neighbour's slot B; g*_{i+1} stays local in
   // slot A; the rest population stays put.
+  ad.refresh();
   collide<R, FAST, SC>(P, U, ct, x, z, g, sp, dp, delta, rho, ux, uy, uz, uu, rinv, static_cast<const R*>(d.blf),
                        [&](int i, R v) {
     if (i == 0) st(ad.rest(), v);
@@ -305,7 +406,7 @@ __device__ __forceinline__ void step_cell(const Dev& d, const Params& P, const U
 // MINB: minimum resident 128-thread blocks per SM the register allocation
 // must allow (8 -> 64 registers, 6 -> 80); the autotuner picks per form.  The
 // fused force is added where it is computed, so the force variant fits 64 too.
-template <class St, int PAR, bool MAC, bool FRC, bool W64, bool FAST, int MINB>
+template <class St, int PAR, bool MAC, bool FRC, bool W64, bool FAST, int MINB, bool AOS = false>
 __global__ void __launch_bounds__(128, MINB)
 k_step_inplace(Dev d, Params P, Uni<typename St::real> U, SlotPtrs T) {
   using Off = typename OffT<W64>::type;
@@ -314,7 +415,11 @@ k_step_inplace(Dev d, Params P, Uni<typename St::real> U, SlotPtrs T) {
   const int z = blockIdx.z;
   if (x < d.nx && y < d.ny) {
     const Off cell = ((Off)z * d.ny + y) * d.nx + x;
-    step_cell_at<St, PAR, MAC, FRC, W64, FAST>(d, P, U, x, y, z, cell, AddrSlots<St, PAR, Off>(d, T, cell, x, y, z));
+    if constexpr (AOS)
+      step_cell_at<St, PAR, MAC, FRC, W64, FAST>(d, P, U, x, y, z, cell, AddrAos<St, PAR, Off>(d, cell, x, y, z));
+    else
+      step_cell_at<St, PAR, MAC, FRC, W64, FAST>(d, P, U, x, y, z, cell,
+                                                 AddrSlots<St, PAR, Off>(d, T, cell, x, y, z));
   }
 }
 
@@ -368,20 +473,13 @@ k_step_closure(Dev d, Params P, Uni<float> U, CloArgs A) {
   const int z = blockIdx.z;
   const int nx = d.nx, ny = d.ny;
   const bool inr = x < nx && y < ny;
-  const Off N = (Off)d.N;
   const Off cell = ((Off)z * ny + y) * nx + x;
-  S* const Fc = static_cast<S*>(d.pop) + cell;
-  const Deltas<Off> D(x, y, z, nx, ny, d.nz);
-  constexpr bool E = (PAR == 0);
+  const AddrRt<St, PAR, Off> ad(d, cell, x, y, z);
   double fx = 0.0, fy = 0.0, fz = 0.0;
   auto emit = [&](int i, R v) {
-    if (i == 0) {
-      St::st(Fc, v);
-    } else if (i & 1) {
-      St::st(Fc + D.odd(i) + (Off)(E ? i : i + 1) * N, v);
-    } else {
-      St::st(Fc + (Off)(E ? i : i - 1) * N, v);
-    }
+    if (i == 0) St::st(ad.rest(), v);
+    else if (i & 1) St::st(ad.b((i - 1) >> 1, true), v);
+    else St::st(ad.a((i - 2) >> 1, false), v);
   };
   R g[Q];
   R delta = R(0.0), rho = R(1.0), ux = R(0.0), uy = R(0.0), uz = R(0.0), uu = R(0.0), rinv = R(1.0);
@@ -389,11 +487,11 @@ k_step_closure(Dev d, Params P, Uni<float> U, CloArgs A) {
   bool fluid = false, inside = false;
   if (inr) {
     const uint32_t lw = __ldg(d.link + cell);
-    g[0] = St::ld(Fc);
+    g[0] = St::ld(ad.rest());
 #pragma unroll
-    for (int i = 1; i < Q; i += 2) {
-      g[i] = St::ld(Fc + (Off)(E ? i + 1 : i) * N);
-      g[i + 1] = St::ld(Fc + D.odd(i) + (Off)(E ? i : i + 1) * N);
+    for (int k = 0; k < 9; ++k) {
+      g[2 * k + 1] = St::ld(ad.a(k, false));
+      g[2 * k + 2] = St::ld(ad.b(k, true));
     }
     const uint32_t ct = (lw >> LINK_CLASS_SHIFT) & 7u;
     if (is_solid(ct)) {
@@ -402,9 +500,9 @@ k_step_closure(Dev d, Params P, Uni<float> U, CloArgs A) {
       const uint32_t bb = lw & 0x3ffffu;
       if (bb) {
 #pragma unroll
-        for (int i = 1; i < Q; i += 2) {
-          if ((bb >> (i - 1)) & 1u) g[i] = St::ld(Fc + (Off)(E ? i : i + 1) * N);
-          if ((bb >> i) & 1u) g[i + 1] = St::ld(Fc + D.odd(i) + (Off)(E ? i + 1 : i) * N);
+        for (int k = 0; k < 9; ++k) {
+          if ((bb >> (2 * k)) & 1u) g[2 * k + 1] = St::ld(ad.b(k, false));
+          if ((bb >> (2 * k + 1)) & 1u) g[2 * k + 2] = St::ld(ad.a(k, true));
         }
         if (lw & LINK_SLOW) {
           const Wrap w = wrap3(x, y, z, nx, ny, d.nz);
@@ -529,8 +627,6 @@ k_step_closure_tc(Dev d, Params P, Uni<float> U, CloArgs A, int gx, int gy, long
   bool dead = false;
   unsigned nfb = 0;
   const int nx = d.nx, ny = d.ny;
-  const Off N = (Off)d.N;
-  constexpr bool E = (PAR == 0);
   for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const int bxi = (int)(t % gx);
     const long long rest = t / gx;
@@ -539,16 +635,11 @@ k_step_closure_tc(Dev d, Params P, Uni<float> U, CloArgs A, int gx, int gy, long
     const int x = bxi * 64 + (tid & 63), y = byi * 2 + (tid >> 6);
     const bool inr = x < nx && y < ny;
     const Off cell = ((Off)z * ny + (inr ? y : 0)) * nx + (inr ? x : 0);
-    S* const Fc = static_cast<S*>(d.pop) + cell;
-    const Deltas<Off> D(inr ? x : 0, inr ? y : 0, z, nx, ny, d.nz);
+    const AddrRt<St, PAR, Off> ad(d, cell, inr ? x : 0, inr ? y : 0, z);
     auto emit = [&](int i, R v) {
-      if (i == 0) {
-        St::st(Fc, v);
-      } else if (i & 1) {
-        St::st(Fc + D.odd(i) + (Off)(E ? i : i + 1) * N, v);
-      } else {
-        St::st(Fc + (Off)(E ? i : i - 1) * N, v);
-      }
+      if (i == 0) St::st(ad.rest(), v);
+      else if (i & 1) St::st(ad.b((i - 1) >> 1, true), v);
+      else St::st(ad.a((i - 2) >> 1, false), v);
     };
     R g[Q];
     R delta = R(0.0), rho = R(1.0), ux = R(0.0), uy = R(0.0), uz = R(0.0), uu = R(0.0), rinv = R(1.0);
@@ -557,11 +648,11 @@ k_step_closure_tc(Dev d, Params P, Uni<float> U, CloArgs A, int gx, int gy, long
     if (inr) {
       double fx = 0.0, fy = 0.0, fz = 0.0;
       const uint32_t lw = __ldg(d.link + cell);
-      g[0] = St::ld(Fc);
+      g[0] = St::ld(ad.rest());
 #pragma unroll
-      for (int i = 1; i < Q; i += 2) {
-        g[i] = St::ld(Fc + (Off)(E ? i + 1 : i) * N);
-        g[i + 1] = St::ld(Fc + D.odd(i) + (Off)(E ? i : i + 1) * N);
+      for (int k = 0; k < 9; ++k) {
+        g[2 * k + 1] = St::ld(ad.a(k, false));
+        g[2 * k + 2] = St::ld(ad.b(k, true));
       }
       const uint32_t ct = (lw >> LINK_CLASS_SHIFT) & 7u;
       if (is_solid(ct)) {
@@ -570,9 +661,9 @@ k_step_closure_tc(Dev d, Params P, Uni<float> U, CloArgs A, int gx, int gy, long
         const uint32_t bb = lw & 0x3ffffu;
         if (bb) {
 #pragma unroll
-          for (int i = 1; i < Q; i += 2) {
-            if ((bb >> (i - 1)) & 1u) g[i] = St::ld(Fc + (Off)(E ? i : i + 1) * N);
-            if ((bb >> i) & 1u) g[i + 1] = St::ld(Fc + D.odd(i) + (Off)(E ? i + 1 : i) * N);
+          for (int k = 0; k < 9; ++k) {
+            if ((bb >> (2 * k)) & 1u) g[2 * k + 1] = St::ld(ad.b(k, false));
+            if ((bb >> (2 * k + 1)) & 1u) g[2 * k + 2] = St::ld(ad.a(k, true));
           }
           if (lw & LINK_SLOW) {
             const Wrap w = wrap3(x, y, z, nx, ny, d.nz);
@@ -730,7 +821,7 @@ __global__ void k_init(Dev d, Params P) {
 #pragma unroll
   for (int k = 0; k < Q; ++k) {
     const R e = equilibrium<R, false>(k, delta, rho, ux, uy, uz, uu, R(0.0));  // init is STRICT in both modes
-    const int64_t off = INPLACE ? eso_loc(k, 0, cell, x, y, z, w, d.nx, d.ny, N) : (int64_t)k * N + cell;
+    const int64_t off = INPLACE ? eso_loc(d, k, 0, cell, x, y, z, w) : (int64_t)k * N + cell;
     St::st(F + off, e);
   }
 }
@@ -746,7 +837,7 @@ __global__ void k_put_dir(Dev d, const double* __restrict__ v, int k, int parity
   if (x >= d.nx || y >= d.ny) return;
   const int64_t cell = ((int64_t)z * d.ny + y) * d.nx + x;
   const Wrap w = wrap3(x, y, z, d.nx, d.ny, d.nz);
-  const int64_t off = INPLACE ? eso_loc(k, parity, cell, x, y, z, w, d.nx, d.ny, d.N) : (int64_t)k * d.N + cell;
+  const int64_t off = INPLACE ? eso_loc(d, k, parity, cell, x, y, z, w) : (int64_t)k * d.N + cell;
   St::st(static_cast<S*>(d.pop) + off, St::from_double(v[cell]));
 }
 
@@ -759,7 +850,7 @@ __global__ void k_get_dir(Dev d, double* __restrict__ v, int k, int parity) {
   if (x >= d.nx || y >= d.ny) return;
   const int64_t cell = ((int64_t)z * d.ny + y) * d.nx + x;
   const Wrap w = wrap3(x, y, z, d.nx, d.ny, d.nz);
-  const int64_t off = INPLACE ? eso_loc(k, parity, cell, x, y, z, w, d.nx, d.ny, d.N) : (int64_t)k * d.N + cell;
+  const int64_t off = INPLACE ? eso_loc(d, k, parity, cell, x, y, z, w) : (int64_t)k * d.N + cell;
   v[cell] = (double)St::ld(static_cast<const S*>(d.pop) + off);
 }
 
@@ -772,7 +863,7 @@ __device__ __forceinline__ void gather_state(const Dev& d, int parity, int64_t c
   const Wrap w = wrap3(x, y, z, d.nx, d.ny, d.nz);
 #pragma unroll
   for (int k = 0; k < Q; ++k) {
-    const int64_t off = INPLACE ? eso_loc(k, parity, cell, x, y, z, w, d.nx, d.ny, d.N) : (int64_t)k * d.N + cell;
+    const int64_t off = INPLACE ? eso_loc(d, k, parity, cell, x, y, z, w) : (int64_t)k * d.N + cell;
     g[k] = St::ld(F + off);
   }
 }
@@ -842,7 +933,7 @@ __global__ void k_forces(Dev d, int parity, double* partials) {
 #pragma unroll
       for (int i = 1; i < Q; ++i) {
         if (d.tipo[nbr(i, +1, x, y, z, w, d.nx, d.ny)] != SOLIDO) continue;
-        const int64_t off = INPLACE ? eso_loc(i, parity, cell, x, y, z, w, d.nx, d.ny, d.N) : (int64_t)i * d.N + cell;
+        const int64_t off = INPLACE ? eso_loc(d, i, parity, cell, x, y, z, w) : (int64_t)i * d.N + cell;
         const R q = R(2.0) * (St::ld(F + off) + Lit<R>::w(i));
         fx += (double)(cx(i) * q); fy += (double)(cy(i) * q); fz += (double)(cz(i) * q);
       }
@@ -1031,7 +1122,7 @@ struct OpsImpl {
     constexpr int kDefault = sizeof(R) == 8 ? 4 : (MAC ? 6 : 8);
     const bool w64 = (int64_t)Q * d.N >= (int64_t)INT32_MAX;
     if constexpr (!MAC && !FRC && sizeof(typename St::store_t) <= 4) {
-      if (L.pipe > 0 && !w64) {
+      if (L.pipe > 0 && !w64 && !d.aos) {
         const dim3 grid((d.nx + 63) / 64, d.ny, (d.nz + L.pipe - 1) / L.pipe);
         if (L.pipe == 4) k_step_pipe<St, PAR, FAST, 4, 64><<<grid, 64, 0, s>>>(d, P, U);
         else if (L.pipe == 8) k_step_pipe<St, PAR, FAST, 8, 64><<<grid, 64, 0, s>>>(d, P, U);
@@ -1040,6 +1131,11 @@ struct OpsImpl {
       }
     }
     const SlotPtrs T = make_slots<St>(d, PAR);
+    if (d.aos) {
+      if constexpr (FAST && sizeof(R) == 4)
+        k_step_inplace<St, PAR, MAC, FRC, false, FAST, kDefault, true><<<L.grid, L.block, 0, s>>>(d, P, U, T);
+      return;
+    }
     // the plain hot-loop variant also exists with a looser register cap
     if (!MAC && !FRC && sizeof(R) == 4 && L.occ == 6) {
       if (w64) k_step_inplace<St, PAR, MAC, FRC, true, FAST, 6><<<L.grid, L.block, 0, s>>>(d, P, U, T);
@@ -1067,6 +1163,7 @@ struct OpsImpl {
   }
   static cudaError_t step(const Dev& d, const Params& P, int parity, bool inplace, bool mac, bool frc, bool fast,
                           Launch L, cudaStream_t s) {
+    if (d.aos && !(fast && kFastOK && inplace)) return cudaErrorNotSupported;   // AoSoA: FAST, in-place only
     const Uni<R> U = make_uni<R>(P, R(St::kScale));
     if (fast && kFastOK) go<kFastOK>(d, P, U, parity, inplace, mac, frc, L, s);
     else go<false>(d, P, U, parity, inplace, mac, frc, L, s);

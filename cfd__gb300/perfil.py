@@ -4,6 +4,7 @@ committed ncu summaries under profiles/ capture.
     python -m cfd__gb300.perfil [--grid 512x256x192|320x160x128]
                                 [--storage f32|f16s|bf16s|f64] [--steps K] [--warmup W]
                                 [--closure K] [--engine 0|1] [--block BX] [--variant MINB]
+                                [--forces] [--soa]
 
 W warm-up steps, then K steps, then a synchronize; prints the wall time.
 The step kernel runs once per step (k_step_inplace, or k_step_closure with
@@ -26,13 +27,15 @@ def main(argv=None):
     ap.add_argument("--engine", type=int, default=0)
     ap.add_argument("--block", type=int, default=0)
     ap.add_argument("--variant", type=int, default=0, help="lbm_set_launch min_blocks code")
+    ap.add_argument("--forces", action="store_true", help="steps with the fused force (passoComForcas)")
+    ap.add_argument("--soa", action="store_true", help="keep the in-place set in the SoA layout")
     a = ap.parse_args(argv)
     from . import build as B
     B.build()
     from .cargas import GRIDS, carga
     from .solver import SolverCUDA
     tipo, cfg, desc = carga(a.grid)
-    s = SolverCUDA(GRIDS[a.grid], storage=a.storage, escrever_macros=False)
+    s = SolverCUDA(GRIDS[a.grid], storage=a.storage, escrever_macros=False, soa=a.soa)
     s.definirTipos(tipo)
     s.configurar(**cfg, closure=a.closure)
     if a.closure:
@@ -42,14 +45,15 @@ def main(argv=None):
     if a.block or a.variant:
         s.definirBloco(a.block or 64, a.variant)
     s.inicializar()
-    s.passo(a.warmup)
+    run = s.passoComForcas if a.forces else s.passo
+    run(a.warmup)
     s.sincronizar()
     t0 = time.perf_counter()
-    s.passo(a.steps)
+    run(a.steps)
     s.sincronizar()
     dt = time.perf_counter() - t0
     N = int(tipo.size)
-    print(f"{desc}: {a.storage}, {a.steps} steps in {dt * 1e3:.2f} ms ({N * a.steps / dt / 1e6:.0f} MLUPS wall)")
+    print(f"{desc}: {a.storage}, layout {s.info()['layout']}, {a.steps} steps in {dt * 1e3:.2f} ms ({N * a.steps / dt / 1e6:.0f} MLUPS wall)")
     s.destruir()
 
 

@@ -33,11 +33,12 @@ def js_round(v: float) -> int:
 class SolverCUDA:
     """A D3Q19 TRT/LES wind tunnel on one GB300, one CUDA stream per solver."""
 
-    def __init__(self, grade, storage="f32", escrever_macros=True, pingpong=False, estrito=False):
+    def __init__(self, grade, storage="f32", escrever_macros=True, pingpong=False, estrito=False, soa=False):
         """storage: "f32" | "f16s" | "bf16s" | "f64"; pingpong: the reference's
         two-set A/B layout instead of the in-place one; estrito: the shader's
         arithmetic read literally (no fused multiply-add) instead of the FAST
-        restatement."""
+        restatement; soa: keep the in-place set in the SoA layout even where
+        the AoSoA layout applies (info()["layout"] says which is in use)."""
         self._lib = nat.load()
         self.nx, self.ny, self.nz = int(grade["nx"]), int(grade["ny"]), int(grade["nz"])
         self.N = self.nx * self.ny * self.nz
@@ -49,7 +50,7 @@ class SolverCUDA:
         self._rampa = None
         self.fontes = {"passo": "cfd__gb300/csrc/lbm_kernels.cuh:k_step_inplace"}
         flags = (nat.FLAG_WRITE_MACROS if escrever_macros else 0) | (nat.FLAG_PINGPONG if pingpong else 0) | \
-            (nat.FLAG_STRICT if estrito else 0)
+            (nat.FLAG_STRICT if estrito else 0) | (nat.FLAG_SOA if soa else 0)
         dims = nat.Dims(self.nx, self.ny, self.nz)
         h = C.c_void_p()
         nat.check(self._lib.lbm_create(C.byref(dims), STORAGE[storage], flags, C.byref(h)))

@@ -80,6 +80,15 @@ extern "C" {
                                      default is the FAST restatement (fixed
                                      fused multiply-adds, u = m (1/rho)); both
                                      are reproduced bit for bit by the oracle */
+#define LBM_FLAG_SOA           8  /* keep the in-place set in the SoA layout
+                                     (slot k of cell c at k N + c).  Default:
+                                     the AoSoA layout (blocks of 32 cells along
+                                     x, their 19 slots one after the other)
+                                     whenever nx is a multiple of 32 and the
+                                     step is the FAST in-place one with fp32
+                                     arithmetic and 19 N < 2^31; SoA otherwise.
+                                     The layout is internal: populations in and
+                                     out are always the natural layout. */
 
 typedef struct lbm_ctx lbm_ctx;
 
@@ -110,6 +119,7 @@ typedef struct {
   int64_t steps;           /* steps done since init / set_populations */
   int32_t parity;          /* steps & 1 — the in-place layout's phase */
   int32_t block_x;         /* chosen launch shape of the step kernel */
+  int32_t layout;          /* population set: 0 in-place SoA, 1 ping-pong, 2 in-place AoSoA */
 } lbm_info;
 
 /* SolverWebGPU.criar (src/backend/webgpu/solver.js:93-124): allocates; fails
