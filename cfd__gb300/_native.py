@@ -101,6 +101,8 @@ SIGNATURES = {
     "lbm_last_error": (C.c_char_p, []),
     "lbm_set_block": (C.c_int, [C.c_void_p, C.c_int]),
     "lbm_set_launch": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "lbm_autotune": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
+                               C.POINTER(C.c_float)]),
     "lbm_forces_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(Dims), C.c_void_p, C.c_void_p]),
     "lbm_batch_create": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_void_p)]),
     "lbm_batch_destroy": (C.c_int, [C.c_void_p]),
@@ -114,6 +116,9 @@ SIGNATURES = {
     "lbm_batch_set_tile": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "lbm_batch_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "lbm_batch_set_mode": (C.c_int, [C.c_void_p, C.c_int]),
+    "lbm_batch_get_tile": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
+    "lbm_batch_autotune": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                     C.POINTER(C.c_float)]),
     "closure_train": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.POINTER(ClosureCfg),
                                 C.POINTER(ClosureWeights), C.c_void_p]),
     "closure_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.POINTER(ClosureWeights),

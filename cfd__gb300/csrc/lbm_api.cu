@@ -9,7 +9,10 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "../../include/lbm.h"
@@ -197,6 +200,16 @@ cudaError_t closure_samples_launch(const float4* mac, const uint8_t* tipo, int n
 
 namespace {
 
+// Launch shapes chosen by lbm_autotune, per (nx, ny, nz, storage, flags,
+// layout), for this process: a context created later with the same key
+// starts with the measured shape.
+struct Shape {
+  int bx, by, occ, pipe;
+};
+using ShapeKey = std::tuple<int, int, int, int, int, int>;
+std::mutex g_tune_mu;
+std::map<ShapeKey, Shape> g_tuned;
+
 Ops ops_for(int storage) {
   switch (storage) {
     case LBM_F32: return ops_f32();
@@ -374,6 +387,13 @@ int lbm_create(const lbm_dims* dims, int storage, int flags, lbm_ctx** out) {
   if (!r) r = dalloc(c, &c->blf, sizeof(double) * (size_t)dims->nz, "inlet boundary-layer factors");
   if (!r && (flags & LBM_FLAG_WRITE_MACROS)) r = ensure_macros(c);
   if (r) { lbm_destroy(c); return r; }
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tuned.find(ShapeKey(dims->nx, dims->ny, dims->nz, storage, flags & ~LBM_FLAG_WRITE_MACROS, c->aos));
+    if (it != g_tuned.end()) {
+      c->block_x = it->second.bx; c->block_y = it->second.by; c->occ = it->second.occ; c->pipe = it->second.pipe;
+    }
+  }
   cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) { lbm_destroy(c); return cuda_fail(e, "cudaStreamCreate"); }
   c->own_stream = true;
@@ -884,10 +904,77 @@ int lbm_set_launch(lbm_ctx* c, int block_x, int min_blocks) {
   return LBM_OK;
 }
 
+int lbm_autotune(lbm_ctx* c, int steps, int* block_x, int* block_y, int* variant, float* ms_per_step) {
+  int r = check_ready(c, true);
+  if (r) return r;
+  if (!c->inplace) return fail(LBM_ENOTSUP, "the tuner times the in-place step");
+  if (!c->state_set) return fail(LBM_ESTATE, "no state yet (initialise or set populations first)");
+  if (steps < 2 || steps > 100000) return fail(LBM_EINVAL, "steps must be in [2, 100000]");
+  // candidates: threads along x and y of the block (<= 128), the register-cap
+  // variant (8 or 6 resident blocks; the AoSoA step is built for 8), and for
+  // the SoA set the pipelined step (cells per thread along z)
+  std::vector<Shape> cand;
+  for (int bx : {32, 64, 128})
+    for (int by : {1, 2, 4})
+      if (bx * by <= 128) cand.push_back({bx, by, 8, 0});
+  if (!c->aos && c->storage != LBM_F64) {
+    cand.push_back({64, 1, 6, 0});
+    cand.push_back({128, 1, 6, 0});
+    if ((int64_t)Q * c->N < (int64_t)INT32_MAX)
+      for (int kz : {4, 8, 16}) cand.push_back({64, 1, 8, kz});
+  }
+  // the state is saved and put back: the trials advance a copy of it
+  const size_t set_bytes = (size_t)c->N * Q * c->ops.elem_bytes;
+  void* keep = nullptr;
+  cudaError_t e = cudaMalloc(&keep, set_bytes);
+  if (e != cudaSuccess) { cudaGetLastError(); return fail(LBM_ENOMEM, "no device memory for the tuner's copy of the state"); }
+  const Shape saved{c->block_x, c->block_y, c->occ, c->pipe};
+  const int64_t steps0 = c->steps;
+  const int since0 = c->clo_since;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  Shape best = saved;
+  float best_ms = 1e30f;
+  e = cudaMemcpyAsync(keep, c->pop, set_bytes, cudaMemcpyDeviceToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  for (size_t q = 0; q < cand.size() && e == cudaSuccess && !r; ++q) {
+    c->block_x = cand[q].bx; c->block_y = cand[q].by; c->occ = cand[q].occ; c->pipe = cand[q].pipe;
+    for (int k = 0; k < 2 && !r; ++k) r = launch_step(c, false, nullptr);   // warm-up
+    e = cudaEventRecord(e0, c->stream);
+    for (int k = 0; k < steps && !r && e == cudaSuccess; ++k) r = launch_step(c, false, nullptr);
+    if (e == cudaSuccess) e = cudaEventRecord(e1, c->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    if (!r && e == cudaSuccess && ms / steps < best_ms) { best_ms = ms / steps; best = cand[q]; }
+  }
+  cudaError_t e2 = cudaMemcpyAsync(c->pop, keep, set_bytes, cudaMemcpyDeviceToDevice, c->stream);
+  if (e2 == cudaSuccess) e2 = cudaStreamSynchronize(c->stream);
+  cudaFree(keep);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  c->steps = steps0;
+  c->clo_since = since0;
+  if (r) { c->block_x = saved.bx; c->block_y = saved.by; c->occ = saved.occ; c->pipe = saved.pipe; return r; }
+  if (e != cudaSuccess) return cuda_fail(e, "tuner");
+  if (e2 != cudaSuccess) return cuda_fail(e2, "tuner state restore");
+  c->block_x = best.bx; c->block_y = best.by; c->occ = best.occ; c->pipe = best.pipe;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tuned[ShapeKey(c->dims.nx, c->dims.ny, c->dims.nz, c->storage, c->flags & ~LBM_FLAG_WRITE_MACROS, c->aos)] = best;
+  }
+  if (block_x) *block_x = best.bx;
+  if (block_y) *block_y = best.by;
+  if (variant) *variant = best.pipe ? 100 + best.pipe : best.occ;
+  if (ms_per_step) *ms_per_step = best_ms;
+  return LBM_OK;
+}
+
 int lbm_set_block(lbm_ctx* c, int block_x) {
   if (!c) return fail(LBM_EINVAL, "null context");
   if (block_x < 0 || block_x > 128 || (block_x % 32) != 0) return fail(LBM_EINVAL, "block_x must be 0 or a multiple of 32 up to 128");
   c->block_x = block_x;
+  c->block_y = 1;
   return LBM_OK;
 }
 

@@ -82,7 +82,17 @@ __global__ void __launch_bounds__(kTile, MINB) k_batch_step(const __grid_constan
     const int z = rest / gy;
     const int x = bxi * tx + (int)(threadIdx.x % tx);
     const int y = byi * D.ty + (int)(threadIdx.x / tx);
-    if (x < D.d.nx && y < D.d.ny) step_cell<St, PAR, false, false, false, FAST>(D.d, D.P, D.U, x, y, z);
+    if (x < D.d.nx && y < D.d.ny) {
+      const int32_t cell = (z * D.d.ny + y) * D.d.nx + x;
+      if constexpr (FAST) {
+        if (D.d.aos) {
+          step_cell_at<St, PAR, false, false, false, FAST>(D.d, D.P, D.U, x, y, z, cell,
+                                                           AddrAos<St, PAR, int32_t>(D.d, cell, x, y, z));
+          continue;
+        }
+      }
+      step_cell<St, PAR, false, false, false, FAST>(D.d, D.P, D.U, x, y, z);
+    }
   }
 }
 
@@ -317,6 +327,7 @@ int lbm_batch_create(const lbm_dims* dims, int ntunnels, int storage, int flags,
     TunnelDesc& D = b->host[k];
     memset(&D, 0, sizeof D);
     D.d.nx = d.nx; D.d.ny = d.ny; D.d.nz = d.nz; D.d.N = N;
+    D.d.aos = (b->fast && d.nx % kAosB == 0) ? 1 : 0;   // the AoSoA layout where the FAST step can use it
     void* p = nullptr;
     const size_t sb = (size_t)N * Q * b->ops.elem_bytes;
     if ((r = balloc(b, &p, sb, "populations"))) break;
@@ -531,6 +542,108 @@ int lbm_batch_set_mode(lbm_batch* b, int mode) {
   if (mode != b->mode) drop_graphs(b);
   b->desc_dirty = true;
   b->mode = mode;
+  return LBM_OK;
+}
+
+int lbm_batch_get_tile(lbm_batch* b, int k, int* tile_x) {
+  if (!b || !tile_x) return bfail(LBM_EINVAL, "null argument");
+  if (k < 0 || k >= (int)b->host.size()) return bfail(LBM_EINVAL, "tunnel index out of range");
+  int r = sync_desc(b);
+  if (r) return r;
+  *tile_x = b->host[k].tx;
+  return LBM_OK;
+}
+
+int lbm_batch_autotune(lbm_batch* b, int steps, int* mode_out, int* minb_out, float* ms_out) {
+  int r = check_ready(b);
+  if (r) return r;
+  if (steps < 1 || steps > 100000) return bfail(LBM_EINVAL, "steps must be in [1, 100000]");
+  const int G = b->graph_steps;
+  const int n = ((steps + G - 1) / G) * G;   // whole graph replays
+  // every tunnel's set is saved and put back: the trials advance copies
+  std::vector<void*> keep(b->host.size(), nullptr);
+  for (size_t k = 0; k < b->host.size(); ++k) {
+    const size_t bytes = (size_t)b->host[k].d.N * Q * b->ops.elem_bytes;
+    if (cudaMalloc(&keep[k], bytes) != cudaSuccess) {
+      cudaGetLastError();
+      for (void* p : keep) if (p) cudaFree(p);
+      return bfail(LBM_ENOMEM, "no device memory for the tuner's copies of the tunnels' states");
+    }
+    cudaMemcpyAsync(keep[k], b->host[k].d.pop, bytes, cudaMemcpyDeviceToDevice, b->stream);
+  }
+  const int64_t steps0 = b->steps;
+  const int mode0 = b->mode, minb0 = b->minb;
+  const std::vector<int> tiles0 = b->tile_req;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  auto trial = [&](float* ms) -> int {
+    b->desc_dirty = true;
+    int q = lbm_batch_step(b, G);   // builds the graphs for this choice
+    if (q) return q;
+    if (cudaEventRecord(e0, b->stream) != cudaSuccess) return bfail(LBM_ECUDA, "tuner event");
+    if ((q = lbm_batch_step(b, n))) return q;
+    cudaEventRecord(e1, b->stream);
+    if (cudaEventSynchronize(e1) != cudaSuccess) return bfail(LBM_ECUDA, "tuner event");
+    cudaEventElapsedTime(ms, e0, e1);
+    *ms /= (float)n;
+    return LBM_OK;
+  };
+  // mode 0 (graph of per-tunnel chains), then mode 1 at both register caps
+  float best = 1e30f, ms = 0.f;
+  int best_mode = 0, best_minb = 8;
+  std::vector<int> best_tiles = tiles0;
+  b->mode = 0;
+  if (!(r = trial(&ms)) && ms < best) { best = ms; best_mode = 0; }
+  float best1 = 1e30f;
+  int minb1 = 8;
+  for (int mb : {8, 6}) {
+    if (r) break;
+    b->mode = 1;
+    b->minb = mb;
+    if (!(r = trial(&ms)) && ms < best1) { best1 = ms; minb1 = mb; }
+  }
+  // mode 1: tile width per size class (tunnels of equal nx), coordinate descent
+  std::vector<int> classes;
+  for (const auto& D : b->host) classes.push_back(D.d.nx);
+  std::sort(classes.begin(), classes.end());
+  classes.erase(std::unique(classes.begin(), classes.end()), classes.end());
+  b->minb = minb1;
+  for (int cls : classes) {
+    int keep_tx = 0;
+    for (int tx : {32, 64, 128}) {
+      if (r) break;
+      std::vector<int> save = b->tile_req;
+      for (size_t k = 0; k < b->host.size(); ++k)
+        if (b->host[k].d.nx == cls) b->tile_req[k] = tx;
+      if (!(r = trial(&ms)) && ms < best1) { best1 = ms; keep_tx = tx; }
+      b->tile_req = save;
+    }
+    if (keep_tx)
+      for (size_t k = 0; k < b->host.size(); ++k)
+        if (b->host[k].d.nx == cls) b->tile_req[k] = keep_tx;
+  }
+  if (!r && best1 < best) { best = best1; best_mode = 1; best_minb = minb1; best_tiles = b->tile_req; }
+  // put the states back
+  for (size_t k = 0; k < b->host.size(); ++k) {
+    const size_t bytes = (size_t)b->host[k].d.N * Q * b->ops.elem_bytes;
+    cudaMemcpyAsync(b->host[k].d.pop, keep[k], bytes, cudaMemcpyDeviceToDevice, b->stream);
+  }
+  cudaError_t e = cudaStreamSynchronize(b->stream);
+  for (void* p : keep) cudaFree(p);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  b->steps = steps0;
+  drop_graphs(b);
+  b->desc_dirty = true;
+  if (r) { b->mode = mode0; b->minb = minb0; b->tile_req = tiles0; return r; }
+  if (e != cudaSuccess) return bfail(LBM_ECUDA, std::string("tuner state restore: ") + cudaGetErrorString(e));
+  b->mode = best_mode;
+  b->minb = best_minb;
+  b->tile_req = best_mode == 1 ? best_tiles : tiles0;
+  if (mode_out) *mode_out = best_mode;
+  if (minb_out) *minb_out = best_minb;
+  if (ms_out) *ms_out = best;
   return LBM_OK;
 }
 

@@ -125,9 +125,13 @@ def precisao(steps=10000, grade=None, forms=("f64", "f32", "f16s", "bf16s"), sam
 
 def lote(n_tunnels=64, steps=256, storages=("f32", "f16s"), seed=2026):
     """Batched workload: n tunnels drawn by sorteio_lote (96x48x48 to
-    256x128x128).  Aggregate MLUPS = sum N_k * steps / time, for the batch
-    (one persistent launch per step, CUDA-graph replay) and for the same
-    tunnels run one after another with the single-tunnel solver."""
+    256x128x128).  Aggregate MLUPS = sum N_k * steps / time, for the batch in
+    mode 0 (a captured graph of per-tunnel chains), in mode 1 (one persistent
+    launch per step over all tunnels' tiles) with the cost model's tiles, in
+    the configuration lbm_batch_autotune measures best (its choices are
+    recorded), and for the same tunnels run one after another with the
+    single-tunnel solver.  Every form is timed over `steps` steps between CUDA
+    events after 64 warm-up steps."""
     import torch
 
     from .lote import LoteCUDA, sorteio_lote
@@ -137,26 +141,41 @@ def lote(n_tunnels=64, steps=256, storages=("f32", "f16s"), seed=2026):
     out = {"tunnels": n_tunnels, "cells": cells, "steps": steps,
            "omega_flagged": int(sum(t[3]["flag_omega"] for t in tun)), "forms": {}}
     stream = torch.cuda.Stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def novo(st, modo):
+        L = LoteCUDA([t[0] for t in tun], storage=st)
+        L.definirStream(stream.cuda_stream)
+        L.definirModo(modo)
+        for k, (g, tipo, cfg, info) in enumerate(tun):
+            L.definirTipos(k, tipo)
+            L.configurar(k, **cfg)
+        L.inicializar()
+        return L
+
+    def cronometrar(L):
+        L.passo(64)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        L.passo(steps)
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1)
+
     for st in storages:
         ms_modes = {}
         for modo in (0, 1):
-            L = LoteCUDA([t[0] for t in tun], storage=st)
-            L.definirStream(stream.cuda_stream)
-            L.definirModo(modo)
-            for k, (g, tipo, cfg, info) in enumerate(tun):
-                L.definirTipos(k, tipo)
-                L.configurar(k, **cfg)
-            L.inicializar()
-            L.passo(64)
-            torch.cuda.synchronize()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            L.passo(steps)
-            e1.record(stream)
-            e1.synchronize()
-            ms_modes[modo] = e0.elapsed_time(e1)
+            L = novo(st, modo)
+            ms_modes[modo] = cronometrar(L)
             L.destruir()
-        ms_batch = ms_modes[0]
+        L = novo(st, 0)
+        L.passo(64)
+        escolha = L.autoajustar(64)
+        ms_tuned = cronometrar(L)
+        classes = {}
+        for k, (g, tipo, cfg, info) in enumerate(tun):
+            classes.setdefault(g["nx"], escolha["tiles"][k])
+        L.destruir()
         ms_seq = 0.0
         for g, tipo, cfg, info in tun:
             s = SolverCUDA(g, storage=st, escrever_macros=False)
@@ -172,10 +191,17 @@ def lote(n_tunnels=64, steps=256, storages=("f32", "f16s"), seed=2026):
             e1.synchronize()
             ms_seq += e0.elapsed_time(e1)
             s.destruir()
-        out["forms"][st] = {"batched_MLUPS": cells * steps / (ms_batch / 1e3) / 1e6,
-                            "persistent_launch_MLUPS": cells * steps / (ms_modes[1] / 1e3) / 1e6,
-                            "sequential_MLUPS": cells * steps / (ms_seq / 1e3) / 1e6,
-                            "speedup": ms_seq / ms_batch}
+        mlups = lambda ms: cells * steps / (ms / 1e3) / 1e6
+        out["forms"][st] = {"mode0_graph_of_chains_MLUPS": mlups(ms_modes[0]),
+                            "mode1_persistent_launch_MLUPS": mlups(ms_modes[1]),
+                            "tuned_MLUPS": mlups(ms_tuned),
+                            "tuner_choice": {"mode": escolha["mode"],
+                                             "resident_ctas_per_sm": escolha["resident_ctas_per_sm"],
+                                             "tile_x_per_nx": {str(k): v for k, v in sorted(classes.items())},
+                                             "measured_ms_per_step": escolha["ms_per_step"]},
+                            "sequential_MLUPS": mlups(ms_seq),
+                            "mode1_vs_sequential": ms_seq / ms_modes[1],
+                            "tuned_vs_sequential": ms_seq / ms_tuned}
     return out
 
 

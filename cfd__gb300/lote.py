@@ -72,6 +72,20 @@ class LoteCUDA:
         """0: graph of per-tunnel chains (default); 1: one persistent launch per step."""
         nat.check(self._lib.lbm_batch_set_mode(self._h, int(modo)))
 
+    def ladrilho(self, k):
+        """Tile width along x of tunnel k in the persistent launch."""
+        t = C.c_int()
+        nat.check(self._lib.lbm_batch_get_tile(self._h, int(k), C.byref(t)))
+        return t.value
+
+    def autoajustar(self, passos=64):
+        """Measured choice of mode, register cap and per-size-class tile
+        width (lbm_batch_autotune); the states are kept."""
+        m, mb, ms = C.c_int(), C.c_int(), C.c_float()
+        nat.check(self._lib.lbm_batch_autotune(self._h, int(passos), C.byref(m), C.byref(mb), C.byref(ms)))
+        return {"mode": m.value, "resident_ctas_per_sm": mb.value, "ms_per_step": ms.value,
+                "tiles": [self.ladrilho(k) for k in range(self.T)]}
+
     def definirStream(self, ptr):
         nat.check(self._lib.lbm_batch_set_stream(self._h, C.c_void_p(ptr)))
 

@@ -262,6 +262,14 @@ class SolverCUDA:
         register-cap variant (min resident blocks per SM: 8 or 6; 0 = default)."""
         nat.check(self._lib.lbm_set_launch(self._h, int(block_x), int(min_blocos)))
 
+    def autoajustar(self, passos=20):
+        """Measure the step kernel's launch shapes on a copy of the current
+        state (lbm_autotune) and keep the fastest: returns the choice and its
+        milliseconds per step."""
+        bx, by, var, ms = C.c_int(), C.c_int(), C.c_int(), C.c_float()
+        nat.check(self._lib.lbm_autotune(self._h, int(passos), C.byref(bx), C.byref(by), C.byref(var), C.byref(ms)))
+        return {"block_x": bx.value, "block_y": by.value, "variant": var.value, "ms_per_step": ms.value}
+
     # --------------------------------------------------------------- state I/O
     def salvarEstado(self) -> bytes:
         """Checkpoint of the population set (include/lbm_state.h)."""

@@ -201,8 +201,22 @@ int lbm_get_info(lbm_ctx* ctx, lbm_info* info);
 const char* lbm_last_error(void);
 
 /* Launch-shape override of the step kernel (threads along x per block; 0 =
- * autotuned).  Used by the autotuner and the benchmark sweep. */
+ * the shape lbm_autotune measured for this grid, storage, flags and layout
+ * earlier in the process, else 64). */
 int lbm_set_block(lbm_ctx* ctx, int block_x);
+
+/* Measured choice of the step kernel's launch: every candidate shape
+ * (threads along x and y of the block, the register-cap variant, and for the
+ * SoA layout the pipelined step) runs `steps` steps timed with CUDA events
+ * on a copy of the current state; the state and the step count are put
+ * back, the fastest shape is applied and remembered for contexts of the
+ * same grid, storage, flags and layout created later in the process.  The
+ * copy takes one population set of device memory for the duration.
+ * Outputs (nullable): the chosen block shape, the variant code of
+ * lbm_set_launch, and the measured milliseconds per step.  No counterpart
+ * in the reference (its workgroup is fixed at 64 x 1 x 1,
+ * src/core/emit/wgsl.js:186). */
+int lbm_autotune(lbm_ctx* ctx, int steps, int* block_x, int* block_y, int* variant, float* ms_per_step);
 
 /* Launch shape plus register-cap variant of the plain step kernel:
  * min_blocks = 8 (64 registers/thread), 6 (80) or 0 (default 8). */

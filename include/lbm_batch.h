@@ -10,7 +10,9 @@
  * tunnel (the GPU overlaps the chains), or (lbm_batch_set_mode 1) one
  * persistent launch per step whose CTAs walk the tiles of every tunnel.  Arithmetic is identical to lbm_step (same per-cell code), so
  * each tunnel's state equals the state a separate lbm_ctx would reach.
- * Storage forms: LBM_F32, LBM_F16S, LBM_BF16S (in-place layout only).
+ * Storage forms: LBM_F32, LBM_F16S, LBM_BF16S (in-place layout only; a
+ * tunnel whose nx is a multiple of 32 keeps its set in the AoSoA layout of
+ * lbm.h's LBM_FLAG_SOA note, unless the batch is LBM_FLAG_STRICT).
  */
 #ifndef CFD_GB300_LBM_BATCH_H
 #define CFD_GB300_LBM_BATCH_H
@@ -47,6 +49,17 @@ int lbm_batch_set_tile(lbm_batch* b, int k, int tile_x);
  * walks the tiles of all tunnels (descriptors in the launch parameters). */
 int lbm_batch_set_mode(lbm_batch* b, int mode);
 int lbm_batch_info(lbm_batch* b, int64_t* total_cells, int64_t* device_bytes);
+/* The tile width along x tunnel k's tiles use in the persistent launch. */
+int lbm_batch_get_tile(lbm_batch* b, int k, int* tile_x);
+/* Measured choice of how the batch steps: mode 0; mode 1 with the kernel
+ * built for 8 or 6 resident 128-thread CTAs per SM; then, for mode 1, the
+ * tile width (32, 64, 128) of each size class (tunnels of equal nx), one
+ * class at a time.  Each candidate runs `steps` steps (rounded up to whole
+ * 32-step graph replays) timed with CUDA events on copies of the tunnels'
+ * states; states and step count are put back, the fastest choice is kept.
+ * The copies take one population set per tunnel of device memory for the
+ * duration.  Outputs (nullable): mode, resident CTAs per SM, ms per step. */
+int lbm_batch_autotune(lbm_batch* b, int steps, int* mode, int* min_blocks, float* ms_per_step);
 
 #ifdef __cplusplus
 }
