@@ -540,6 +540,24 @@ def run_ours(args):
                 s2.destruir()
             variants[st] = row
         forms["step_variants"] = variants
+        # the in-place set's two layouts side by side (AoSoA is the default
+        # where nx is a multiple of 32)
+        lay = {}
+        for st in ("f32", "f16s", "bf16s"):
+            row = {}
+            for name, soa in (("aosoa", False), ("soa", True)):
+                s2 = SolverCUDA(grade, storage=st, escrever_macros=False, soa=soa)
+                s2.definirStream(stream.cuda_stream)
+                s2.definirTipos(tipo)
+                s2.configurar(**cfg)
+                s2.inicializar()
+                s2.passo(args.warmup)
+                ms2, _ = timed(s2, stream, args.steps, min_total_ms=300.0)
+                row[name] = {"MLUPS": N * args.steps / (ms2 / 1e3) / 1e6, "layout": s2.info()["layout"],
+                             "roofline_frac": BYTES_PER_CELL[st] * N / (ms2 / args.steps / 1e3) / 1e9 / peak}
+                s2.destruir()
+            lay[st] = row
+        forms["layouts"] = lay
         # the mesh-body tunnel: its plain step, the learned closure (trained
         # on that tunnel's body) and the visualisation compute
         g2 = GRIDS["320x160x128"]

@@ -392,6 +392,16 @@ __device__ __forceinline__ void smag_rates_c18(const Params& P, const Uni<R>& U,
   omegaM = tm / fma_r<R>(R(0.5), tm, R(P.magic));
 }
 
+// Relaxation rates of a FLUIDO cell for collide(): the Smagorinsky rates by
+// default; the held closure steps supply their own (lbm_kernels.cuh).
+struct SmagRates {
+  template <typename R>
+  __device__ __forceinline__ void operator()(const Params& P, const Uni<R>& U, const R* ns, R rinv, R& omegaP,
+                                             R& omegaM) const {
+    smag_rates_fast<R>(P, U, ns, rinv, omegaP, omegaM);
+  }
+};
+
 // TRT per pair and the sponge blend (src/core/emit/ir.js:304-323, :458-478).
 // spt: the sponge targets in the units of g (U.sp_tf, or U.sp_tfs for
 // populations held times the storage scale).
@@ -439,10 +449,12 @@ __device__ __forceinline__ void trt_emit_fast(const Uni<R>& U, int x, const R* g
 // SC (FAST only): g, sp, dp and delta are held times the power-of-two `scale`
 // (moments_fast_scaled) and the emitted values are too; every operation on
 // them is the unscaled one times the scale, exactly.
-template <typename R, bool FAST, bool SC = false, typename Emit>
+// rates(P, U, ns, rinv, omegaP, omegaM): the FLUIDO cell's relaxation rates
+// in the FAST form (SmagRates: Smagorinsky).
+template <typename R, bool FAST, bool SC = false, typename Emit, typename Rates = SmagRates>
 __device__ __forceinline__ void collide(const Params& P, const Uni<R>& U, uint32_t ct, int x, int z, const R* g,
                                         const R* sp, const R* dp, R delta, R rho, R ux, R uy, R uz, R uu, R rinv,
-                                        const R* blf_tab, Emit&& emit, R scale = R(1.0)) {
+                                        const R* blf_tab, Emit&& emit, R scale = R(1.0), Rates rates = Rates()) {
   static_assert(FAST || !SC, "the scaled form is a FAST restatement");
   if (ct == ESPELHO_Y) {
 #pragma unroll
@@ -508,11 +520,11 @@ __device__ __forceinline__ void collide(const Params& P, const Uni<R>& U, uint32
       // scaled: e = (S rho) a + S delta and the LES term's (S c18 qs) (rinv / S)
       // are S times / exactly the unscaled operations
       fluid_neq_fast<R>(sp, dp, delta, rho * scale, ux, uy, uz, uu, e0, ns, nd);
-      smag_rates_fast<R>(P, U, ns, rinv * (R(1.0) / scale), omegaP, omegaM);
+      rates(P, U, ns, rinv * (R(1.0) / scale), omegaP, omegaM);
       trt_emit_fast<R>(U, x, g, e0, ns, nd, omegaP, omegaM, U.sp_tfs, emit);
     } else {
       fluid_neq_fast<R>(sp, dp, delta, rho, ux, uy, uz, uu, e0, ns, nd);
-      smag_rates_fast<R>(P, U, ns, rinv, omegaP, omegaM);
+      rates(P, U, ns, rinv, omegaP, omegaM);
       trt_emit_fast<R>(U, x, g, e0, ns, nd, omegaP, omegaM, U.sp_tf, emit);
     }
     return;

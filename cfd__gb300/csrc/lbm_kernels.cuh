@@ -308,9 +308,10 @@ struct AddrRt {
 // Shared by the single-tunnel kernel and the batched kernel, so both run
 // the identical arithmetic.
 // FRC: the cell's momentum-exchange force goes to d.force (add_force).
-template <class St, int PAR, bool MAC, bool FRC, bool W64, bool FAST, class Addr>
+template <class St, int PAR, bool MAC, bool FRC, bool W64, bool FAST, class Addr, class Rates = SmagRates>
 __device__ __forceinline__ void step_cell_at(const Dev& d, const Params& P, const Uni<typename St::real>& U, int x,
-                                             int y, int z, typename OffT<W64>::type cell, Addr ad) {
+                                             int y, int z, typename OffT<W64>::type cell, Addr ad,
+                                             Rates rates = Rates()) {
   double fx = 0.0, fy = 0.0, fz = 0.0;
   using R = typename St::real;
   using S = typename St::store_t;
@@ -388,7 +389,7 @@ __device__ __forceinline__ void step_cell_at(const Dev& d, const Params& P, cons
     if (i == 0) st(ad.rest(), v);
     else if (i & 1) st(ad.b((i - 1) >> 1, true), v);
     else st(ad.a((i - 2) >> 1, false), v);
-  }, scale);
+  }, scale, rates);
 }
 
 // One cell of the in-place step (everything the step does for cell x, y, z),
@@ -611,6 +612,52 @@ k_step_closure(Dev d, Params P, Uni<float> U, CloArgs A) {
 // moments in registers while the three layers run (one CTA barrier and one
 // tcgen05.mma round trip per layer); then the rates and TRT as in
 // k_step_closure.  MODE 0 or 1 (mode 2 has no network: k_step_closure).
+// Rates of the closure's held steps (evaluated every k-th step): from the
+// eddy viscosity stored per cell by the last network step, the Smagorinsky
+// rates where it is NaN (a fallback cell) -- the same rules as the network
+// step uses with a fresh output.
+struct HeldRates {
+  const float* nu;
+  int64_t cell;
+  int coef;
+  template <typename R>
+  __device__ __forceinline__ void operator()(const Params& P, const Uni<R>& U, const R* ns, R rinv, R& omegaP,
+                                             R& omegaM) const {
+    const float v = __ldg(nu + cell);
+    if (v == v) {
+      if (coef) {
+        smag_rates_c18<R>(P, U, ns, rinv, 18.0f * v, omegaP, omegaM);
+      } else {
+        const float tauT = U.tau0 + 3.0f * v, tm = tauT - 0.5f;
+        omegaP = __frcp_rn(tauT);
+        omegaM = __fdividef(tm, fmaf(0.5f, tm, P.magic));
+      }
+    } else {
+      smag_rates_fast<R>(P, U, ns, rinv, omegaP, omegaM);
+    }
+  }
+};
+
+// A held closure step: the plain in-place step's cell code and addressing
+// (either layout), with HeldRates for FLUIDO cells.
+template <class St, int PAR, bool MAC, bool FRC, bool AOS>
+__global__ void __launch_bounds__(128, 8) k_step_held(Dev d, Params P, Uni<typename St::real> U, SlotPtrs T,
+                                                      const float* __restrict__ nu, int coef) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int z = blockIdx.z;
+  if (x < d.nx && y < d.ny) {
+    const int32_t cell = (z * d.ny + y) * d.nx + x;
+    const HeldRates rates{nu, cell, coef};
+    if constexpr (AOS)
+      step_cell_at<St, PAR, MAC, FRC, false, true>(d, P, U, x, y, z, cell, AddrAos<St, PAR, int32_t>(d, cell, x, y, z),
+                                                   rates);
+    else
+      step_cell_at<St, PAR, MAC, FRC, false, true>(d, P, U, x, y, z, cell,
+                                                   AddrSlots<St, PAR, int32_t>(d, T, cell, x, y, z), rates);
+  }
+}
+
 constexpr int kClosureTcPerSm = 4;
 template <class St, int PAR, bool MAC, bool FRC, bool W64, int MODE>
 __global__ void __launch_bounds__(128, kClosureTcPerSm)
@@ -1238,6 +1285,15 @@ struct OpsImpl {
   template <int PAR, bool MAC, bool FRC>
   static void go_closure_m(const Dev& d, const Params& P, const Uni<float>& U, int engine, int mode,
                            const CloArgs& A, Launch L, cudaStream_t s) {
+    if constexpr (sizeof(R) == 4) {
+      if (mode == 2 && (int64_t)Q * d.N < (int64_t)INT32_MAX) {
+        const Uni<R> Us = make_uni<R>(P, R(St::kScale));
+        const SlotPtrs T = make_slots<St>(d, PAR);
+        if (d.aos) k_step_held<St, PAR, MAC, FRC, true><<<L.grid, L.block, 0, s>>>(d, P, Us, T, A.nu, A.coef);
+        else k_step_held<St, PAR, MAC, FRC, false><<<L.grid, L.block, 0, s>>>(d, P, Us, T, A.nu, A.coef);
+        return;
+      }
+    }
     if (mode == 2) go_closure<PAR, MAC, FRC, 0, 2>(d, P, U, A, L, s);
     else if (engine == 0) { mode == 1 ? go_closure<PAR, MAC, FRC, 0, 1>(d, P, U, A, L, s) : go_closure<PAR, MAC, FRC, 0, 0>(d, P, U, A, L, s); }
     else { mode == 1 ? go_closure<PAR, MAC, FRC, 1, 1>(d, P, U, A, L, s) : go_closure<PAR, MAC, FRC, 1, 0>(d, P, U, A, L, s); }
