@@ -530,7 +530,9 @@ def run_ours(args):
         variants = {}
         for st in ("f32", "f16s", "bf16s"):
             row = {}
-            for name, code in (("64_registers", 8), ("80_registers", 6)):
+            codes = (("64_registers_recompute_addresses", 8), ("64_registers_keep_addresses", 9)) \
+                if (GRIDS[args.grid]["nx"] % 32 == 0 and st != "f64") else (("64_registers", 8), ("80_registers", 6))
+            for name, code in codes:
                 s2 = make(st)
                 s2.definirBloco(64, code)
                 s2.passo(args.warmup)

@@ -13,7 +13,7 @@ import threading
 from . import build as _build
 
 F32, F16S, BF16S, F64 = 0, 1, 2, 3
-FLAG_WRITE_MACROS, FLAG_PINGPONG, FLAG_STRICT, FLAG_SOA = 1, 2, 4, 8
+FLAG_WRITE_MACROS, FLAG_PINGPONG, FLAG_STRICT, FLAG_SOA, FLAG_AOS = 1, 2, 4, 8, 16
 
 OK, EINVAL, ENOMEM, ECUDA, ETIMEDOUT, ESTATE, ENOTSUP = 0, -1, -2, -3, -4, -5, -6
 _NAMES = {EINVAL: "EINVAL", ENOMEM: "ENOMEM", ECUDA: "ECUDA", ETIMEDOUT: "ETIMEDOUT",
@@ -101,6 +101,8 @@ SIGNATURES = {
     "lbm_last_error": (C.c_char_p, []),
     "lbm_set_block": (C.c_int, [C.c_void_p, C.c_int]),
     "lbm_set_launch": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "lbm_autotune_layout": (C.c_int, [C.POINTER(Dims), C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int),
+                                      C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "lbm_autotune": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int),
                                C.POINTER(C.c_float)]),
     "lbm_forces_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(Dims), C.c_void_p, C.c_void_p]),

@@ -37,7 +37,7 @@ constexpr int TC_B2_BYTES = 32 * TC_K2 * 2;      // 3072
 constexpr int TC_B3_BYTES = 16 * TC_K2 * 2;      // 1536
 constexpr int TC_B_BYTES = TC_B1_BYTES + TC_B2_BYTES + TC_B3_BYTES;   // 5632
 constexpr uint32_t TC_TMEM_COLS = 32;
-constexpr uint32_t TC_WAIT_LIMIT = 1u << 20;     // mbarrier polls (~0.5 us apart) before giving up
+constexpr uint32_t TC_WAIT_LIMIT = 1u << 20;     // suspended mbarrier tries (<= ~1 us each) before giving up
 
 // Byte offset of (row r, element k) in a K-major no-swizzle operand with K
 // elements per row.
@@ -70,24 +70,25 @@ __device__ __forceinline__ void tc_commit(uint64_t* bar) {
                : "memory");
 }
 
-__device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
+// One wait on the phase of the given parity: the hardware suspends the
+// thread until the phase completes or about `hint_ns` nanoseconds pass.
+__device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity, uint32_t hint_ns) {
   uint32_t ok;
   asm volatile(
-      "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+      "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\nselp.u32 %0, 1, 0, p;\n}\n"
       : "=r"(ok)
-      : "r"(smem_addr(bar)), "r"(parity)
+      : "r"(smem_addr(bar)), "r"(parity), "r"(hint_ns)
       : "memory");
   return ok != 0;
 }
 
-// Bounded wait for the phase of the given parity; false when it gave up.
-// Between polls the warp sleeps, leaving the issue slots to the CTAs that
-// are streaming populations.
+// Bounded wait for the phase of the given parity; false when it gave up
+// (after TC_WAIT_LIMIT suspended tries of up to a microsecond each).  A
+// suspended warp leaves the issue slots to the CTAs that are streaming
+// populations.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
-  for (uint32_t i = 0; i < TC_WAIT_LIMIT; ++i) {
-    if (mbar_try(bar, parity)) return true;
-    __nanosleep(i < 4 ? 128u : 512u);
-  }
+  for (uint32_t i = 0; i < TC_WAIT_LIMIT; ++i)
+    if (mbar_try(bar, parity, 1000u)) return true;
   return false;
 }
 

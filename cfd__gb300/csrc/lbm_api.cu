@@ -209,6 +209,9 @@ struct Shape {
 using ShapeKey = std::tuple<int, int, int, int, int, int>;
 std::mutex g_tune_mu;
 std::map<ShapeKey, Shape> g_tuned;
+// Layouts chosen by lbm_autotune_layout, per (nx, ny, nz, storage, flags).
+using LayoutKey = std::tuple<int, int, int, int, int>;
+std::map<LayoutKey, bool> g_layout;
 
 Ops ops_for(int storage) {
   switch (storage) {
@@ -365,18 +368,31 @@ int lbm_create(const lbm_dims* dims, int storage, int flags, lbm_ctx** out) {
   if (dims->nx < 1 || dims->ny < 1 || dims->nz < 1) return fail(LBM_EINVAL, "grid dimensions must be >= 1");
   if (dims->ny > 65535 * 256 || dims->nz > 65535) return fail(LBM_EINVAL, "grid too large for the launch shape");
   if (storage < LBM_F32 || storage > LBM_F64) return fail(LBM_EINVAL, "unknown storage form");
-  if (flags & ~(LBM_FLAG_WRITE_MACROS | LBM_FLAG_PINGPONG | LBM_FLAG_STRICT | LBM_FLAG_SOA))
+  if (flags & ~(LBM_FLAG_WRITE_MACROS | LBM_FLAG_PINGPONG | LBM_FLAG_STRICT | LBM_FLAG_SOA | LBM_FLAG_AOS))
     return fail(LBM_EINVAL, "unknown flag bits");
+  if ((flags & LBM_FLAG_SOA) && (flags & LBM_FLAG_AOS)) return fail(LBM_EINVAL, "LBM_FLAG_SOA and LBM_FLAG_AOS together");
   lbm_ctx* c = new lbm_ctx();
   c->dims = *dims;
   c->N = (int64_t)dims->nx * dims->ny * dims->nz;
   c->storage = storage;
   c->flags = flags;
   c->inplace = !(flags & LBM_FLAG_PINGPONG);
-  // AoSoA when the in-place FAST step can use it: nx a multiple of the
-  // 32-cell block, fp32 arithmetic, 32-bit element offsets
-  c->aos = c->inplace && !(flags & (LBM_FLAG_SOA | LBM_FLAG_STRICT)) && storage != LBM_F64 && dims->nx % 32 == 0 &&
-           (int64_t)Q * c->N < (int64_t)INT32_MAX;
+  // AoSoA where the in-place FAST step can use it (nx a multiple of the
+  // 32-cell block, fp32 arithmetic, 32-bit element offsets) and it is the
+  // layout asked for, the one lbm_autotune_layout measured faster for this
+  // grid, or by default for fp32 storage (measured on GB300: faster for fp32,
+  // slower than SoA for the 16-bit forms)
+  const bool aos_ok = c->inplace && !(flags & LBM_FLAG_STRICT) && storage != LBM_F64 && dims->nx % 32 == 0 &&
+                      (int64_t)Q * c->N < (int64_t)INT32_MAX;
+  bool want_aos = storage == LBM_F32;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_layout.find(LayoutKey(dims->nx, dims->ny, dims->nz, storage, flags & ~LBM_FLAG_WRITE_MACROS));
+    if (it != g_layout.end()) want_aos = it->second;
+  }
+  if (flags & LBM_FLAG_AOS) want_aos = true;
+  if (flags & LBM_FLAG_SOA) want_aos = false;
+  c->aos = aos_ok && want_aos;
   c->ops = ops_for(storage);
   const size_t set_bytes = (size_t)c->N * Q * c->ops.elem_bytes;
   int r = dalloc(c, &c->pop, set_bytes, "populations");
@@ -894,9 +910,11 @@ int lbm_set_launch(lbm_ctx* c, int block_x, int min_blocks) {
   if (!c) return fail(LBM_EINVAL, "null context");
   // min_blocks 4/8/16 with block_x = 64 selects the pipelined step with that
   // many cells per thread along z
-  if (min_blocks != 0 && min_blocks != 6 && min_blocks != 8 && min_blocks != 104 && min_blocks != 108 &&
-      min_blocks != 116)
-    return fail(LBM_EINVAL, "min_blocks must be 0, 6, 8, or 100 + cells per thread (4, 8, 16) for the pipelined step");
+  if (min_blocks != 0 && min_blocks != 6 && min_blocks != 8 && min_blocks != 9 && min_blocks != 104 &&
+      min_blocks != 108 && min_blocks != 116)
+    return fail(LBM_EINVAL,
+                "min_blocks must be 0, 6, 8, 9 (AoSoA: addresses kept from load to store), or 100 + cells per "
+                "thread (4, 8, 16) for the pipelined step");
   int r = lbm_set_block(c, block_x);
   if (r) return r;
   if (min_blocks >= 100) { c->pipe = min_blocks - 100; c->occ = 8; }
@@ -916,7 +934,10 @@ int lbm_autotune(lbm_ctx* c, int steps, int* block_x, int* block_y, int* variant
   std::vector<Shape> cand;
   for (int bx : {32, 64, 128})
     for (int by : {1, 2, 4})
-      if (bx * by <= 128) cand.push_back({bx, by, 8, 0});
+      if (bx * by <= 128) {
+        cand.push_back({bx, by, 8, 0});
+        if (c->aos) cand.push_back({bx, by, 9, 0});
+      }
   if (!c->aos && c->storage != LBM_F64) {
     cand.push_back({64, 1, 6, 0});
     cand.push_back({128, 1, 6, 0});
@@ -967,6 +988,55 @@ int lbm_autotune(lbm_ctx* c, int steps, int* block_x, int* block_y, int* variant
   if (block_y) *block_y = best.by;
   if (variant) *variant = best.pipe ? 100 + best.pipe : best.occ;
   if (ms_per_step) *ms_per_step = best_ms;
+  return LBM_OK;
+}
+
+int lbm_autotune_layout(const lbm_dims* dims, int storage, int flags, int steps, int* layout, float* ms_aos,
+                        float* ms_soa) {
+  if (!dims || !layout) return fail(LBM_EINVAL, "null argument");
+  if (steps < 2 || steps > 100000) return fail(LBM_EINVAL, "steps must be in [2, 100000]");
+  flags &= ~(LBM_FLAG_SOA | LBM_FLAG_AOS | LBM_FLAG_WRITE_MACROS);
+  float ms[2] = {0.f, 0.f};
+  int lay[2] = {0, 0};
+  // the same free stream in an all-fluid box of this grid, once per layout
+  for (int q = 0; q < 2; ++q) {
+    lbm_ctx* c = nullptr;
+    int r = lbm_create(dims, storage, flags | (q == 0 ? LBM_FLAG_AOS : LBM_FLAG_SOA), &c);
+    if (r) return r;
+    lay[q] = c->inplace ? (c->aos ? 2 : 0) : 1;
+    lbm_params p{};
+    p.omega_plus = 1.9f; p.magic = 0.1875f; p.les_cs = 0.1f;
+    p.inlet_u[0] = 0.05f;
+    p.sponge_start = (float)dims->nx + 10.0f; p.sponge_len = 4.0f;
+    std::vector<uint32_t> t((size_t)c->N, 0u);
+    r = lbm_configure(c, &p);
+    if (!r) r = lbm_set_types(c, t.data(), t.size());
+    if (!r) r = lbm_init_equilibrium(c);
+    if (!r) r = lbm_step(c, 2);
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t e = cudaSuccess;
+    if (!r) e = cudaEventCreate(&e0);
+    if (!r && e == cudaSuccess) e = cudaEventCreate(&e1);
+    if (!r && e == cudaSuccess) e = cudaEventRecord(e0, c->stream);
+    if (!r && e == cudaSuccess) r = lbm_step(c, steps);
+    if (!r && e == cudaSuccess) e = cudaEventRecord(e1, c->stream);
+    if (!r && e == cudaSuccess) e = cudaEventSynchronize(e1);
+    if (!r && e == cudaSuccess) e = cudaEventElapsedTime(&ms[q], e0, e1);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    lbm_destroy(c);
+    if (r) return r;
+    if (e != cudaSuccess) return cuda_fail(e, "layout tuner");
+    ms[q] /= (float)steps;
+  }
+  const bool aos = lay[0] == 2 && ms[0] < ms[1];
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_layout[LayoutKey(dims->nx, dims->ny, dims->nz, storage, flags)] = aos;
+  }
+  *layout = aos ? 2 : lay[1];
+  if (ms_aos) *ms_aos = lay[0] == 2 ? ms[0] : -1.f;
+  if (ms_soa) *ms_soa = ms[1];
   return LBM_OK;
 }
 

@@ -322,21 +322,24 @@ inline Uni<R> make_uni(const Params& P, R scale = R(1.0)) {
 // Pair form of the shifted equilibrium (c_j = -c_i, w_j = w_i):
 //   e_i + e_j = 2 w (delta + rho (4.5 cu^2 - 1.5 uu)),  e_i - e_j = 6 w rho cu;
 // ns = (g_i + g_j) - (e_i + e_j), nd = (g_i - g_j) - (e_i - e_j).
+// Fused as: B = fma(-rho, 1.5 uu, delta) once per cell (e0 = w0 B), then per
+// pair E = fma(4.5 rho cu, cu, B), ns = fma(-2w, E, s), nd = fma(-6 w rho, cu, d):
+// four operations a pair.
 template <typename R>
 __device__ __forceinline__ void fluid_neq_fast(const R* sp, const R* dp, R delta, R rho, R ux, R uy, R uz, R uu,
                                                R& e0, R* ns, R* nd) {
   const R uu15 = R(1.5) * uu;
-  e0 = Lit<R>::w(0) * fma_r<R>(-rho, uu15, delta);
+  const R B = fma_r<R>(-rho, uu15, delta);
+  e0 = Lit<R>::w(0) * B;
+  const R a45 = R(4.5) * rho;
   const R r6a = (R(6.0) * Lit<R>::w(1)) * rho, r6d = (R(6.0) * Lit<R>::w(7)) * rho;
 #pragma unroll
   for (int k = 0; k < 9; ++k) {
     const int i = 2 * k + 1;
     const R cu = dotc<R>(i, ux, uy, uz);
-    const R a2 = fma_r<R>(R(4.5) * cu, cu, -uu15);
-    const R es = (R(2.0) * Lit<R>::w(i)) * fma_r<R>(rho, a2, delta);
-    const R ed = (i <= 6 ? r6a : r6d) * cu;
-    ns[k] = sp[k] - es;
-    nd[k] = dp[k] - ed;
+    const R E = fma_r<R>(a45 * cu, cu, B);
+    ns[k] = fma_r<R>(-(R(2.0) * Lit<R>::w(i)), E, sp[k]);
+    nd[k] = fma_r<R>(-(i <= 6 ? r6a : r6d), cu, dp[k]);
   }
 }
 

@@ -25,6 +25,7 @@
 //    faithful debug path; both layouts give bit-identical states.
 #pragma once
 #include <algorithm>
+#include <type_traits>
 
 #include "closure_mlp.cuh"
 #include "lbm_core.cuh"
@@ -212,10 +213,7 @@ struct AddrSlots {
   Deltas<Off> D;
   __device__ __forceinline__ AddrSlots(const Dev& d, const SlotPtrs& t, Off c, int x, int y, int z)
       : T(t), cell(c), D(x, y, z, d.nx, d.ny, d.nz) {}
-  // Make the index state opaque to the compiler, so that the store addresses
-  // are formed again after the collide instead of being kept in registers
-  // since the loads.
-  __device__ __forceinline__ void refresh() { opaque(cell); }
+  __device__ __forceinline__ void refresh() {}
   __device__ __forceinline__ S* rest() const { return static_cast<S*>(T.rest) + cell; }
   __device__ __forceinline__ S* a(int k, bool nb) const {
     return static_cast<S*>(T.a[k]) + (nb ? cell + D.odd(2 * k + 1) : cell);
@@ -257,8 +255,11 @@ struct DeltasAos {
 };
 
 // AoSoA addressing: the location's slot-0 element (own cell, or a
-// neighbour's) plus the slot as a constant 32 k elements.
-template <class St, int PAR, class Off>
+// neighbour's) plus the slot as a constant 32 k elements.  RF: make the index
+// state opaque to the compiler before the collide, so that the store
+// addresses are formed again instead of being kept in registers since the
+// loads (fewer live registers, more instructions); the tuner picks.
+template <class St, int PAR, class Off, bool RF = true>
 struct AddrAos {
   using S = typename St::store_t;
   S* F;
@@ -267,7 +268,7 @@ struct AddrAos {
   __device__ __forceinline__ AddrAos(const Dev& d, Off cell, int x, int y, int z)
       : F(static_cast<S*>(d.pop)), ob((Off)aos_base(cell)), D(x, y, z, d.nx, d.ny, d.nz) {}
   __device__ __forceinline__ void refresh() {
-    opaque(ob); opaque(D.xp); opaque(D.yp); opaque(D.ym); opaque(D.zp); opaque(D.zm);
+    if constexpr (RF) { opaque(ob); opaque(D.xp); opaque(D.yp); opaque(D.ym); opaque(D.zp); opaque(D.zm); }
   }
   __device__ __forceinline__ S* rest() const { return F + ob; }
   __device__ __forceinline__ S* a(int k, bool nb) const {
@@ -407,7 +408,7 @@ __device__ __forceinline__ void step_cell(const Dev& d, const Params& P, const U
 // MINB: minimum resident 128-thread blocks per SM the register allocation
 // must allow (8 -> 64 registers, 6 -> 80); the autotuner picks per form.  The
 // fused force is added where it is computed, so the force variant fits 64 too.
-template <class St, int PAR, bool MAC, bool FRC, bool W64, bool FAST, int MINB, bool AOS = false>
+template <class St, int PAR, bool MAC, bool FRC, bool W64, bool FAST, int MINB, bool AOS = false, bool RF = true>
 __global__ void __launch_bounds__(128, MINB)
 k_step_inplace(Dev d, Params P, Uni<typename St::real> U, SlotPtrs T) {
   using Off = typename OffT<W64>::type;
@@ -417,7 +418,8 @@ k_step_inplace(Dev d, Params P, Uni<typename St::real> U, SlotPtrs T) {
   if (x < d.nx && y < d.ny) {
     const Off cell = ((Off)z * d.ny + y) * d.nx + x;
     if constexpr (AOS)
-      step_cell_at<St, PAR, MAC, FRC, W64, FAST>(d, P, U, x, y, z, cell, AddrAos<St, PAR, Off>(d, cell, x, y, z));
+      step_cell_at<St, PAR, MAC, FRC, W64, FAST>(d, P, U, x, y, z, cell,
+                                                 AddrAos<St, PAR, Off, RF>(d, cell, x, y, z));
     else
       step_cell_at<St, PAR, MAC, FRC, W64, FAST>(d, P, U, x, y, z, cell,
                                                  AddrSlots<St, PAR, Off>(d, T, cell, x, y, z));
@@ -617,13 +619,11 @@ k_step_closure(Dev d, Params P, Uni<float> U, CloArgs A) {
 // rates where it is NaN (a fallback cell) -- the same rules as the network
 // step uses with a fresh output.
 struct HeldRates {
-  const float* nu;
-  int64_t cell;
+  float v;     // the cell's stored eddy viscosity (or Cs^2), loaded with the populations
   int coef;
   template <typename R>
   __device__ __forceinline__ void operator()(const Params& P, const Uni<R>& U, const R* ns, R rinv, R& omegaP,
                                              R& omegaM) const {
-    const float v = __ldg(nu + cell);
     if (v == v) {
       if (coef) {
         smag_rates_c18<R>(P, U, ns, rinv, 18.0f * v, omegaP, omegaM);
@@ -648,7 +648,7 @@ __global__ void __launch_bounds__(128, 8) k_step_held(Dev d, Params P, Uni<typen
   const int z = blockIdx.z;
   if (x < d.nx && y < d.ny) {
     const int32_t cell = (z * d.ny + y) * d.nx + x;
-    const HeldRates rates{nu, cell, coef};
+    const HeldRates rates{__ldg(nu + cell), coef};
     if constexpr (AOS)
       step_cell_at<St, PAR, MAC, FRC, false, true>(d, P, U, x, y, z, cell, AddrAos<St, PAR, int32_t>(d, cell, x, y, z),
                                                    rates);
@@ -658,10 +658,10 @@ __global__ void __launch_bounds__(128, 8) k_step_held(Dev d, Params P, Uni<typen
   }
 }
 
-constexpr int kClosureTcPerSm = 4;
-template <class St, int PAR, bool MAC, bool FRC, bool W64, int MODE>
+constexpr int kClosureTcPerSm = 6;
+template <class St, int PAR, bool MAC, bool FRC, bool W64, int MODE, bool AOS>
 __global__ void __launch_bounds__(128, kClosureTcPerSm)
-k_step_closure_tc(Dev d, Params P, Uni<float> U, CloArgs A, int gx, int gy, long long ntiles) {
+k_step_closure_tc(Dev d, Params P, Uni<float> U, CloArgs A, SlotPtrs T, int gx, int gy, long long ntiles) {
   using R = float;
   using S = typename St::store_t;
   using Off = typename OffT<W64>::type;
@@ -682,7 +682,14 @@ k_step_closure_tc(Dev d, Params P, Uni<float> U, CloArgs A, int gx, int gy, long
     const int x = bxi * 64 + (tid & 63), y = byi * 2 + (tid >> 6);
     const bool inr = x < nx && y < ny;
     const Off cell = ((Off)z * ny + (inr ? y : 0)) * nx + (inr ? x : 0);
-    const AddrRt<St, PAR, Off> ad(d, cell, inr ? x : 0, inr ? y : 0, z);
+    // addressing of the context's layout (32-bit offsets), or either layout
+    // chosen at run time for sets past 2^31 elements
+    using Ad = std::conditional_t<W64, AddrRt<St, PAR, Off>,
+                                  std::conditional_t<AOS, AddrAos<St, PAR, Off>, AddrSlots<St, PAR, Off>>>;
+    const Ad ad = [&]() {
+      if constexpr (W64 || AOS) return Ad(d, cell, inr ? x : 0, inr ? y : 0, z);
+      else return Ad(d, T, cell, inr ? x : 0, inr ? y : 0, z);
+    }();
     auto emit = [&](int i, R v) {
       if (i == 0) St::st(ad.rest(), v);
       else if (i & 1) St::st(ad.b((i - 1) >> 1, true), v);
@@ -1179,8 +1186,13 @@ struct OpsImpl {
     }
     const SlotPtrs T = make_slots<St>(d, PAR);
     if (d.aos) {
-      if constexpr (FAST && sizeof(R) == 4)
-        k_step_inplace<St, PAR, MAC, FRC, false, FAST, kDefault, true><<<L.grid, L.block, 0, s>>>(d, P, U, T);
+      if constexpr (FAST && sizeof(R) == 4) {
+        // variant 9: store addresses kept in registers from the loads
+        if (!MAC && !FRC && L.occ == 9)
+          k_step_inplace<St, PAR, MAC, FRC, false, FAST, kDefault, true, false><<<L.grid, L.block, 0, s>>>(d, P, U, T);
+        else
+          k_step_inplace<St, PAR, MAC, FRC, false, FAST, kDefault, true><<<L.grid, L.block, 0, s>>>(d, P, U, T);
+      }
       return;
     }
     // the plain hot-loop variant also exists with a looser register cap
@@ -1250,7 +1262,9 @@ struct OpsImpl {
   template <int PAR, bool MAC, bool FRC, bool W64, int MODE>
   static void go_closure_tc(const Dev& d, const Params& P, const Uni<float>& U, const CloArgs& A, cudaStream_t s) {
     if constexpr (sizeof(R) == 4) {
-      auto* k = &k_step_closure_tc<St, PAR, MAC, FRC, W64, MODE>;
+      const SlotPtrs T = make_slots<St>(d, PAR);
+      auto* k = (!W64 && d.aos) ? &k_step_closure_tc<St, PAR, MAC, FRC, W64, MODE, true>
+                                : &k_step_closure_tc<St, PAR, MAC, FRC, W64, MODE, false>;
       // the kernel is built for kClosureTcPerSm resident CTAs per SM
       // (launch bounds), each holding 32 of the SM's 512 TMEM columns
       int dev = 0, sms = 1;
@@ -1260,7 +1274,7 @@ struct OpsImpl {
       const int gx = (d.nx + 63) / 64, gy = (d.ny + 1) / 2;
       const long long ntiles = (long long)gx * gy * d.nz;
       const unsigned grid = (unsigned)std::max<long long>(1, std::min<long long>(ntiles, (long long)per_sm * sms));
-      k<<<grid, 128, 0, s>>>(d, P, U, A, gx, gy, ntiles);
+      k<<<grid, 128, 0, s>>>(d, P, U, A, T, gx, gy, ntiles);
     }
   }
   template <int PAR, bool MAC, bool FRC, int ENG, int MODE>

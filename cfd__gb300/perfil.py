@@ -4,7 +4,7 @@ committed ncu summaries under profiles/ capture.
     python -m cfd__gb300.perfil [--grid 512x256x192|320x160x128]
                                 [--storage f32|f16s|bf16s|f64] [--steps K] [--warmup W]
                                 [--closure K] [--engine 0|1] [--block BX] [--variant MINB]
-                                [--forces] [--soa]
+                                [--forces] [--soa | --aos]
 
 W warm-up steps, then K steps, then a synchronize; prints the wall time.
 The step kernel runs once per step (k_step_inplace, or k_step_closure with
@@ -29,13 +29,19 @@ def main(argv=None):
     ap.add_argument("--variant", type=int, default=0, help="lbm_set_launch min_blocks code")
     ap.add_argument("--forces", action="store_true", help="steps with the fused force (passoComForcas)")
     ap.add_argument("--soa", action="store_true", help="keep the in-place set in the SoA layout")
+    ap.add_argument("--aos", action="store_true", help="keep the in-place set in the AoSoA layout")
+    ap.add_argument("--lote", type=int, default=0,
+                    help="instead: the batched workload of this many seeded tunnels (--mode 0/1)")
+    ap.add_argument("--mode", type=int, default=1)
     a = ap.parse_args(argv)
+    if a.lote:
+        return lote(a)
     from . import build as B
     B.build()
     from .cargas import GRIDS, carga
     from .solver import SolverCUDA
     tipo, cfg, desc = carga(a.grid)
-    s = SolverCUDA(GRIDS[a.grid], storage=a.storage, escrever_macros=False, soa=a.soa)
+    s = SolverCUDA(GRIDS[a.grid], storage=a.storage, escrever_macros=False, soa=True if a.soa else (False if a.aos else None))
     s.definirTipos(tipo)
     s.configurar(**cfg, closure=a.closure)
     if a.closure:
@@ -55,6 +61,27 @@ def main(argv=None):
     N = int(tipo.size)
     print(f"{desc}: {a.storage}, layout {s.info()['layout']}, {a.steps} steps in {dt * 1e3:.2f} ms ({N * a.steps / dt / 1e6:.0f} MLUPS wall)")
     s.destruir()
+
+
+def lote(a):
+    from . import build as B
+    B.build()
+    from .lote import LoteCUDA, sorteio_lote
+    tun = sorteio_lote(a.lote, 2026)
+    L = LoteCUDA([t[0] for t in tun], storage=a.storage)
+    L.definirModo(a.mode)
+    for k, (g, tipo, cfg, info) in enumerate(tun):
+        L.definirTipos(k, tipo)
+        L.configurar(k, **cfg)
+    L.inicializar()
+    L.passo(a.warmup)
+    t0 = time.perf_counter()
+    L.passo(a.steps)
+    L.medirForcas()
+    dt = time.perf_counter() - t0
+    print(f"{a.lote} tunnels, {L.celulas} cells, mode {a.mode}: {a.steps} steps in {dt * 1e3:.2f} ms "
+          f"({L.celulas * a.steps / dt / 1e6:.0f} MLUPS wall)")
+    L.destruir()
 
 
 if __name__ == "__main__":

@@ -33,12 +33,15 @@ def js_round(v: float) -> int:
 class SolverCUDA:
     """A D3Q19 TRT/LES wind tunnel on one GB300, one CUDA stream per solver."""
 
-    def __init__(self, grade, storage="f32", escrever_macros=True, pingpong=False, estrito=False, soa=False):
+    def __init__(self, grade, storage="f32", escrever_macros=True, pingpong=False, estrito=False, soa=None):
         """storage: "f32" | "f16s" | "bf16s" | "f64"; pingpong: the reference's
         two-set A/B layout instead of the in-place one; estrito: the shader's
         arithmetic read literally (no fused multiply-add) instead of the FAST
-        restatement; soa: keep the in-place set in the SoA layout even where
-        the AoSoA layout applies (info()["layout"] says which is in use)."""
+        restatement; soa: True keeps the in-place set in the SoA layout,
+        False asks for the AoSoA layout where it applies, None (default)
+        takes the library's choice (autotuneLayout's measurement, else AoSoA
+        for f32 and SoA for the 16-bit forms); info()["layout"] says which
+        is in use."""
         self._lib = nat.load()
         self.nx, self.ny, self.nz = int(grade["nx"]), int(grade["ny"]), int(grade["nz"])
         self.N = self.nx * self.ny * self.nz
@@ -50,7 +53,7 @@ class SolverCUDA:
         self._rampa = None
         self.fontes = {"passo": "cfd__gb300/csrc/lbm_kernels.cuh:k_step_inplace"}
         flags = (nat.FLAG_WRITE_MACROS if escrever_macros else 0) | (nat.FLAG_PINGPONG if pingpong else 0) | \
-            (nat.FLAG_STRICT if estrito else 0) | (nat.FLAG_SOA if soa else 0)
+            (nat.FLAG_STRICT if estrito else 0) | (0 if soa is None else (nat.FLAG_SOA if soa else nat.FLAG_AOS))
         dims = nat.Dims(self.nx, self.ny, self.nz)
         h = C.c_void_p()
         nat.check(self._lib.lbm_create(C.byref(dims), STORAGE[storage], flags, C.byref(h)))
@@ -261,6 +264,18 @@ class SolverCUDA:
         """Launch shape of the step kernel: threads along x per block and the
         register-cap variant (min resident blocks per SM: 8 or 6; 0 = default)."""
         nat.check(self._lib.lbm_set_launch(self._h, int(block_x), int(min_blocos)))
+
+    @staticmethod
+    def autoajustarLayout(grade, storage="f32", passos=20, estrito=False):
+        """Time both layouts of the in-place set on a free stream of this grid
+        (lbm_autotune_layout); the faster becomes the default for solvers of
+        this grid and storage created afterwards in this process."""
+        lib = nat.load()
+        dims = nat.Dims(int(grade["nx"]), int(grade["ny"]), int(grade["nz"]))
+        lay, a, b = C.c_int(), C.c_float(), C.c_float()
+        nat.check(lib.lbm_autotune_layout(C.byref(dims), STORAGE[storage], nat.FLAG_STRICT if estrito else 0,
+                                          int(passos), C.byref(lay), C.byref(a), C.byref(b)))
+        return {"layout": lay.value, "ms_aosoa": a.value, "ms_soa": b.value}
 
     def autoajustar(self, passos=20):
         """Measure the step kernel's launch shapes on a copy of the current

@@ -81,14 +81,20 @@ extern "C" {
                                      fused multiply-adds, u = m (1/rho)); both
                                      are reproduced bit for bit by the oracle */
 #define LBM_FLAG_SOA           8  /* keep the in-place set in the SoA layout
-                                     (slot k of cell c at k N + c).  Default:
-                                     the AoSoA layout (blocks of 32 cells along
-                                     x, their 19 slots one after the other)
-                                     whenever nx is a multiple of 32 and the
-                                     step is the FAST in-place one with fp32
-                                     arithmetic and 19 N < 2^31; SoA otherwise.
-                                     The layout is internal: populations in and
-                                     out are always the natural layout. */
+                                     (slot k of cell c at k N + c) */
+#define LBM_FLAG_AOS          16  /* keep it in the AoSoA layout (blocks of 32
+                                     cells along x, their 19 slots one after
+                                     the other) where that applies: nx a
+                                     multiple of 32, the FAST in-place step,
+                                     fp32 arithmetic, 19 N < 2^31.
+                                     Without either flag: the layout
+                                     lbm_autotune_layout measured faster for
+                                     this grid, storage and flags earlier in
+                                     the process, else AoSoA for LBM_F32 and
+                                     SoA for the 16-bit forms (the faster one
+                                     of each on GB300).  The layout is
+                                     internal: populations in and out are
+                                     always the natural layout. */
 
 typedef struct lbm_ctx lbm_ctx;
 
@@ -218,8 +224,21 @@ int lbm_set_block(lbm_ctx* ctx, int block_x);
  * src/core/emit/wgsl.js:186). */
 int lbm_autotune(lbm_ctx* ctx, int steps, int* block_x, int* block_y, int* variant, float* ms_per_step);
 
+/* Measured choice of the in-place set's layout for a grid: a free stream in
+ * an all-fluid box of these dimensions runs `steps` steps in each layout
+ * (timed with CUDA events; two contexts created and destroyed in turn); the
+ * faster layout becomes the default of lbm_create for this grid, storage and
+ * flags in this process.  layout: 2 AoSoA, 0 SoA (1 if flags ask for the
+ * ping-pong set); ms_*: milliseconds per step (-1 where AoSoA does not
+ * apply; nullable).  No counterpart in the reference. */
+int lbm_autotune_layout(const lbm_dims* dims, int storage, int flags, int steps, int* layout, float* ms_aos,
+                        float* ms_soa);
+
 /* Launch shape plus register-cap variant of the plain step kernel:
- * min_blocks = 8 (64 registers/thread), 6 (80) or 0 (default 8). */
+ * min_blocks = 8 (64 registers/thread), 6 (80) or 0 (default 8); with the
+ * AoSoA layout 8 forms the store addresses again after the collide and 9
+ * keeps them in registers from the loads; 100 + k (k = 4, 8, 16) selects the
+ * pipelined SoA step with k cells per thread along z. */
 int lbm_set_launch(lbm_ctx* ctx, int block_x, int min_blocks);
 
 /* Momentum-exchange force for callers that cannot allocate device memory when

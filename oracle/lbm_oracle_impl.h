@@ -226,19 +226,21 @@ void FN(orc_step)(const orc_params* P, int nx, int ny, int nz, const uint32_t* t
           }
         } else if (fast) {
           /* FLUIDO, FAST pair form: e_i + e_j = 2w (delta + rho (4.5 cu^2 - 1.5 uu)),
-           * e_i - e_j = 6 w rho cu; Pi from the pair sums; TRT on the pairs. */
-          const REAL e0 = FN(W_)[0] * ORC_FMA(-rho, uu15, delta);
+           * e_i - e_j = 6 w rho cu, fused as B = fma(-rho, 1.5 uu, delta),
+           * E = fma(4.5 rho cu, cu, B), ns = fma(-2w, E, s), nd = fma(-6 w rho, cu, d);
+           * Pi from the pair sums; TRT on the pairs. */
+          const REAL B = ORC_FMA(-rho, uu15, delta);
+          const REAL e0 = FN(W_)[0] * B;
+          const REAL a45 = LIT(4.5) * rho;
           const REAL r6a = (LIT(6.0) * FN(W_)[1]) * rho, r6d = (LIT(6.0) * FN(W_)[7]) * rho;
           REAL ns[9], nd[9];
           ORC_UNROLL
           for (int k = 0; k < 9; ++k) {
             const int i = 2 * k + 1;
             const REAL cu = FN(orc_dotc)(i, ux, uy, uz);
-            const REAL a2 = ORC_FMA(LIT(4.5) * cu, cu, -uu15);
-            const REAL es = (LIT(2.0) * FN(W_)[i]) * ORC_FMA(rho, a2, delta);
-            const REAL ed = (i <= 6 ? r6a : r6d) * cu;
-            ns[k] = sp[k] - es;
-            nd[k] = dp[k] - ed;
+            const REAL E = ORC_FMA(a45 * cu, cu, B);
+            ns[k] = ORC_FMA(-(LIT(2.0) * FN(W_)[i]), E, sp[k]);
+            nd[k] = ORC_FMA(-(i <= 6 ? r6a : r6d), cu, dp[k]);
           }
           const REAL tau0 = LIT(1.0) / omegaPlus;
           REAL omegaP, omegaM;

@@ -71,3 +71,26 @@ def test_batch_autotune_keeps_states(native):
     lote.destruir()
     for s in solos:
         s.destruir()
+
+
+def test_layout_tuner_sets_the_default(native):
+    """lbm_autotune_layout times both layouts and makes the faster one the
+    default for solvers of that grid and storage; an explicit flag still
+    wins, and the two flags together are refused."""
+    from cfd__gb300 import SolverCUDA
+    from cfd__gb300._native import LbmError
+    g = {"nx": 64, "ny": 32, "nz": 24}
+    r = SolverCUDA.autoajustarLayout(g, "f16s", passos=4)
+    assert r["layout"] in (0, 2) and r["ms_soa"] > 0 and r["ms_aosoa"] > 0
+    s = SolverCUDA(g, storage="f16s")
+    assert s.info()["layout"] == r["layout"]
+    assert SolverCUDA(g, storage="f16s", soa=True).info()["layout"] == 0
+    assert SolverCUDA(g, storage="f16s", soa=False).info()["layout"] == 2
+    assert SolverCUDA({"nx": 70, "ny": 32, "nz": 24}, storage="f32", soa=False).info()["layout"] == 0  # nx % 32
+    from cfd__gb300 import _native as nat
+    import ctypes as C
+    h = C.c_void_p()
+    dims = nat.Dims(64, 32, 24)
+    rc = nat.load().lbm_create(C.byref(dims), nat.F32, nat.FLAG_SOA | nat.FLAG_AOS, C.byref(h))
+    with pytest.raises(LbmError, match="EINVAL"):
+        nat.check(rc)
