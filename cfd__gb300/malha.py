@@ -61,14 +61,14 @@ def contagem_stl_binario(buf: bytes):
 def _stl_binario(buf, info, avisos):
     n, base = info["n"], info["base"]
     if info["deslocado"]:
-        avisos.append(f"cabeçalho de {base - 4} bytes em vez de 80 — a contagem de triângulos está no "
-                      f"deslocamento {base - 4}, onde a conta fecha exata")
+        avisos.append(f"stl-header-size: {base - 4}-byte header (80 expected); triangle count read at byte "
+                      f"{base - 4}, the offset where 4 + 50 n bytes follow exactly")
     rec = np.frombuffer(buf, dtype=np.dtype([("nrm", "<f4", 3), ("v", "<f4", 9), ("attr", "<u2")]), count=n,
                         offset=base)
     positions = np.ascontiguousarray(rec["v"].reshape(-1)).astype(np.float32)
     if info["truncado"] > 0:
-        avisos.append(f"arquivo termina cedo: {info['truncado']} triângulo(s) declarado(s) no cabeçalho não "
-                      "estão no arquivo e foram ignorados")
+        avisos.append(f"stl-truncated: {info['truncado']} declared triangle(s) missing from the end of the "
+                      "file; read the complete ones")
     return positions, np.arange(n * 3, dtype=np.uint32)
 
 
@@ -87,10 +87,10 @@ def _stl_ascii(texto, avisos):
     for m in _VERTEX.finditer(texto):
         verts.extend((_num(m.group(1)), _num(m.group(2)), _num(m.group(3))))
     if not verts:
-        raise ValueError('STL ASCII sem nenhum "vertex"')
+        raise ValueError("stl-ascii-empty: no vertex lines")
     if len(verts) % 9:
         sobra = (len(verts) % 9) // 3
-        avisos.append(f"{sobra} vértice(s) soltos no fim do arquivo, descartados")
+        avisos.append(f"stl-trailing-vertices: {sobra} vertex line(s) after the last full triangle, dropped")
         verts = verts[:len(verts) - len(verts) % 9]
     positions = np.array(verts, np.float64).astype(np.float32)
     return positions, np.arange(positions.size // 3, dtype=np.uint32)
@@ -104,14 +104,14 @@ def parse_stl(buf: bytes, avisos=None):
         cab = buf[:min(80, b["base"] - 4)].decode("latin1")
         cab = re.sub(r"\0.*$", "", cab, flags=re.S).strip()
         if re.match(r"^solid", cab, re.I):
-            avisos.append('cabeçalho começa com "solid" mas o arquivo é binário — detectado pela aritmética '
-                          '84 + 50n, não pelo prefixo')
+            avisos.append("stl-solid-binary: the header text begins with 'solid' but the size fits the binary "
+                          "layout (84 + 50 n bytes); read as binary")
         pos, idx = _stl_binario(buf, b, avisos)
         return {"positions": pos, "indices": idx, "formato": "stl-binario", "nome": cab}
     texto = buf.decode("utf-8", errors="replace")
     if not re.match(r"^\s*solid", texto, re.I):
-        raise ValueError("não é STL: a contagem binária não fecha com o tamanho do arquivo e o conteúdo não "
-                         'começa com "solid"')
+        raise ValueError("stl-unknown: the size does not fit the binary layout and the text does not begin "
+                         "with 'solid'")
     m = re.search(r"^\s*solid[ \t]*(.*)$", texto, re.M)
     pos, idx = _stl_ascii(texto, avisos)
     return {"positions": pos, "indices": idx, "formato": "stl-ascii", "nome": (m.group(1) if m else "").strip()}
@@ -150,11 +150,11 @@ def parse_obj(texto: str, avisos=None):
             if not nome:
                 nome = t[2:].strip()
     if not tris:
-        raise ValueError("OBJ sem faces trianguláveis")
+        raise ValueError("obj-no-faces: no face with three or more vertices")
     nv = len(vx) // 3
     fora = sum(1 for i in tris if i < 0 or i >= nv)
     if fora:
-        avisos.append(f"{fora} índice(s) de face fora do intervalo, descartados")
+        avisos.append(f"obj-index-range: {fora} face index/indices outside the vertex list, dropped")
     return {"positions": np.array(vx, np.float64).astype(np.float32),
             "indices": np.array([i for i in tris if 0 <= i < nv], np.uint32), "formato": "obj", "nome": nome}
 
@@ -170,7 +170,7 @@ def parse_ply(buf: bytes, avisos=None):
     cab = buf[:65536].decode("latin1")
     fim = cab.find("end_header")
     if fim < 0:
-        raise ValueError("PLY sem end_header nos primeiros 64 KB")
+        raise ValueError("ply-header: end_header not found in the first 64 KiB")
     inicio = cab.find("\n", fim) + 1
     formato, atual, elementos = None, None, []
     for l in re.split(r"\r?\n", cab[:fim]):
@@ -188,7 +188,7 @@ def parse_ply(buf: bytes, avisos=None):
     ev = next((e for e in elementos if e["nome"] == "vertex"), None)
     ef = next((e for e in elementos if e["nome"] == "face"), None)
     if ev is None:
-        raise ValueError('PLY sem elemento "vertex"')
+        raise ValueError("ply-vertex: no vertex element declared")
     positions = np.zeros(ev["contagem"] * 3, np.float32)
     tris = []
     ix = next((k for k, q in enumerate(ev["props"]) if q["nome"] == "x"), -1)
@@ -217,7 +217,7 @@ def parse_ply(buf: bytes, avisos=None):
         def ler(tipo):
             c = _PLY_TIPOS.get(tipo)
             if c is None:
-                raise ValueError(f"tipo PLY desconhecido: {tipo}")
+                raise ValueError(f"ply-type: property type {tipo} not recognised")
             v = struct.unpack_from(e + c, buf, p[0])[0]
             p[0] += struct.calcsize(c)
             return v
@@ -238,7 +238,7 @@ def parse_ply(buf: bytes, avisos=None):
                     for k in range(1, n - 1):
                         tris.extend((face[0], face[k], face[k + 1]))
     if not tris:
-        raise ValueError("PLY sem faces")
+        raise ValueError("ply-faces: no face element or no faces")
     return {"positions": positions, "indices": np.array(tris, np.uint32), "formato": "ply", "nome": ""}
 
 
@@ -280,13 +280,13 @@ def _montar_gltf(js, buffers, avisos):
         comp = _COMP.get(acc.get("componentType"))
         n = _NCOMP.get(acc.get("type"))
         if not comp or not n:
-            raise ValueError(f"accessor {i_acc}: tipo não suportado")
+            raise ValueError(f"gltf-accessor: accessor {i_acc} has a component type this reader does not take")
         if acc.get("bufferView") is None:
             return np.zeros(acc["count"] * n, comp[0])
         bv = js["bufferViews"][acc["bufferView"]]
         buf = buffers[bv.get("buffer", 0)] if bv.get("buffer", 0) < len(buffers) else None
         if buf is None:
-            raise ValueError("bufferView aponta para buffer ausente")
+            raise ValueError("gltf-buffer-view: refers to a buffer that was not loaded")
         base = bv.get("byteOffset", 0) + acc.get("byteOffset", 0)
         passo = bv.get("byteStride", 0)
         if not passo or passo == comp[1] * n:
@@ -309,10 +309,11 @@ def _montar_gltf(js, buffers, avisos):
         if node.get("mesh") is not None:
             for prim in js["meshes"][node["mesh"]].get("primitives", []):
                 if prim.get("mode") is not None and prim["mode"] != 4:
-                    avisos.append(f"primitivo com mode={prim['mode']} (não TRIANGLES) ignorado")
+                    avisos.append(f"gltf-mode: primitive of mode {prim['mode']} is not a triangle list, skipped")
                     continue
                 if (prim.get("extensions") or {}).get("KHR_draco_mesh_compression"):
-                    avisos.append("primitivo comprimido com Draco ignorado — exporte sem compressão Draco")
+                    avisos.append("gltf-draco: Draco-compressed primitive skipped (no decoder here); export it "
+                                  "uncompressed")
                     continue
                 i_pos = (prim.get("attributes") or {}).get("POSITION")
                 if i_pos is None:
@@ -341,7 +342,7 @@ def _montar_gltf(js, buffers, avisos):
     for r in raizes:
         visitar(r, ident)
     if not pos_acc:
-        raise ValueError("glTF sem geometria triangular")
+        raise ValueError("gltf-empty: no triangle geometry in the scene")
     return np.concatenate(pos_acc), np.concatenate(idx_acc)
 
 
@@ -353,10 +354,10 @@ def parse_glb(buf: bytes, avisos=None):
     """src/geom/parse.js:500-532."""
     avisos = [] if avisos is None else avisos
     if struct.unpack_from("<I", buf, 0)[0] != 0x46546C67:
-        raise ValueError('sem a magia "glTF"')
+        raise ValueError("glb-magic: the file does not start with the glTF magic bytes")
     versao = struct.unpack_from("<I", buf, 4)[0]
     if versao != 2:
-        avisos.append(f"GLB versão {versao}; o leitor é de glTF 2.0")
+        avisos.append(f"glb-version: container version {versao}, read as glTF 2.0")
     js, bins, p = None, [], 12
     while p + 8 <= len(buf):
         tam, tipo = struct.unpack_from("<II", buf, p)
@@ -367,7 +368,7 @@ def parse_glb(buf: bytes, avisos=None):
             bins.append(dados)
         p += 8 + tam + ((4 - tam % 4) % 4)
     if js is None:
-        raise ValueError("GLB sem chunk JSON")
+        raise ValueError("glb-json: no JSON chunk")
     buffers = []
     for i, b in enumerate(js.get("buffers", [])):
         if b.get("uri") is None:
@@ -375,7 +376,7 @@ def parse_glb(buf: bytes, avisos=None):
         elif b["uri"].startswith("data:"):
             buffers.append(_b64(b["uri"]))
         else:
-            avisos.append(f'buffer externo "{b["uri"]}" não pôde ser carregado')
+            avisos.append(f"gltf-external-buffer: {b['uri']} is a separate file and was not loaded")
             buffers.append(None)
     if not buffers:
         buffers.append(bins[0] if bins else None)
@@ -394,7 +395,8 @@ def parse_gltf(texto: str, avisos=None):
         if (b.get("uri") or "").startswith("data:"):
             buffers.append(_b64(b["uri"]))
         else:
-            avisos.append(f'buffer externo "{b.get("uri")}" não pôde ser carregado — use .glb, que embute os dados')
+            avisos.append(f"gltf-external-buffer: {b.get('uri')} is a separate file and was not loaded (a .glb "
+                          "carries its buffers inside)")
             buffers.append(None)
     cenas = js.get("scenes")
     nome = (cenas[js.get("scene", 0)].get("name") if cenas else None) or ""
@@ -422,7 +424,7 @@ def ler(buf: bytes, nome_arquivo: str = ""):
         r = parse_stl(buf, avisos)
     nt = r["indices"].size // 3
     if not nt:
-        raise ValueError(f"{r['formato']}: nenhum triângulo")
+        raise ValueError(f"{r['formato']}: the file holds no triangles")
     return dict(r, avisos=avisos, nTriangulos=nt, nVertices=r["positions"].size // 3)
 
 

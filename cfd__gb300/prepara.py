@@ -88,11 +88,11 @@ def palpitar_unidade(comprimento):
             return {"fator": fator, "nome": nome, "tipico": [lo, hi], "normalizado": False, "confianca": "plausível"}
     if 0.2 < comprimento < 2.5:
         return {"fator": 1, "nome": "normalizado", "normalizado": True, "confianca": "nenhuma",
-                "aviso": f"maior dimensão = {comprimento:.3f}; o modelo parece normalizado. Informe o comprimento "
-                         "real do corpo — Re e Cd dependem dele."}
+                "aviso": f"unit-normalised: longest side {comprimento:.3f} looks like a unit-scaled model; give "
+                         "the body's real length (comprimentoM), since Re and Cd use it"}
     return {"fator": 1, "nome": "desconhecida", "normalizado": True, "confianca": "nenhuma",
-            "aviso": f"maior dimensão = {comprimento:.4g}, fora de qualquer faixa típica. Informe o comprimento "
-                     "real do corpo."}
+            "aviso": f"unit-unknown: longest side {comprimento:.4g} fits no unit's usual range; give the body's "
+                     "real length (comprimentoM)"}
 
 
 def colocar(positions, ordem, grade, celulas_por_comprimento, espelhar=(False, False, False), fracao_entrada=0.28,
@@ -130,10 +130,11 @@ def colocar(positions, ordem, grade, celulas_por_comprimento, espelhar=(False, F
     for a, nome in ((0, "x"), (1, "y"), (2, "z")):
         lim = (grade["nx"], grade["ny"], grade["nz"])[a]
         if ef["min"][a] < 0 or ef["max"][a] > lim:
-            avisos.append(f"o corpo sai do domínio em {nome} ({ef['min'][a]:.1f}…{ef['max'][a]:.1f} de 0…{lim})")
+            avisos.append(f"body-outside: along {nome} the body spans {ef['min'][a]:.1f} to {ef['max'][a]:.1f}, "
+                          f"the grid 0 to {lim}")
     if bloqueio > 0.10:
-        avisos.append(f"bloqueio de {bloqueio * 100:.1f}% — acima de 10% a correção de Maskell deixa de ser "
-                      "confiável; use um domínio maior")
+        avisos.append(f"blockage: the body's box covers {bloqueio * 100:.1f} % of the cross-section; past 10 % the "
+                      "Maskell blockage correction is not reliable, so widen the grid")
     return {"positions": out.reshape(-1), "escala": s, "extentos": ef, "bloqueioCaixa": bloqueio, "avisos": avisos}
 
 
@@ -165,9 +166,9 @@ def preparar(malha, grade, **opcoes):
     if unidade.get("aviso"):
         avisos.append(unidade["aviso"])
     if sentido["confianca"] < 0.12:
-        avisos.append(f"frente e traseira quase igualmente altas ({sentido['alturaFrente']:.2f} vs "
-                      f"{sentido['alturaTras']:.2f}): o sentido é um chute. Confira se o vento chega pelo nariz e "
-                      "inverta se não chegar.")
+        avisos.append(f"direction-guess: front and rear heights are close ({sentido['alturaFrente']:.2f}, "
+                      f"{sentido['alturaTras']:.2f}), so the flow direction is a guess; check that the flow meets "
+                      "the nose and set inverterSentido otherwise")
     return dict(col, indices=malha["indices"], eixos=eixos,
                 sentido=dict(sentido, aplicado=inverter, manual=opcoes.get("inverterSentido") is not None),
                 unidade=unidade, comprimentoM=comprimento_m, extentosOriginais=ext, avisos=avisos)

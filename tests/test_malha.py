@@ -29,14 +29,14 @@ def test_stl_binary_and_its_quirks():
     # 79-byte header: the count is found where the arithmetic closes
     r = malha.ler(stl_bin(TRI, base=79))
     assert r["nTriangulos"] == 3 and np.array_equal(r["positions"], TRI.reshape(-1))
-    assert any("79 bytes" in a for a in r["avisos"])
+    assert any("stl-header-size: 79-byte" in a for a in r["avisos"])
     # a binary file whose header starts with "solid"
     r = malha.ler(stl_bin(TRI, header=b"solid exported by a CAD tool"))
-    assert r["formato"] == "stl-binario" and any("solid" in a for a in r["avisos"])
+    assert r["formato"] == "stl-binario" and any("stl-solid-binary" in a for a in r["avisos"])
     assert r["nome"] == "solid exported by a CAD tool"
     # one byte short: the incomplete last record is dropped, with a warning
     r = malha.ler(stl_bin(TRI, cut=1))
-    assert r["nTriangulos"] == 2 and any("termina cedo" in a for a in r["avisos"])
+    assert r["nTriangulos"] == 2 and any("stl-truncated" in a for a in r["avisos"])
 
 
 def test_stl_ascii():
@@ -50,7 +50,7 @@ def test_stl_ascii():
     r = malha.ler(txt.encode())
     assert r["formato"] == "stl-ascii" and r["nome"] == "caixa" and r["nTriangulos"] == 3
     assert np.array_equal(r["positions"], TRI.reshape(-1))
-    assert any("soltos" in a for a in r["avisos"])
+    assert any("stl-trailing-vertices" in a for a in r["avisos"])
     with pytest.raises(ValueError):
         malha.ler(b"not a mesh at all, just text of some length that is not stl" * 3)
 
@@ -62,7 +62,7 @@ def test_obj_polygons_negative_indices_and_range_quirk():
     assert r["indices"].tolist() == [0, 1, 2, 0, 2, 3, 4, 3, 2]
     # an out-of-range index is dropped on its own (the reference's filter)
     r = malha.ler(b"v 0 0 0\nv 1 0 0\nv 0 1 0\nf 1 2 3\nf 1 2 9\n", "y.obj")
-    assert r["indices"].tolist() == [0, 1, 2, 0, 1] and any("fora do intervalo" in a for a in r["avisos"])
+    assert r["indices"].tolist() == [0, 1, 2, 0, 1] and any("obj-index-range" in a for a in r["avisos"])
 
 
 def test_ply_ascii_and_binary():
