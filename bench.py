@@ -526,12 +526,17 @@ def run_ours(args):
                                       "traffic": ncu_traffic(st, args.grid), "algorithmic_bytes_per_cell": 76}}
             s2.destruir()
         forms["precision_study"] = precision_study(args.grid)
-        # the step kernel's register-cap variants side by side (lbm_set_launch codes)
+        # the step kernel's addressing variants side by side (lbm_set_launch
+        # codes) in each storage form's default layout: AoSoA for fp32 (where
+        # nx is a multiple of 32), SoA for the 16-bit forms
         variants = {}
         for st in ("f32", "f16s", "bf16s"):
             row = {}
-            codes = (("64_registers_recompute_addresses", 8), ("64_registers_keep_addresses", 9)) \
-                if (GRIDS[args.grid]["nx"] % 32 == 0 and st != "f64") else (("64_registers", 8), ("80_registers", 6))
+            if GRIDS[args.grid]["nx"] % 32 == 0 and st == "f32":
+                codes = (("aosoa_recompute_addresses", 8), ("aosoa_keep_addresses", 9))
+            else:
+                codes = (("soa_slot_pointers", 8), ("soa_slot_offsets_32bit", 20), ("soa_base_plus_slot_times_n", 21),
+                         ("soa_80_registers", 6))
             for name, code in codes:
                 s2 = make(st)
                 s2.definirBloco(64, code)

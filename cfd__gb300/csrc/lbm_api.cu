@@ -910,11 +910,11 @@ int lbm_set_launch(lbm_ctx* c, int block_x, int min_blocks) {
   if (!c) return fail(LBM_EINVAL, "null context");
   // min_blocks 4/8/16 with block_x = 64 selects the pipelined step with that
   // many cells per thread along z
-  if (min_blocks != 0 && min_blocks != 6 && min_blocks != 8 && min_blocks != 9 && min_blocks != 104 &&
-      min_blocks != 108 && min_blocks != 116)
+  if (min_blocks != 0 && min_blocks != 6 && min_blocks != 8 && min_blocks != 9 && min_blocks != 20 &&
+      min_blocks != 21 && min_blocks != 104 && min_blocks != 108 && min_blocks != 116)
     return fail(LBM_EINVAL,
-                "min_blocks must be 0, 6, 8, 9 (AoSoA: addresses kept from load to store), or 100 + cells per "
-                "thread (4, 8, 16) for the pipelined step");
+                "min_blocks must be 0, 6, 8, 9 (AoSoA: addresses kept from load to store), 20 or 21 (SoA addressing "
+                "variants), or 100 + cells per thread (4, 8, 16) for the pipelined step");
   int r = lbm_set_block(c, block_x);
   if (r) return r;
   if (min_blocks >= 100) { c->pipe = min_blocks - 100; c->occ = 8; }
@@ -929,19 +929,25 @@ int lbm_autotune(lbm_ctx* c, int steps, int* block_x, int* block_y, int* variant
   if (!c->state_set) return fail(LBM_ESTATE, "no state yet (initialise or set populations first)");
   if (steps < 2 || steps > 100000) return fail(LBM_EINVAL, "steps must be in [2, 100000]");
   // candidates: threads along x and y of the block (<= 128), the register-cap
-  // variant (8 or 6 resident blocks; the AoSoA step is built for 8), and for
-  // the SoA set the pipelined step (cells per thread along z)
+  // variant (8 or 6 resident blocks; the AoSoA step is built for 8), the
+  // addressing variants (AoSoA: 9; SoA: 20, 21), and for the SoA set the
+  // pipelined step (cells per thread along z)
+  const bool fits32 = (int64_t)Q * c->N < (int64_t)INT32_MAX;
   std::vector<Shape> cand;
   for (int bx : {32, 64, 128})
     for (int by : {1, 2, 4})
       if (bx * by <= 128) {
         cand.push_back({bx, by, 8, 0});
         if (c->aos) cand.push_back({bx, by, 9, 0});
+        if (!c->aos && c->storage != LBM_F64 && fits32) {
+          cand.push_back({bx, by, 20, 0});
+          cand.push_back({bx, by, 21, 0});
+        }
       }
   if (!c->aos && c->storage != LBM_F64) {
     cand.push_back({64, 1, 6, 0});
     cand.push_back({128, 1, 6, 0});
-    if ((int64_t)Q * c->N < (int64_t)INT32_MAX)
+    if (fits32)
       for (int kz : {4, 8, 16}) cand.push_back({64, 1, 8, kz});
   }
   // the state is saved and put back: the trials advance a copy of it

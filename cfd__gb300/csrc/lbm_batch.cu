@@ -55,12 +55,13 @@ constexpr int kPerLaunch = 64;   // tunnels whose descriptors ride in one launch
 struct BatchArgs {
   int ntun;
   int ntiles;
+  int aos;                     // every tunnel of this launch keeps its set in the AoSoA layout (else SoA)
   int first[kPerLaunch + 1];   // first tile of each tunnel (prefix), local to this launch
   TunnelDesc t[kPerLaunch];
 };
 static_assert(sizeof(BatchArgs) < 32000, "kernel parameter space");
 
-template <class St, int PAR, bool FAST, int MINB>
+template <class St, int PAR, bool FAST, int MINB, bool AOS>
 __global__ void __launch_bounds__(kTile, MINB) k_batch_step(const __grid_constant__ BatchArgs A) {
   // The tunnel of a tile is found by a search over the launch's first-tile
   // prefix; the index is the same for the whole CTA, so the search and the
@@ -84,14 +85,11 @@ __global__ void __launch_bounds__(kTile, MINB) k_batch_step(const __grid_constan
     const int y = byi * D.ty + (int)(threadIdx.x / tx);
     if (x < D.d.nx && y < D.d.ny) {
       const int32_t cell = (z * D.d.ny + y) * D.d.nx + x;
-      if constexpr (FAST) {
-        if (D.d.aos) {
-          step_cell_at<St, PAR, false, false, false, FAST>(D.d, D.P, D.U, x, y, z, cell,
-                                                           AddrAos<St, PAR, int32_t>(D.d, cell, x, y, z));
-          continue;
-        }
-      }
-      step_cell<St, PAR, false, false, false, FAST>(D.d, D.P, D.U, x, y, z);
+      if constexpr (AOS && FAST)
+        step_cell_at<St, PAR, false, false, false, FAST>(D.d, D.P, D.U, x, y, z, cell,
+                                                         AddrAos<St, PAR, int32_t>(D.d, cell, x, y, z));
+      else
+        step_cell<St, PAR, false, false, false, FAST>(D.d, D.P, D.U, x, y, z);
     }
   }
 }
@@ -193,16 +191,29 @@ int sync_desc(lbm_batch* b) {
   drop_graphs(b);
   b->args.clear();
   long long total = 0;
-  // tiles of the largest tunnels first: the persistent CTAs then finish with
-  // the small ones, which evens out the tail
+  // One launch (or more, 64 tunnels each) per layout class, so that each
+  // kernel instance carries a single addressing path.  Within a launch, tiles
+  // of the largest tunnels come first: the persistent CTAs then finish with
+  // the small ones, which evens out the tail.
   std::vector<size_t> order(b->host.size());
   for (size_t k = 0; k < order.size(); ++k) order[k] = k;
-  std::stable_sort(order.begin(), order.end(),
-                   [&](size_t p, size_t q) { return b->host[p].d.N > b->host[q].d.N; });
-  for (size_t k0 = 0; k0 < b->host.size(); k0 += kPerLaunch) {
+  std::stable_sort(order.begin(), order.end(), [&](size_t p, size_t q) {
+    if (b->host[p].d.aos != b->host[q].d.aos) return b->host[p].d.aos > b->host[q].d.aos;
+    return b->host[p].d.N > b->host[q].d.N;
+  });
+  std::vector<std::pair<size_t, size_t>> runs;   // [k0, k1) of `order`, one layout, <= 64 tunnels
+  for (size_t k0 = 0; k0 < order.size();) {
+    size_t k1 = k0;
+    while (k1 < order.size() && k1 - k0 < (size_t)kPerLaunch && b->host[order[k1]].d.aos == b->host[order[k0]].d.aos)
+      ++k1;
+    runs.push_back({k0, k1});
+    k0 = k1;
+  }
+  for (const auto& run : runs) {
     BatchArgs A;
     memset(&A, 0, sizeof A);
-    const size_t k1 = std::min(b->host.size(), k0 + kPerLaunch);
+    const size_t k0 = run.first, k1 = run.second;
+    A.aos = b->host[order[k0]].d.aos;
     long long t = 0;
     for (size_t kk = k0; kk < k1; ++kk) {
       const size_t k = order[kk];
@@ -231,8 +242,13 @@ int sync_desc(lbm_batch* b) {
 
 template <class St, bool FAST, int MINB>
 void launch_batch_m(lbm_batch* b, const BatchArgs& A, int parity, int grid) {
-  if (parity == 0) k_batch_step<St, 0, FAST, MINB><<<grid, kTile, 0, b->stream>>>(A);
-  else k_batch_step<St, 1, FAST, MINB><<<grid, kTile, 0, b->stream>>>(A);
+  if (A.aos) {
+    if (parity == 0) k_batch_step<St, 0, FAST, MINB, true><<<grid, kTile, 0, b->stream>>>(A);
+    else k_batch_step<St, 1, FAST, MINB, true><<<grid, kTile, 0, b->stream>>>(A);
+  } else {
+    if (parity == 0) k_batch_step<St, 0, FAST, MINB, false><<<grid, kTile, 0, b->stream>>>(A);
+    else k_batch_step<St, 1, FAST, MINB, false><<<grid, kTile, 0, b->stream>>>(A);
+  }
 }
 
 template <class St>

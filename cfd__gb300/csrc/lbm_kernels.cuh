@@ -151,6 +151,8 @@ struct Deltas {
 // derived from it are formed again afterwards instead of being kept live.
 __device__ __forceinline__ void opaque(int32_t& v) { asm volatile("" : "+r"(v)); }
 __device__ __forceinline__ void opaque(int64_t& v) { asm volatile("" : "+l"(v)); }
+template <class T>
+__device__ __forceinline__ void opaque(T*& p) { asm volatile("" : "+l"(p)); }
 
 // Where the in-place step of parity PAR finds the two slots of pair k
 // (i = 2k + 1): slot A = (E ? i + 1 : i) holds, at the cell itself, the
@@ -169,6 +171,8 @@ struct SlotPtrs {
   void* a[9];
   void* b[9];
   void* rest;
+  int32_t oa[9];    // the same slots as element offsets from the set's base
+  int32_t ob[9];    // (filled when 19 N < 2^31)
 };
 
 template <class St>
@@ -179,6 +183,9 @@ inline SlotPtrs make_slots(const Dev& d, int par) {
   for (int k = 0; k < 9; ++k) {
     t.a[k] = F + (int64_t)slot_a(k, par) * d.N;
     t.b[k] = F + (int64_t)slot_b(k, par) * d.N;
+    const bool fits = (int64_t)Q * d.N < (int64_t)INT32_MAX;
+    t.oa[k] = fits ? (int32_t)((int64_t)slot_a(k, par) * d.N) : 0;
+    t.ob[k] = fits ? (int32_t)((int64_t)slot_b(k, par) * d.N) : 0;
   }
   t.rest = F;
   return t;
@@ -195,7 +202,11 @@ struct AddrSet {
   Deltas<Off> D;
   __device__ __forceinline__ AddrSet(const Dev& d, Off cell, int x, int y, int z)
       : Fc(static_cast<S*>(d.pop) + cell), N((Off)d.N), D(x, y, z, d.nx, d.ny, d.nz) {}
-  __device__ __forceinline__ void refresh() {}
+  // the slot and neighbour addresses are formed again for the stores
+  // (the batched kernel, whose descriptors leave fewer registers free)
+  __device__ __forceinline__ void refresh() {
+    opaque(Fc); opaque(N); opaque(D.xp); opaque(D.yp); opaque(D.ym); opaque(D.zp); opaque(D.zm);
+  }
   __device__ __forceinline__ S* rest() const { return Fc; }
   __device__ __forceinline__ S* a(int k, bool nb) const {
     return Fc + (nb ? D.odd(2 * k + 1) : (Off)0) + (Off)slot_a(k, PAR) * N;
@@ -221,6 +232,28 @@ struct AddrSlots {
   __device__ __forceinline__ S* b(int k, bool nb) const {
     return static_cast<S*>(T.b[k]) + (nb ? cell + D.odd(2 * k + 1) : cell);
   }
+};
+
+// SoA addressing from one base pointer and the slots' 32-bit element
+// offsets in the launch parameters (19 N < 2^31): slot offset + cell +
+// displacement is one 32-bit add with a constant-bank operand.  The index
+// state is made opaque before the collide, so the store addresses are formed
+// again rather than kept live.
+template <class St, int PAR>
+struct AddrOffs {
+  using S = typename St::store_t;
+  S* F;
+  const SlotPtrs& T;
+  int32_t cell;
+  Deltas<int32_t> D;
+  __device__ __forceinline__ AddrOffs(const Dev& d, const SlotPtrs& t, int32_t c, int x, int y, int z)
+      : F(static_cast<S*>(d.pop)), T(t), cell(c), D(x, y, z, d.nx, d.ny, d.nz) {}
+  __device__ __forceinline__ void refresh() {
+    opaque(cell); opaque(D.xp); opaque(D.yp); opaque(D.ym); opaque(D.zp); opaque(D.zm);
+  }
+  __device__ __forceinline__ S* rest() const { return F + cell; }
+  __device__ __forceinline__ S* a(int k, bool nb) const { return F + (T.oa[k] + (nb ? cell + D.odd(2 * k + 1) : cell)); }
+  __device__ __forceinline__ S* b(int k, bool nb) const { return F + (T.ob[k] + (nb ? cell + D.odd(2 * k + 1) : cell)); }
 };
 
 // Neighbour displacements in AoSoA elements (aos_base(c + d) - aos_base(c)):
@@ -408,7 +441,11 @@ __device__ __forceinline__ void step_cell(const Dev& d, const Params& P, const U
 // MINB: minimum resident 128-thread blocks per SM the register allocation
 // must allow (8 -> 64 registers, 6 -> 80); the autotuner picks per form.  The
 // fused force is added where it is computed, so the force variant fits 64 too.
-template <class St, int PAR, bool MAC, bool FRC, bool W64, bool FAST, int MINB, bool AOS = false, bool RF = true>
+// SOAV (SoA set): 0 slot pointers (AddrSlots), 1 one base and 32-bit slot
+// offsets (AddrOffs), 2 one base and slot x N (AddrSet); 1 and 2 need
+// 19 N < 2^31.
+template <class St, int PAR, bool MAC, bool FRC, bool W64, bool FAST, int MINB, bool AOS = false, bool RF = true,
+          int SOAV = 0>
 __global__ void __launch_bounds__(128, MINB)
 k_step_inplace(Dev d, Params P, Uni<typename St::real> U, SlotPtrs T) {
   using Off = typename OffT<W64>::type;
@@ -420,6 +457,10 @@ k_step_inplace(Dev d, Params P, Uni<typename St::real> U, SlotPtrs T) {
     if constexpr (AOS)
       step_cell_at<St, PAR, MAC, FRC, W64, FAST>(d, P, U, x, y, z, cell,
                                                  AddrAos<St, PAR, Off, RF>(d, cell, x, y, z));
+    else if constexpr (SOAV == 1 && !W64)
+      step_cell_at<St, PAR, MAC, FRC, W64, FAST>(d, P, U, x, y, z, cell, AddrOffs<St, PAR>(d, T, cell, x, y, z));
+    else if constexpr (SOAV == 2 && !W64)
+      step_cell_at<St, PAR, MAC, FRC, W64, FAST>(d, P, U, x, y, z, cell, AddrSet<St, PAR, Off>(d, cell, x, y, z));
     else
       step_cell_at<St, PAR, MAC, FRC, W64, FAST>(d, P, U, x, y, z, cell,
                                                  AddrSlots<St, PAR, Off>(d, T, cell, x, y, z));
@@ -1194,6 +1235,18 @@ struct OpsImpl {
           k_step_inplace<St, PAR, MAC, FRC, false, FAST, kDefault, true><<<L.grid, L.block, 0, s>>>(d, P, U, T);
       }
       return;
+    }
+    // SoA addressing variants of the plain step (20: 32-bit slot offsets,
+    // 21: base + slot x N), both with the store addresses formed again
+    if constexpr (!MAC && !FRC && sizeof(R) == 4) {
+      if (!w64 && L.occ == 20) {
+        k_step_inplace<St, PAR, MAC, FRC, false, FAST, kDefault, false, true, 1><<<L.grid, L.block, 0, s>>>(d, P, U, T);
+        return;
+      }
+      if (!w64 && L.occ == 21) {
+        k_step_inplace<St, PAR, MAC, FRC, false, FAST, kDefault, false, true, 2><<<L.grid, L.block, 0, s>>>(d, P, U, T);
+        return;
+      }
     }
     // the plain hot-loop variant also exists with a looser register cap
     if (!MAC && !FRC && sizeof(R) == 4 && L.occ == 6) {

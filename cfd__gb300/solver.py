@@ -262,7 +262,9 @@ class SolverCUDA:
 
     def definirBloco(self, block_x: int, min_blocos: int = 0):
         """Launch shape of the step kernel: threads along x per block and the
-        register-cap variant (min resident blocks per SM: 8 or 6; 0 = default)."""
+        variant code of lbm_set_launch (8 or 6 resident blocks per SM; 9
+        AoSoA addresses kept; 20 / 21 SoA addressing from one base; 100 + k
+        the pipelined SoA step; 0 = default)."""
         nat.check(self._lib.lbm_set_launch(self._h, int(block_x), int(min_blocos)))
 
     @staticmethod

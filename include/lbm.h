@@ -237,8 +237,11 @@ int lbm_autotune_layout(const lbm_dims* dims, int storage, int flags, int steps,
 /* Launch shape plus register-cap variant of the plain step kernel:
  * min_blocks = 8 (64 registers/thread), 6 (80) or 0 (default 8); with the
  * AoSoA layout 8 forms the store addresses again after the collide and 9
- * keeps them in registers from the loads; 100 + k (k = 4, 8, 16) selects the
- * pipelined SoA step with k cells per thread along z. */
+ * keeps them in registers from the loads; with the SoA layout 8 addresses
+ * each slot from its own base pointer, 20 from one base and the slots'
+ * 32-bit offsets, 21 from one base and slot x N (20 and 21 need 19 N < 2^31
+ * and apply to the plain step with fp32 arithmetic); 100 + k (k = 4, 8, 16)
+ * selects the pipelined SoA step with k cells per thread along z. */
 int lbm_set_launch(lbm_ctx* ctx, int block_x, int min_blocks);
 
 /* Momentum-exchange force for callers that cannot allocate device memory when

@@ -106,3 +106,27 @@ def test_aos_checkpoint_round_trip(native):
         b.carregarEstado(blob)          # an SoA context refuses an AoSoA checkpoint
     for s in (a, b, b2):
         s.destruir()
+
+
+@pytest.mark.parametrize("storage", ["f32", "f16s", "bf16s"])
+def test_soa_addressing_variants_equal(native, storage):
+    """The SoA step's addressing variants (lbm_set_launch 8: slot pointers,
+    20: 32-bit slot offsets, 21: base + slot x N) give the same states bit
+    for bit, with the fused force as well (which runs the default)."""
+    from cfd__gb300 import SolverCUDA
+    grade, tipo, esp = all_types_tunnel(nx=70, ny=24, nz=20)
+    g0 = random_state(int(np.prod(list(grade.values()))), seed=33)
+    fl = ~np.isin(tipo, [1, 4, 7])
+    out = []
+    for code in (8, 20, 21):
+        s = SolverCUDA(grade, storage=storage, soa=True)
+        s.definirTipos(tipo)
+        s.configurar(**CFG, esponja=esp)
+        s.definirBloco(64, code)
+        s.definirPopulacoes(g0)
+        s.passo(11)
+        s.passoComForcas(3)
+        s.passo(4)
+        out.append(s.lerPopulacoes()[:, fl])
+        s.destruir()
+    assert np.array_equal(out[0], out[1]) and np.array_equal(out[0], out[2])
