@@ -43,7 +43,6 @@ struct TunnelDesc {
   Params P;
   Uni<float> U;
   int tx, ty, gx, gy;   // tile shape, tiles along x and y
-  long long tile0;      // first global tile of this tunnel
 };
 
 constexpr int kTile = 128;
@@ -57,17 +56,21 @@ struct BatchArgs {
   int ntiles;
   int aos;                     // every tunnel of this launch keeps its set in the AoSoA layout (else SoA)
   int first[kPerLaunch + 1];   // first tile of each tunnel (prefix), local to this launch
+  const int4* tiles;           // per tile: {tunnel | log2(tile width) << 8, x0, y0, z}, device
   TunnelDesc t[kPerLaunch];
 };
 static_assert(sizeof(BatchArgs) < 32000, "kernel parameter space");
 
 template <class St, int PAR, bool FAST, int MINB, bool AOS>
 __global__ void __launch_bounds__(kTile, MINB) k_batch_step(const __grid_constant__ BatchArgs A) {
-  // The tunnel of a tile is found by a search over the launch's first-tile
-  // prefix; the index is the same for the whole CTA, so the search and the
-  // descriptor reads (straight from the parameter bank, no staging) run on
-  // the uniform datapath.
+  // A tile's tunnel is found by a search over the launch's first-tile
+  // prefix: the index is the same for the whole CTA, so the search and the
+  // descriptor reads (straight from the parameter bank) stay on the uniform
+  // datapath.  Its origin comes from its word in the launch's tile table (one
+  // 16-byte load, the same address for the whole CTA), which spares the
+  // divisions by the tile counts.
   for (int t = blockIdx.x; t < A.ntiles; t += gridDim.x) {
+    const int4 w = __ldg(A.tiles + t);
     int lo = 0, hi = A.ntun;
     while (hi - lo > 1) {
       const int mid = (lo + hi) >> 1;
@@ -75,14 +78,10 @@ __global__ void __launch_bounds__(kTile, MINB) k_batch_step(const __grid_constan
       else hi = mid;
     }
     const TunnelDesc& D = A.t[lo];
-    const int tx = D.tx, gx = D.gx, gy = D.gy;
-    const int local = t - A.first[lo];
-    const int bxi = local % gx;
-    const int rest = local / gx;
-    const int byi = rest % gy;
-    const int z = rest / gy;
-    const int x = bxi * tx + (int)(threadIdx.x % tx);
-    const int y = byi * D.ty + (int)(threadIdx.x / tx);
+    const int lg = w.x >> 8;
+    const int x = w.y + (int)(threadIdx.x & ((1u << lg) - 1u));
+    const int y = w.z + (int)(threadIdx.x >> lg);
+    const int z = w.w;
     if (x < D.d.nx && y < D.d.ny) {
       const int32_t cell = (z * D.d.ny + y) * D.d.nx + x;
       if constexpr (AOS && FAST)
@@ -147,6 +146,8 @@ struct lbm_batch {
   cudaEvent_t fork = nullptr;
   std::vector<cudaEvent_t> joins;
   std::vector<void*> blf;            // per tunnel: nz inlet boundary-layer factors
+  int4* tiles = nullptr;             // tile table of the persistent launches (mode 1)
+  size_t tiles_cap = 0;              // its capacity in tiles
 };
 
 namespace {
@@ -209,32 +210,52 @@ int sync_desc(lbm_batch* b) {
     runs.push_back({k0, k1});
     k0 = k1;
   }
+  std::vector<int4> table;           // every launch's tile words, one after the other
+  std::vector<size_t> table_at;      // where each launch's words start
   for (const auto& run : runs) {
     BatchArgs A;
     memset(&A, 0, sizeof A);
     const size_t k0 = run.first, k1 = run.second;
     A.aos = b->host[order[k0]].d.aos;
+    table_at.push_back(table.size());
     long long t = 0;
     for (size_t kk = k0; kk < k1; ++kk) {
       const size_t k = order[kk];
       TunnelDesc& D = b->host[k];
       const int tx = b->tile_req[k] ? b->tile_req[k] : pick_tile(D.d.nx, D.d.ny);
+      const int lg = tx == 32 ? 5 : (tx == 64 ? 6 : 7);
       D.tx = tx;
       D.ty = kTile / tx;
       D.gx = (D.d.nx + tx - 1) / tx;
       D.gy = (D.d.ny + D.ty - 1) / D.ty;
-      D.tile0 = t;
       A.first[kk - k0] = (int)t;
       A.t[kk - k0] = D;
       t += (long long)D.gx * D.gy * D.d.nz;
+      if (t >= INT32_MAX) return bfail(LBM_EINVAL, "too many tiles in one launch (keep a batch under 2^31 tiles)");
+      for (int z = 0; z < D.d.nz; ++z)
+        for (int by = 0; by < D.gy; ++by)
+          for (int bx = 0; bx < D.gx; ++bx)
+            table.push_back(make_int4((int)(kk - k0) | (lg << 8), bx * tx, by * D.ty, z));
     }
-    if (t >= INT32_MAX) return bfail(LBM_EINVAL, "too many tiles in one launch (keep a batch under 2^31 tiles)");
     A.ntun = (int)(k1 - k0);
     A.first[A.ntun] = (int)t;
     A.ntiles = (int)t;
     b->args.push_back(A);
     total += t;
   }
+  // the table goes to the device once per change of the descriptors (no
+  // launch of the old table is in flight: the stream is drained first)
+  BCK(cudaStreamSynchronize(b->stream), "stream sync");
+  if (table.size() > b->tiles_cap) {
+    if (b->tiles) cudaFree(b->tiles);
+    b->tiles = nullptr;
+    b->tiles_cap = 0;
+    BCK(cudaMalloc(&b->tiles, table.size() * sizeof(int4)), "tile table");
+    b->tiles_cap = table.size();
+  }
+  if (!table.empty())
+    BCK(cudaMemcpy(b->tiles, table.data(), table.size() * sizeof(int4), cudaMemcpyHostToDevice), "tile table upload");
+  for (size_t q = 0; q < b->args.size(); ++q) b->args[q].tiles = b->tiles + table_at[q];
   b->ntiles = total;
   b->desc_dirty = false;
   return LBM_OK;
@@ -388,6 +409,7 @@ int lbm_batch_destroy(lbm_batch* b) {
   for (void* p : b->allocs) cudaFree(p);
   if (b->partials) cudaFree(b->partials);
   if (b->stage) cudaFree(b->stage);
+  if (b->tiles) cudaFree(b->tiles);
   if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
   delete b;
   return LBM_OK;

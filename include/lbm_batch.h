@@ -8,7 +8,8 @@
  * lbm_batch_step captures 32 steps of every tunnel into a CUDA graph and
  * replays it: by default one independent chain of single-tunnel launches per
  * tunnel (the GPU overlaps the chains), or (lbm_batch_set_mode 1) one
- * persistent launch per step whose CTAs walk the tiles of every tunnel.  Arithmetic is identical to lbm_step (same per-cell code), so
+ * persistent launch per step and layout class whose CTAs walk the tiles of
+ * those tunnels.  Arithmetic is identical to lbm_step (same per-cell code), so
  * each tunnel's state equals the state a separate lbm_ctx would reach.
  * Storage forms: LBM_F32, LBM_F16S, LBM_BF16S (in-place layout only; a
  * tunnel whose nx is a multiple of 32 keeps its set in the AoSoA layout of
@@ -46,7 +47,9 @@ int lbm_batch_set_tile(lbm_batch* b, int k, int tile_x);
 /* 0 (default): each step of each tunnel is its own launch of the
  * single-tunnel kernel; the captured graph holds one chain per tunnel and
  * the GPU runs the chains concurrently.  1: one persistent launch per step
- * walks the tiles of all tunnels (descriptors in the launch parameters). */
+ * and layout class walks the tiles of those tunnels (descriptors in the
+ * launch parameters, tile origins in a device table of 16 bytes per tile
+ * that the batch allocates when it first needs it). */
 int lbm_batch_set_mode(lbm_batch* b, int mode);
 int lbm_batch_info(lbm_batch* b, int64_t* total_cells, int64_t* device_bytes);
 /* The tile width along x tunnel k's tiles use in the persistent launch. */
