@@ -100,6 +100,8 @@ def precision_study(grid):
     out = {"recorded": True, "source": d.get("command"), "steps": d.get("steps"), "forms": {}}
     for k, v in d.get("forms", {}).items():
         out["forms"][k] = {kk: v[kk] for kk in ("cd", "cd_err_vs_f64", "u_l2_rel_err_vs_f64") if kk in v}
+        if "stored_values" in v:
+            out["forms"][k]["subnormal_share_of_stored_values"] = v["stored_values"]["subnormal_share"]
     return out
 
 

@@ -35,6 +35,9 @@ UNITS = {
     "lbm_inst_f64.cu": ["-fmad=false"],
     "lbm_inst_f16s.cu": ["-fmad=false"],
     "lbm_inst_bf16s.cu": ["-fmad=false"],
+    "lbm_inst_f32_clo.cu": ["-fmad=false"],
+    "lbm_inst_f16s_clo.cu": ["-fmad=false"],
+    "lbm_inst_bf16s_clo.cu": ["-fmad=false"],
     "vox.cu": ["-fmad=false"],
     "lbm_noalloc.cu": ["-fmad=false"],
     "lbm_batch.cu": ["-fmad=false"],

@@ -319,6 +319,8 @@ int launch_step(lbm_ctx* c, bool mac, double* force) {
     if (!c->clo) return fail(LBM_ESTATE, "closure >= 1 but no network set (call lbm_set_closure first)");
     if (!c->inplace || (c->flags & LBM_FLAG_STRICT) || !c->ops.step_closure)
       return fail(LBM_ENOTSUP, "the learned closure runs in the in-place FAST step with fp32 arithmetic only");
+    if ((int64_t)Q * c->N >= (int64_t)INT32_MAX)
+      return fail(LBM_ENOTSUP, "the learned closure addresses the set with 32-bit indices (19 N < 2^31 cells)");
     const int every = c->P.closure;
     int mode = 0;
     if (every > 1) {

@@ -2,5 +2,9 @@
 #include "lbm_kernels.cuh"
 
 namespace lbm {
-Ops ops_bf16s() { return OpsImpl<StBF16S>::make(); }
+Ops ops_bf16s() {
+  Ops o = OpsImpl<StBF16S>::make();
+  o.step_closure = closure_bf16s();
+  return o;
+}
 }  // namespace lbm

@@ -2,5 +2,9 @@
 #include "lbm_kernels.cuh"
 
 namespace lbm {
-Ops ops_f16s() { return OpsImpl<StF16S>::make(); }
+Ops ops_f16s() {
+  Ops o = OpsImpl<StF16S>::make();
+  o.step_closure = closure_f16s();
+  return o;
+}
 }  // namespace lbm

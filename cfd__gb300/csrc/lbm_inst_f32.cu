@@ -2,5 +2,9 @@
 #include "lbm_kernels.cuh"
 
 namespace lbm {
-Ops ops_f32() { return OpsImpl<StF32>::make(); }
+Ops ops_f32() {
+  Ops o = OpsImpl<StF32>::make();
+  o.step_closure = closure_f32();
+  return o;
+}
 }  // namespace lbm

@@ -496,7 +496,8 @@ struct CloShared {
 // MODE 1: the same, and nu_t (NaN for a fallback cell) is stored per cell.
 // MODE 2: no network: the rates come from the stored nu_t (Smagorinsky where
 //   it is NaN) -- the steps between two network evaluations of a closure
-//   that is evaluated every k-th step.
+//   that is evaluated every k-th step.  Not instantiated: those steps run
+//   k_step_held, the plain step's cell code with the same rate rule.
 // This kernel is the warp engine (closure_mlp.cuh, mma.sync per 32 cells);
 // the CTA engine is k_step_closure_tc below.  Every other class goes through
 // collide() unchanged, before the network.  Modes 0 and 1 run 64 x 2 threads
@@ -1191,6 +1192,9 @@ struct Launch {
   int pipe = 0;  // > 0: pipelined step, cells per thread along z (4, 8, 16)
 };
 
+using StepClosureFn = cudaError_t (*)(const Dev&, const Params&, int parity, bool mac, bool frc, int engine,
+                                      int mode, const CloArgs&, Launch, cudaStream_t);
+
 struct Ops {
   cudaError_t (*step)(const Dev&, const Params&, int parity, bool inplace, bool mac, bool frc, bool fast, Launch,
                       cudaStream_t);
@@ -1202,8 +1206,7 @@ struct Ops {
   cudaError_t (*mass)(const Dev&, int parity, bool inplace, double* partials, Launch, cudaStream_t);
   // in-place FAST step with the learned closure (engine 0/1, mode 0/1/2 of
   // k_step_closure); null for the fp64 reference form
-  cudaError_t (*step_closure)(const Dev&, const Params&, int parity, bool mac, bool frc, int engine, int mode,
-                              const CloArgs&, Launch, cudaStream_t);
+  StepClosureFn step_closure;
   int elem_bytes;
 };
 
@@ -1331,29 +1334,26 @@ struct OpsImpl {
     }
   }
   template <int PAR, bool MAC, bool FRC, int ENG, int MODE>
+  // The closure steps index the set with 32 bits (the caller refuses
+  // 19 N >= 2^31).
   static void go_closure(const Dev& d, const Params& P, const Uni<float>& U, const CloArgs& A, Launch L,
                          cudaStream_t s) {
-    if constexpr (ENG == 1 && MODE != 2) {
-      if ((int64_t)Q * d.N >= (int64_t)INT32_MAX) go_closure_tc<PAR, MAC, FRC, true, MODE>(d, P, U, A, s);
-      else go_closure_tc<PAR, MAC, FRC, false, MODE>(d, P, U, A, s);
+    static_assert(MODE != 2, "held steps run k_step_held");
+    if constexpr (ENG == 1) {
+      go_closure_tc<PAR, MAC, FRC, false, MODE>(d, P, U, A, s);
       return;
     }
     if constexpr (sizeof(R) == 4 && ENG == 0) {
-      // network steps: 64 x 2 threads, four warps (one 128-row MMA tile for
-      // engine 1); held steps: the plain step's launch shape
-      dim3 block(64, 2), grid((d.nx + 63) / 64, (d.ny + 1) / 2, d.nz);
-      if (MODE == 2) { block = L.block; grid = L.grid; }
-      if ((int64_t)Q * d.N >= (int64_t)INT32_MAX)
-        k_step_closure<St, PAR, MAC, FRC, true, ENG, MODE><<<grid, block, 0, s>>>(d, P, U, A);
-      else
-        k_step_closure<St, PAR, MAC, FRC, false, ENG, MODE><<<grid, block, 0, s>>>(d, P, U, A);
+      // network steps: 64 x 2 threads, four warps
+      const dim3 block(64, 2), grid((d.nx + 63) / 64, (d.ny + 1) / 2, d.nz);
+      k_step_closure<St, PAR, MAC, FRC, false, ENG, MODE><<<grid, block, 0, s>>>(d, P, U, A);
     }
   }
   template <int PAR, bool MAC, bool FRC>
   static void go_closure_m(const Dev& d, const Params& P, const Uni<float>& U, int engine, int mode,
                            const CloArgs& A, Launch L, cudaStream_t s) {
     if constexpr (sizeof(R) == 4) {
-      if (mode == 2 && (int64_t)Q * d.N < (int64_t)INT32_MAX) {
+      if (mode == 2) {
         const Uni<R> Us = make_uni<R>(P, R(St::kScale));
         const SlotPtrs T = make_slots<St>(d, PAR);
         if (d.aos) k_step_held<St, PAR, MAC, FRC, true><<<L.grid, L.block, 0, s>>>(d, P, Us, T, A.nu, A.coef);
@@ -1361,8 +1361,7 @@ struct OpsImpl {
         return;
       }
     }
-    if (mode == 2) go_closure<PAR, MAC, FRC, 0, 2>(d, P, U, A, L, s);
-    else if (engine == 0) { mode == 1 ? go_closure<PAR, MAC, FRC, 0, 1>(d, P, U, A, L, s) : go_closure<PAR, MAC, FRC, 0, 0>(d, P, U, A, L, s); }
+    if (engine == 0) { mode == 1 ? go_closure<PAR, MAC, FRC, 0, 1>(d, P, U, A, L, s) : go_closure<PAR, MAC, FRC, 0, 0>(d, P, U, A, L, s); }
     else { mode == 1 ? go_closure<PAR, MAC, FRC, 1, 1>(d, P, U, A, L, s) : go_closure<PAR, MAC, FRC, 1, 0>(d, P, U, A, L, s); }
   }
   static cudaError_t step_closure(const Dev& d, const Params& P, int parity, bool mac, bool frc, int engine,
@@ -1380,14 +1379,17 @@ struct OpsImpl {
     }
     return cudaErrorNotSupported;
   }
+  // Everything but the closure steps, whose kernels are instantiated in a
+  // unit of their own (lbm_inst_*_clo.cu) so that the two compile in parallel.
   static Ops make() {
     Ops o;
     o.step = &step; o.init = &init; o.put_dir = &put_dir; o.get_dir = &get_dir;
     o.macros = &macros; o.forces = &forces; o.mass = &mass;
-    o.step_closure = sizeof(R) == 4 ? &step_closure : nullptr;
+    o.step_closure = nullptr;
     o.elem_bytes = (int)sizeof(typename St::store_t);
     return o;
   }
+  static StepClosureFn closure_entry() { return &step_closure; }
 };
 
 // What other units of the library see of a context.
@@ -1404,5 +1406,8 @@ Ops ops_f32();
 Ops ops_f64();
 Ops ops_f16s();
 Ops ops_bf16s();
+StepClosureFn closure_f32();
+StepClosureFn closure_f16s();
+StepClosureFn closure_bf16s();
 
 }  // namespace lbm

@@ -70,6 +70,30 @@ def caso_precisao(grade, voxelizador=None):
     return mt["tipo"], cfg, area
 
 
+def _subnormal_share(s, fluid):
+    """Where the fp16 store's rounding sits: of the fluid cells' stored values
+    g·2^10 at the end of the run, the share that is zero, the share in the
+    subnormal range (0 < |v| < 2^-14, where fp16 keeps fewer than 11 bits),
+    and per direction the median |g|.  A per-direction power-of-two scale
+    changes the rounding of the subnormal share only: a normal fp16 value
+    keeps 11 significant bits at any exponent."""
+    g = s.lerPopulacoes()
+    out = {"per_direction_median_abs_g": [], "per_direction_subnormal_share": []}
+    n_sub = n_zero = n_all = 0
+    for i in range(19):
+        v = np.abs(g[i, fluid]) * 1024.0
+        z = int(np.count_nonzero(v == 0.0))
+        sb = int(np.count_nonzero((v > 0.0) & (v < 2.0 ** -14)))
+        n_zero += z
+        n_sub += sb
+        n_all += v.size
+        out["per_direction_median_abs_g"].append(float(np.median(v)) / 1024.0)
+        out["per_direction_subnormal_share"].append(sb / v.size)
+    out["zero_share"] = n_zero / n_all
+    out["subnormal_share"] = n_sub / n_all
+    return out
+
+
 def precisao(steps=10000, grade=None, forms=("f64", "f32", "f16s", "bf16s"), sample=50):
     import torch
 
@@ -108,12 +132,15 @@ def precisao(steps=10000, grade=None, forms=("f64", "f32", "f16s", "bf16s"), sam
             cds.append(coeficientes(f, units, area, grade)["cd"])
         s.atualizarMacros()
         m = s.lerMacros().reshape(-1, 4)[:, :3].astype(np.float64)[fluid]
+        sub = _subnormal_share(s, fluid) if form == "f16s" else None
         s.destruir()
         tail = cds[len(cds) * 3 // 4:]
         cd = float(np.mean(tail))
         mlups = N * steps / (ms_total / 1e3) / 1e6
         rec = {"MLUPS": mlups, "roofline_frac": BYTES[form] * mlups * 1e6 / 1e9 / _peak(),
                "cd": cd, "cd_finite": bool(np.isfinite(cds).all())}
+        if sub is not None:
+            rec["stored_values"] = sub
         if ref_u is None:
             ref_u, ref_cd = m, cd
         else:
