@@ -532,11 +532,12 @@ def casos(storage_judge="f64"):
     """The stated outputs of the plain-method workloads.
 
     Mesh body, 320x160x128 (no-slip floor, u_in 0.06, Cs 0.12): Re 2000 on
-    the 96-cell length gives omega+ = 1.98295, above the reference's
-    stability ceiling omega_max = 1.90 (src/core/units.js:60-92).  10 000
-    steps with the stability check of tests/estabilidade.html every 1000;
-    Cd / Cl averaged over steps 5000-10000 if it survives; then the run at
-    the clamped viscosity (omega+ = 1.90, as Units does,
+    the body's 96-cell length gives nu = 0.00288 and omega+ = 1.96603 (on its
+    48-cell semi-axis, nu = 0.00144 and omega+ = 1.98287); both are above the
+    reference's stability ceiling omega_max = 1.90 (src/core/units.js:60-92).
+    10 000 steps of each with the stability check of tests/estabilidade.html
+    every 1000; Cd / Cl averaged over steps 5000-10000 if it survives; then
+    the run at the clamped viscosity (omega+ = 1.90, as Units does,
     src/core/units.js:157-164), with its fp64 run as the accuracy judge.
 
     Sphere, 128x64x64 (D = 16 at (40, 32, 32), Re 100, Cs 0.1): the Cd series
@@ -554,7 +555,9 @@ def casos(storage_judge="f64"):
     area = areaFrontalCorpo(corpo, g2)
     out["mesh_body"]["workload"] = desc
     out["mesh_body"]["frontal_area"] = area
-    for nome, omega in (("re2000", cfg["omegaPlus"]), ("clamped_omega_1.90", 1.90)):
+    omega48 = omega_from_nu(0.06 * 48 / 2000)
+    for nome, omega in (("re2000", cfg["omegaPlus"]), ("re2000_on_semi_axis_48", omega48),
+                        ("clamped_omega_1.90", 1.90)):
         c = dict(cfg, omegaPlus=omega)
         rec, cd, _ = rodar_caso(g2, tipo, c, area, 10000, 0.06, (5000, 10000))
         rec["omega_plus"] = omega
