@@ -197,7 +197,7 @@ __global__ void __launch_bounds__(128) k_eval_tc(const float* __restrict__ feats
                                                  unsigned* __restrict__ err) {
   __shared__ TcPersist S;
   const int tid = threadIdx.x;
-  const uint32_t tmem = tcp_setup(S, F->tcb, tid);
+  const uint32_t tmem = tcp_setup(S, F->tcb, F->w3b, tid);
   uint32_t phase = 0;
   bool dead = false;
   const long long ntiles = (m + TC_ROWS - 1) / TC_ROWS;
@@ -395,8 +395,14 @@ void closure_pack(const closure_weights* w, MlpFrag* F) {
     for (int k = 0; k < NH; ++k) put(TC_B1_BYTES, n, k, TC_K2, w->w2[n * NH + k]);
     put(TC_B1_BYTES, n, NH, TC_K2, w->b2[n]);
   }
-  for (int k = 0; k < NH; ++k) put(TC_B1_BYTES + TC_B2_BYTES, 0, k, TC_K2, w->w3[k]);
-  put(TC_B1_BYTES + TC_B2_BYTES, 0, NH, TC_K2, w->b3);
+  auto bf16f = [](float v) {
+    const uint32_t u = (uint32_t)f32_to_bf16(v) << 16;
+    float f;
+    memcpy(&f, &u, 4);
+    return f;
+  };
+  for (int k = 0; k < NH; ++k) F->w3b[k] = bf16f(w->w3[k]);
+  F->w3b[NH] = bf16f(w->b3);
   for (int a = 0; a < NI; ++a) {
     F->mean[a] = w->mean[a];
     F->inv_std[a] = w->std[a] != 0.0f ? 1.0f / w->std[a] : 0.0f;

@@ -26,6 +26,7 @@ struct MlpFrag {
   uint2 w2[4][2][32];   // layer 2: nt 0..3, kt 0..1
   uint2 w3[2][32];      // layer 3: n 0 only (n 1..7 zero), kt 0..1
   float b1[32], b2[32], b3;
+  float w3b[33];                // output weights and bias, bf16-rounded (CTA engine's CUDA-core layer)
   float mean[6], inv_std[6];
   float nu_scale, nu_max;
   float lo[6], hi[6];           // raw-feature range of the training set

@@ -6,10 +6,14 @@
 // tid).  Per layer: every thread writes its row of the A operand to shared
 // memory, one thread issues the MMA(s) and commits them to an mbarrier, every
 // thread waits on it and reads its row of the accumulator back with
-// tcgen05.ld.  A CTA sets up once and then walks many tiles (persistent).  Biases ride in the K dimension: A carries a constant 1 in
-// column kb and B holds the bias there (layer 1: K = 16 = 6 features + 1 +
-// 9 zeros; layers 2, 3: K = 48 = 32 hidden + 1 + 15 zeros), so the
-// accumulators start at zero and no bias add is needed.
+// tcgen05.ld.  A CTA sets up once and then walks many tiles (persistent).
+// The two hidden layers run on the tensor cores; the 32 -> 1 output layer
+// runs on the CUDA cores from the second layer's accumulators (one dot
+// product per thread), which spares a third barrier and MMA round trip.
+// Biases ride in the K dimension: A carries a constant 1 in column kb and B
+// holds the bias there (layer 1: K = 16 = 6 features + 1 + 9 zeros; layer 2:
+// K = 48 = 32 hidden + 1 + 15 zeros), so the accumulators start at zero and
+// no bias add is needed.
 //
 // Operand layout in shared memory: K-major, no swizzle, the canonical
 // "core matrix" arrangement: a core matrix is 8 rows x 16 bytes (8 bf16 along
@@ -34,8 +38,7 @@ constexpr int TC_ROWS = 128;        // cells per tile (M)
 constexpr int TC_K1 = 16, TC_K2 = 48;
 constexpr int TC_B1_BYTES = 32 * TC_K1 * 2;      // 1024
 constexpr int TC_B2_BYTES = 32 * TC_K2 * 2;      // 3072
-constexpr int TC_B3_BYTES = 16 * TC_K2 * 2;      // 1536
-constexpr int TC_B_BYTES = TC_B1_BYTES + TC_B2_BYTES + TC_B3_BYTES;   // 5632
+constexpr int TC_B_BYTES = TC_B1_BYTES + TC_B2_BYTES;   // 4096 (the output layer runs on the CUDA cores)
 constexpr uint32_t TC_TMEM_COLS = 32;
 constexpr uint32_t TC_WAIT_LIMIT = 1u << 20;     // suspended mbarrier tries (<= ~1 us each) before giving up
 
@@ -137,7 +140,7 @@ __device__ __forceinline__ void sts128(uint8_t* base, uint32_t off, uint32_t a, 
 // The engine of the persistent closure step (k_step_closure_tc): a CTA sets
 // up once (TMEM columns, the mbarrier, the B operands, the constant columns
 // of the A operands) and then walks many 128-cell tiles; per tile it pays one
-// CTA barrier and one MMA round trip per layer.
+// CTA barrier and one MMA round trip per hidden layer.
 //
 // A operands live in two buffers so that the constant columns never need
 // rewriting: a1 (K = 16: features 0..5, the bias 1 at element 6, zeros to
@@ -148,6 +151,8 @@ struct TcPersist {
   alignas(128) uint8_t a1[TC_ROWS * TC_K1 * 2];
   alignas(128) uint8_t a2[TC_ROWS * TC_K2 * 2];
   alignas(128) uint8_t b[TC_B_BYTES];
+  float w3[32];      // output layer on the CUDA cores: weights and bias,
+  float b3;          // bf16-rounded (the values the MMA form would use)
   alignas(8) uint64_t mbar;
   uint32_t tmem;
   uint32_t err;      // a wait gave up: no further MMA is issued
@@ -157,8 +162,10 @@ __device__ __forceinline__ void mbar_init_fence() {
   asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
 }
 
-// Set-up of a persistent CTA (128 threads, every thread calls it).
-__device__ __forceinline__ uint32_t tcp_setup(TcPersist& S, const uint4* __restrict__ bw, int tid) {
+// Set-up of a persistent CTA (128 threads, every thread calls it).  w3b:
+// the output layer's 32 weights and its bias, bf16-rounded, as fp32.
+__device__ __forceinline__ uint32_t tcp_setup(TcPersist& S, const uint4* __restrict__ bw,
+                                              const float* __restrict__ w3b, int tid) {
   if (tid < 32) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_addr(&S.tmem)),
                  "r"(TC_TMEM_COLS)
@@ -172,6 +179,8 @@ __device__ __forceinline__ uint32_t tcp_setup(TcPersist& S, const uint4* __restr
   }
   uint4* bd = reinterpret_cast<uint4*>(S.b);
   for (int i = tid; i < TC_B_BYTES / 16; i += TC_ROWS) bd[i] = __ldg(bw + i);
+  if (tid < 32) S.w3[tid] = __ldg(w3b + tid);
+  if (tid == 32) S.b3 = __ldg(w3b + 32);
   // constant columns of this thread's rows
   sts128(S.a1, tc_off(tid, 8, TC_K1), 0u, 0u, 0u, 0u);
   sts128(S.a2, tc_off(tid, 32, TC_K2), 0x3F80u, 0u, 0u, 0u);   // bf16 1.0 at element 32
@@ -230,11 +239,32 @@ __device__ __forceinline__ void tcp_hidden_to_a2(TcPersist& S, uint32_t tmem, in
   }
 }
 
+// Output layer (32 -> 1) of this thread's row on the CUDA cores, from the
+// second hidden layer's accumulators in TMEM: ReLU, bf16 rounding (the
+// operand the MMA form would read), then a fixed-order fp32 dot product.
+__device__ __forceinline__ float tcp_output(const TcPersist& S, uint32_t tmem, int tid) {
+  const uint32_t lane_addr = tmem + ((uint32_t)(tid & ~31) << 16);
+  float y = S.b3;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    float v[16];
+    tc_ld16(lane_addr + 16u * h, v);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const uint32_t q = tc_relu_pack(v[2 * i], v[2 * i + 1]);
+      y = fmaf(__uint_as_float(q << 16), S.w3[16 * h + 2 * i], y);
+      y = fmaf(__uint_as_float(q & 0xffff0000u), S.w3[16 * h + 2 * i + 1], y);
+    }
+  }
+  return y;
+}
+
 // The network for the CTA's current tile: x = this thread's normalised
 // features (zeros for threads without a fluid cell).  All 128 threads call
-// it.  `phase` is the parity of the mbarrier's next phase (three phases per
-// tile), `dead` the give-up state (tcp_issue).  NaN when the network was not
-// run or a wait gave up.
+// it.  `phase` is the parity of the mbarrier's next phase (two phases per
+// tile: the hidden layers on the tensor cores, the output layer on the CUDA
+// cores), `dead` the give-up state (tcp_issue).  NaN when the network was
+// not run or a wait gave up.
 __device__ __forceinline__ float tcp_mlp(TcPersist& S, uint32_t tmem, int tid, const float (&x)[6], uint32_t& phase,
                                          bool& dead) {
   const float nan = __int_as_float(0x7fc00000);
@@ -247,11 +277,7 @@ __device__ __forceinline__ float tcp_mlp(TcPersist& S, uint32_t tmem, int tid, c
   if (!tcp_issue(S, S.a2, tmem, tid, TC_K2, 32, 3, TC_B1_BYTES, dead)) return nan;
   ok = tcp_wait(S, phase, dead) && ok;
   phase ^= 1u;
-  tcp_hidden_to_a2(S, tmem, tid);
-  if (!tcp_issue(S, S.a2, tmem, tid, TC_K2, 16, 3, TC_B1_BYTES + TC_B2_BYTES, dead)) return nan;
-  ok = tcp_wait(S, phase, dead) && ok;
-  phase ^= 1u;
-  const float y = tc_ld1(tmem + ((uint32_t)(tid & ~31) << 16));
+  const float y = tcp_output(S, tmem, tid);
   return ok ? y : nan;
 }
 

@@ -653,8 +653,9 @@ k_step_closure(Dev d, Params P, Uni<float> U, CloArgs A) {
 // sets up its tensor memory, mbarrier and B operands once.  Per tile every
 // thread pulls its cell exactly as k_step_closure does, collides the
 // boundary classes at once, and for a FLUIDO cell keeps the pulled g and its
-// moments in registers while the three layers run (one CTA barrier and one
-// tcgen05.mma round trip per layer); then the rates and TRT as in
+// moments in registers while the network runs (one CTA barrier and one
+// tcgen05.mma round trip per hidden layer, the output layer on the CUDA
+// cores); then the rates and TRT as in
 // k_step_closure.  MODE 0 or 1 (mode 2 has no network: k_step_closure).
 // Rates of the closure's held steps (evaluated every k-th step): from the
 // eddy viscosity stored per cell by the last network step, the Smagorinsky
@@ -703,7 +704,7 @@ __global__ void __launch_bounds__(128, 8) k_step_held(Dev d, Params P, Uni<typen
 constexpr int kClosureTcPerSm = 6;
 template <class St, int PAR, bool MAC, bool FRC, bool W64, int MODE, bool AOS>
 __global__ void __launch_bounds__(128, kClosureTcPerSm)
-k_step_closure_tc(Dev d, Params P, Uni<float> U, CloArgs A, SlotPtrs T, int gx, int gy, long long ntiles) {
+k_step_closure_tc(Dev d, Params P, Uni<float> U, CloArgs A, SlotPtrs T, int gx, int gy) {
   using R = float;
   using S = typename St::store_t;
   using Off = typename OffT<W64>::type;
@@ -711,16 +712,17 @@ k_step_closure_tc(Dev d, Params P, Uni<float> U, CloArgs A, SlotPtrs T, int gx, 
   static_assert(MODE != 2, "held steps have no network");
   __shared__ TcPersist SH;
   const int tid = threadIdx.x;
-  const uint32_t tmem = tcp_setup(SH, A.F->tcb, tid);
+  const uint32_t tmem = tcp_setup(SH, A.F->tcb, A.F->w3b, tid);
   uint32_t phase = 0;
   bool dead = false;
   unsigned nfb = 0;
   const int nx = d.nx, ny = d.ny;
-  for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const int bxi = (int)(t % gx);
-    const long long rest = t / gx;
-    const int byi = (int)(rest % gy);
-    const int z = (int)(rest / gy);
+  // tile t = (z gy + byi) gx + bxi, walked with stride gridDim.x: the
+  // decomposition is divided out once and then advanced with carries
+  const int G = (int)gridDim.x;
+  const int gsx = G % gx, gsy = (G / gx) % gy, gsz = G / (gx * gy);
+  int bxi = (int)blockIdx.x % gx, byi = ((int)blockIdx.x / gx) % gy, z = (int)blockIdx.x / (gx * gy);
+  for (; z < d.nz;) {
     const int x = bxi * 64 + (tid & 63), y = byi * 2 + (tid >> 6);
     const bool inr = x < nx && y < ny;
     const Off cell = ((Off)z * ny + (inr ? y : 0)) * nx + (inr ? x : 0);
@@ -831,6 +833,13 @@ k_step_closure_tc(Dev d, Params P, Uni<float> U, CloArgs A, SlotPtrs T, int gx, 
       }
       trt_emit_fast<R>(U, x, g, e0, ns, nd, omegaP, omegaM, U.sp_tf, emit);
     }
+    bxi += gsx;
+    const int cx_ = bxi >= gx;
+    bxi -= cx_ ? gx : 0;
+    byi += gsy + cx_;
+    const int cy_ = byi >= gy;
+    byi -= cy_ ? gy : 0;
+    z += gsz + cy_;
   }
   tcp_teardown(SH, tmem, tid, phase, dead);
   // fallback count: one atomic per warp for the whole kernel
@@ -1330,12 +1339,12 @@ struct OpsImpl {
       const int gx = (d.nx + 63) / 64, gy = (d.ny + 1) / 2;
       const long long ntiles = (long long)gx * gy * d.nz;
       const unsigned grid = (unsigned)std::max<long long>(1, std::min<long long>(ntiles, (long long)per_sm * sms));
-      k<<<grid, 128, 0, s>>>(d, P, U, A, T, gx, gy, ntiles);
+      k<<<grid, 128, 0, s>>>(d, P, U, A, T, gx, gy);
     }
   }
-  template <int PAR, bool MAC, bool FRC, int ENG, int MODE>
   // The closure steps index the set with 32 bits (the caller refuses
   // 19 N >= 2^31).
+  template <int PAR, bool MAC, bool FRC, int ENG, int MODE>
   static void go_closure(const Dev& d, const Params& P, const Uni<float>& U, const CloArgs& A, Launch L,
                          cudaStream_t s) {
     static_assert(MODE != 2, "held steps run k_step_held");
