@@ -104,7 +104,9 @@ int closure_samples(lbm_ctx* ctx, float tau0_coarse, float s_min, int x0, int x1
 /* Network for a solver context.  lbm_params.closure = 1 then evaluates it in
  * every step; closure = k > 1 evaluates it every k-th step and relaxes the
  * steps in between with the nu_t it gave (held per cell, 4 bytes a cell).
- * LBM_ENOTSUP for the fp64 reference form, STRICT arithmetic and ping-pong. */
+ * LBM_ENOTSUP for the fp64 reference form, STRICT arithmetic and ping-pong;
+ * a step with the closure on a set of 19 N >= 2^31 elements (N > 113 M cells)
+ * returns LBM_ENOTSUP too (the closure steps index with 32 bits). */
 int lbm_set_closure(lbm_ctx* ctx, const closure_weights* w);
 
 /* Engine of the fused step's network (see closure_eval); default 0. */
