@@ -49,7 +49,7 @@ METRIC = "MLUPS & % HBM roofline on 1 GB300, FP16-store vs FP32 plain, Cd err \u
 from cfd__gb300.cargas import GRIDS  # noqa: E402
 
 GRID = GRIDS["320x160x128"]
-BYTES_PER_CELL = {"f32": 152, "f16s": 76, "bf16s": 76, "f64": 304}
+BYTES_PER_CELL = {"f32": 152, "f16s": 76, "bf16s": 76, "f64": 304, "f16sr": 76, "bf16sr": 76}
 
 
 def oracle_voxelizer(pos, idx, grade):
@@ -517,7 +517,7 @@ def run_ours(args):
                                             "note": "passoComForcas(K): step with the fused force, its per-step "
                                                     "slot clear and one read-back of the K forces"}
         s2.destruir()
-        for st in ("f16s", "bf16s"):
+        for st in ("f16s", "bf16s", "f16sr", "bf16sr"):
             s2 = make(st)
             s2.passo(args.warmup)
             ms2, R2 = timed(s2, stream, args.steps)
@@ -629,7 +629,7 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=40)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--storage", default="f32", choices=["f32", "f16s", "bf16s", "f64"])
+    ap.add_argument("--storage", default="f32", choices=["f32", "f16s", "bf16s", "f64", "f16sr", "bf16sr"])
     ap.add_argument("--grid", default="512x256x192", choices=sorted(GRIDS))
     ap.add_argument("--no-forms", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")

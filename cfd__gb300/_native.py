@@ -12,7 +12,7 @@ import threading
 
 from . import build as _build
 
-F32, F16S, BF16S, F64 = 0, 1, 2, 3
+F32, F16S, BF16S, F64, F16SR, BF16SR = 0, 1, 2, 3, 4, 5
 FLAG_WRITE_MACROS, FLAG_PINGPONG, FLAG_STRICT, FLAG_SOA, FLAG_AOS = 1, 2, 4, 8, 16
 
 OK, EINVAL, ENOMEM, ECUDA, ETIMEDOUT, ESTATE, ENOTSUP = 0, -1, -2, -3, -4, -5, -6

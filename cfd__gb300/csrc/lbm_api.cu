@@ -218,9 +218,13 @@ Ops ops_for(int storage) {
     case LBM_F32: return ops_f32();
     case LBM_F64: return ops_f64();
     case LBM_F16S: return ops_f16s();
+    case LBM_F16SR: return ops_f16sr();
+    case LBM_BF16SR: return ops_bf16sr();
     default: return ops_bf16s();
   }
 }
+
+bool is_sr(int storage) { return storage == LBM_F16SR || storage == LBM_BF16SR; }
 
 Launch cell_launch(const lbm_ctx* c) {
   // The in-place step is compiled for at most 128 threads per block.
@@ -250,6 +254,7 @@ Dev dev_of(const lbm_ctx* c) {
   d.force = nullptr;
   d.blf = c->blf_on ? c->blf : nullptr;
   d.aos = c->aos ? 1 : 0;
+  d.seed = sr_seed(c->steps);
   return d;
 }
 
@@ -369,7 +374,9 @@ int lbm_create(const lbm_dims* dims, int storage, int flags, lbm_ctx** out) {
   *out = nullptr;
   if (dims->nx < 1 || dims->ny < 1 || dims->nz < 1) return fail(LBM_EINVAL, "grid dimensions must be >= 1");
   if (dims->ny > 65535 * 256 || dims->nz > 65535) return fail(LBM_EINVAL, "grid too large for the launch shape");
-  if (storage < LBM_F32 || storage > LBM_F64) return fail(LBM_EINVAL, "unknown storage form");
+  if (storage < LBM_F32 || storage > LBM_BF16SR) return fail(LBM_EINVAL, "unknown storage form");
+  if (is_sr(storage) && (flags & LBM_FLAG_PINGPONG))
+    return fail(LBM_ENOTSUP, "the stochastically rounded storage forms use the in-place set only");
   if (flags & ~(LBM_FLAG_WRITE_MACROS | LBM_FLAG_PINGPONG | LBM_FLAG_STRICT | LBM_FLAG_SOA | LBM_FLAG_AOS))
     return fail(LBM_EINVAL, "unknown flag bits");
   if ((flags & LBM_FLAG_SOA) && (flags & LBM_FLAG_AOS)) return fail(LBM_EINVAL, "LBM_FLAG_SOA and LBM_FLAG_AOS together");
@@ -382,11 +389,12 @@ int lbm_create(const lbm_dims* dims, int storage, int flags, lbm_ctx** out) {
   // AoSoA where the in-place FAST step can use it (nx a multiple of the
   // 32-cell block, fp32 arithmetic, 32-bit element offsets) and it is the
   // layout asked for, the one lbm_autotune_layout measured faster for this
-  // grid, or by default for fp32 storage (measured on GB300: faster for fp32,
-  // slower than SoA for the 16-bit forms)
+  // grid, or by default for fp32 and the stochastically rounded 16-bit forms
+  // (measured on GB300: faster for those, slower than SoA on 512x256x192 for
+  // the round-to-nearest 16-bit forms)
   const bool aos_ok = c->inplace && !(flags & LBM_FLAG_STRICT) && storage != LBM_F64 && dims->nx % 32 == 0 &&
                       (int64_t)Q * c->N < (int64_t)INT32_MAX;
-  bool want_aos = storage == LBM_F32;
+  bool want_aos = storage == LBM_F32 || is_sr(storage);   // the SR forms: AoSoA measured faster on both grids
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_layout.find(LayoutKey(dims->nx, dims->ny, dims->nz, storage, flags & ~LBM_FLAG_WRITE_MACROS));
@@ -949,7 +957,7 @@ int lbm_autotune(lbm_ctx* c, int steps, int* block_x, int* block_y, int* variant
   if (!c->aos && c->storage != LBM_F64) {
     cand.push_back({64, 1, 6, 0});
     cand.push_back({128, 1, 6, 0});
-    if (fits32)
+    if (fits32 && !is_sr(c->storage))   // the pipelined step has no stochastic rounding
       for (int kz : {4, 8, 16}) cand.push_back({64, 1, 8, kz});
   }
   // the state is saved and put back: the trials advance a copy of it

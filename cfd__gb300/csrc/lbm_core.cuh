@@ -591,6 +591,7 @@ __device__ __forceinline__ void collide(const Params& P, const Uni<R>& U, uint32
 // kScaled: the stored value is the population times kScale (a power of two);
 // ld_raw / st_raw move the stored value without the scale.
 struct StF32 {
+  static constexpr bool kSR = false;   // stores rounded to nearest
   using store_t = float;
   using real = float;
   static constexpr bool kScaled = false;
@@ -604,6 +605,7 @@ struct StF32 {
   static __device__ __forceinline__ float from_word(uint32_t w, uint32_t) { return __uint_as_float(w); }
 };
 struct StF64 {
+  static constexpr bool kSR = false;   // stores rounded to nearest
   using store_t = double;
   using real = double;
   static constexpr bool kScaled = false;
@@ -617,6 +619,7 @@ struct StF64 {
 // fp16 holding g_i * 2^10: the scale lifts the ~1e-5 free-stream deviations
 // out of the fp16 subnormal range.  Scaling by a power of two is exact.
 struct StF16S {
+  static constexpr bool kSR = false;   // stores rounded to nearest
   using store_t = uint16_t;
   using real = float;
   static constexpr bool kScaled = true;
@@ -635,6 +638,7 @@ struct StF16S {
   static __device__ __forceinline__ float from_double(double v) { return (float)v; }
 };
 struct StBF16S {
+  static constexpr bool kSR = false;   // stores rounded to nearest
   using store_t = uint16_t;
   using real = float;
   static constexpr bool kScaled = false;
@@ -651,6 +655,45 @@ struct StBF16S {
     *p = __bfloat16_as_ushort(__float2bfloat16_rn(v));
   }
   static __device__ __forceinline__ float from_double(double v) { return (float)v; }
+};
+
+// Stochastic rounding of the 16-bit stores (LBM_F16SR, LBM_BF16SR).  A
+// stored value v (fp32, in the stored scale) keeps its top bits; the dropped
+// low bits B (13 for fp16, 16 for bf16) round it up in magnitude with
+// probability B / 2^bits: r, uniform on [0, 2^bits), is added to the fp32 bit
+// pattern (sign and magnitude, so the carry goes into the magnitude for
+// either sign) and the result is truncated (round toward zero).  r comes from
+// a hash of the colliding cell, the step count and the direction, so a run is
+// reproducible and the oracle restates it bit for bit.
+__host__ __device__ __forceinline__ uint32_t sr_seed(int64_t step) {
+  return (uint32_t)((uint64_t)step * 0x632BE5ABull);
+}
+__host__ __device__ __forceinline__ uint32_t sr_cell_hash(uint32_t cell, uint32_t seed) {
+  uint32_t h = cell * 0x9E3779B1u + seed;
+  h ^= h >> 16;
+  h *= 0x7FEB352Du;
+  h ^= h >> 15;
+  h *= 0x846CA68Bu;
+  h ^= h >> 16;
+  return h;
+}
+// per direction i: an odd multiplier; r = top `bits` bits of h * sr_mult(i)
+__host__ __device__ constexpr uint32_t sr_mult(int i) { return 0x9E3779B1u * (2u * (uint32_t)i + 1u); }
+
+struct StF16SR : StF16S {
+  static constexpr bool kSR = true;
+  static constexpr int kSRBits = 13;
+  // vs: the value times 2^10 (the stored scale)
+  static __device__ __forceinline__ void st_sr(uint16_t* p, float vs, uint32_t r) {
+    *p = __half_as_ushort(__float2half_rz(__uint_as_float(__float_as_uint(vs) + r)));
+  }
+};
+struct StBF16SR : StBF16S {
+  static constexpr bool kSR = true;
+  static constexpr int kSRBits = 16;
+  static __device__ __forceinline__ void st_sr(uint16_t* p, float vs, uint32_t r) {
+    *p = __bfloat16_as_ushort(__float2bfloat16_rz(__uint_as_float(__float_as_uint(vs) + r)));
+  }
 };
 
 // ------------------------------------------------------------- link words

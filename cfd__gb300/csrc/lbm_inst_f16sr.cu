@@ -1,0 +1,7 @@
+// lbm_inst_f16sr.cu — kernel instantiation for the f16sr population storage form
+// (16-bit stores rounded stochastically).
+#include "lbm_kernels.cuh"
+
+namespace lbm {
+Ops ops_f16sr() { return OpsImpl<StF16SR>::make(); }
+}  // namespace lbm

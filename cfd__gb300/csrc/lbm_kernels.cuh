@@ -46,6 +46,7 @@ struct Dev {
   double* force;         // nullable: kForceSlots x 3 doubles accumulated by the fused force
   const void* blf;       // nullable: nz inlet boundary-layer factors in the arithmetic type
   int aos;               // in-place set in the AoSoA layout (elem_off) instead of SoA
+  uint32_t seed;         // sr_seed(step count): the stochastic rounding of the SR storage forms
 };
 
 // The in-place set's two layouts.  SoA: slot k of location c at k N + c.
@@ -150,6 +151,7 @@ struct Deltas {
 // An integer the compiler must treat as changed here (an empty asm): values
 // derived from it are formed again afterwards instead of being kept live.
 __device__ __forceinline__ void opaque(int32_t& v) { asm volatile("" : "+r"(v)); }
+__device__ __forceinline__ void opaque(uint32_t& v) { asm volatile("" : "+r"(v)); }
 __device__ __forceinline__ void opaque(int64_t& v) { asm volatile("" : "+l"(v)); }
 template <class T>
 __device__ __forceinline__ void opaque(T*& p) { asm volatile("" : "+l"(p)); }
@@ -418,11 +420,27 @@ __device__ __forceinline__ void step_cell_at(const Dev& d, const Params& P, cons
   // g*_i of an odd i goes to the neighbour's slot B; g*_{i+1} stays local in
   // slot A; the rest population stays put.
   ad.refresh();
+  // the SR storage forms round each store stochastically (sr_cell_hash)
+  uint32_t hsr = 0;
+  if constexpr (St::kSR) hsr = sr_cell_hash((uint32_t)cell, d.seed);
+  auto put = [&](S* p, R v, int i) {
+    if constexpr (St::kSR) {
+      // the hash passes through an empty asm that also reads the stored
+      // value, so each rounding offset is formed when its value exists, not
+      // all 19 at the start (which would keep them live through the collide)
+      uint32_t h = hsr;
+      const R vs = SC ? v : v * R(St::kScale);
+      asm volatile("" : "+r"(h) : "f"(vs));
+      St::st_sr(p, vs, (h * sr_mult(i)) >> (32 - St::kSRBits));
+    } else {
+      st(p, v);
+    }
+  };
   collide<R, FAST, SC>(P, U, ct, x, z, g, sp, dp, delta, rho, ux, uy, uz, uu, rinv, static_cast<const R*>(d.blf),
                        [&](int i, R v) {
-    if (i == 0) st(ad.rest(), v);
-    else if (i & 1) st(ad.b((i - 1) >> 1, true), v);
-    else st(ad.a((i - 2) >> 1, false), v);
+    if (i == 0) put(ad.rest(), v, 0);
+    else if (i & 1) put(ad.b((i - 1) >> 1, true), v, i);
+    else put(ad.a((i - 2) >> 1, false), v, i);
   }, scale, rates);
 }
 
@@ -1228,7 +1246,7 @@ struct OpsImpl {
   static void go_inplace(const Dev& d, const Params& P, const Uni<R>& U, Launch L, cudaStream_t s) {
     constexpr int kDefault = sizeof(R) == 8 ? 4 : (MAC ? 6 : 8);
     const bool w64 = (int64_t)Q * d.N >= (int64_t)INT32_MAX;
-    if constexpr (!MAC && !FRC && sizeof(typename St::store_t) <= 4) {
+    if constexpr (!MAC && !FRC && sizeof(typename St::store_t) <= 4 && !St::kSR) {
       if (L.pipe > 0 && !w64 && !d.aos) {
         const dim3 grid((d.nx + 63) / 64, d.ny, (d.nz + L.pipe - 1) / L.pipe);
         if (L.pipe == 4) k_step_pipe<St, PAR, FAST, 4, 64><<<grid, 64, 0, s>>>(d, P, U);
@@ -1288,6 +1306,7 @@ struct OpsImpl {
   static cudaError_t step(const Dev& d, const Params& P, int parity, bool inplace, bool mac, bool frc, bool fast,
                           Launch L, cudaStream_t s) {
     if (d.aos && !(fast && kFastOK && inplace)) return cudaErrorNotSupported;   // AoSoA: FAST, in-place only
+    if (St::kSR && !inplace) return cudaErrorNotSupported;                      // SR forms: in-place only
     const Uni<R> U = make_uni<R>(P, R(St::kScale));
     if (fast && kFastOK) go<kFastOK>(d, P, U, parity, inplace, mac, frc, L, s);
     else go<false>(d, P, U, parity, inplace, mac, frc, L, s);
@@ -1418,5 +1437,7 @@ Ops ops_bf16s();
 StepClosureFn closure_f32();
 StepClosureFn closure_f16s();
 StepClosureFn closure_bf16s();
+Ops ops_f16sr();
+Ops ops_bf16sr();
 
 }  // namespace lbm

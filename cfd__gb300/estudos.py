@@ -27,7 +27,7 @@ import time
 
 import numpy as np
 
-BYTES = {"f32": 152, "f16s": 76, "bf16s": 76, "f64": 304}
+BYTES = {"f32": 152, "f16s": 76, "bf16s": 76, "f64": 304, "f16sr": 76, "bf16sr": 76}
 
 
 def _peak():
@@ -94,7 +94,7 @@ def _subnormal_share(s, fluid):
     return out
 
 
-def precisao(steps=10000, grade=None, forms=("f64", "f32", "f16s", "bf16s"), sample=50):
+def precisao(steps=10000, grade=None, forms=("f64", "f32", "f16s", "bf16s", "f16sr", "bf16sr"), sample=50):
     import torch
 
     from .forces import coeficientes
@@ -132,7 +132,7 @@ def precisao(steps=10000, grade=None, forms=("f64", "f32", "f16s", "bf16s"), sam
             cds.append(coeficientes(f, units, area, grade)["cd"])
         s.atualizarMacros()
         m = s.lerMacros().reshape(-1, 4)[:, :3].astype(np.float64)[fluid]
-        sub = _subnormal_share(s, fluid) if form == "f16s" else None
+        sub = _subnormal_share(s, fluid) if form in ("f16s", "f16sr") else None
         s.destruir()
         tail = cds[len(cds) * 3 // 4:]
         cd = float(np.mean(tail))

@@ -20,7 +20,7 @@ import time
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--grid", default="512x256x192")
-    ap.add_argument("--storage", default="f32", choices=["f32", "f16s", "bf16s", "f64"])
+    ap.add_argument("--storage", default="f32", choices=["f32", "f16s", "bf16s", "f64", "f16sr", "bf16sr"])
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--closure", type=int, default=0, help="learned closure evaluated every K steps (0: off)")

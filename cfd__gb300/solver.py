@@ -22,7 +22,8 @@ from . import _native as nat
 from .lattice import MAGIC, Q
 from .lattice import equilibrium as _equilibrium
 
-STORAGE = {"f32": nat.F32, "f16s": nat.F16S, "bf16s": nat.BF16S, "f64": nat.F64}
+STORAGE = {"f32": nat.F32, "f16s": nat.F16S, "bf16s": nat.BF16S, "f64": nat.F64, "f16sr": nat.F16SR,
+           "bf16sr": nat.BF16SR}
 
 
 def js_round(v: float) -> int:
@@ -34,7 +35,8 @@ class SolverCUDA:
     """A D3Q19 TRT/LES wind tunnel on one GB300, one CUDA stream per solver."""
 
     def __init__(self, grade, storage="f32", escrever_macros=True, pingpong=False, estrito=False, soa=None):
-        """storage: "f32" | "f16s" | "bf16s" | "f64"; pingpong: the reference's
+        """storage: "f32" | "f16s" | "bf16s" | "f64" | "f16sr" | "bf16sr" (the
+        16-bit forms with stochastically rounded stores); pingpong: the reference's
         two-set A/B layout instead of the in-place one; estrito: the shader's
         arithmetic read literally (no fused multiply-add) instead of the FAST
         restatement; soa: True keeps the in-place set in the SoA layout,

@@ -67,6 +67,15 @@ extern "C" {
 #define LBM_F16S   1   /* fp16 of g_i * 2^10, fp32 arithmetic (76 B/cell/step) */
 #define LBM_BF16S  2   /* bf16 of g_i, fp32 arithmetic (76 B/cell/step) */
 #define LBM_F64    3   /* fp64 g_i and fp64 arithmetic: the accuracy reference */
+#define LBM_F16SR  4   /* as LBM_F16S, the step's stores rounded stochastically:
+                          the 13 bits fp16 drops from the fp32 value decide the
+                          rounding direction against a per-cell, per-step,
+                          per-direction hash (unbiased; reproducible: the hash
+                          depends on the cell, the step count and the
+                          direction only).  In-place set only; no learned
+                          closure; not in batches. */
+#define LBM_BF16SR 5   /* as LBM_BF16S, stores rounded stochastically (16
+                          dropped bits), same limits as LBM_F16SR */
 
 /* lbm_create flags */
 #define LBM_FLAG_WRITE_MACROS  1  /* the last step of each lbm_step writes (u, delta) */
@@ -91,8 +100,9 @@ extern "C" {
                                      lbm_autotune_layout measured faster for
                                      this grid, storage and flags earlier in
                                      the process, else AoSoA for LBM_F32 and
-                                     SoA for the 16-bit forms (the faster one
-                                     of each on GB300).  The layout is
+                                     the SR forms and SoA for LBM_F16S and
+                                     LBM_BF16S (the faster one of each on
+                                     GB300).  The layout is
                                      internal: populations in and out are
                                      always the natural layout. */
 

@@ -37,6 +37,8 @@
 #define ORC_F32 0
 #define ORC_F16S 1
 #define ORC_BF16S 2
+#define ORC_F16SR 4
+#define ORC_BF16SR 5
 
 /* Same field layout as lbm_params in include/lbm.h. */
 typedef struct {
@@ -151,6 +153,43 @@ static float orc_bf16_to_f32(uint16_t b) {
   return f;
 }
 
+/* Round toward zero (truncation) into binary16 and bfloat16: the last step
+ * of the stochastic rounding of the SR storage forms. */
+static uint16_t orc_f32_to_f16_rz(float f) {
+  uint32_t x;
+  memcpy(&x, &f, 4);
+  const uint32_t sign = (x >> 16) & 0x8000u;
+  const uint32_t ex = (x >> 23) & 0xffu;
+  uint32_t mant = x & 0x7fffffu;
+  if (ex == 0xffu) return (uint16_t)(sign | (mant ? 0x7e00u : 0x7c00u));
+  const int e = (int)ex - 127 + 15;
+  if (e >= 31) return (uint16_t)(sign | 0x7bffu);   /* toward zero: the largest finite value */
+  if (e <= 0) {
+    if (e < -10) return (uint16_t)sign;
+    mant |= 0x800000u;
+    return (uint16_t)(sign | (mant >> (14 - e)));
+  }
+  return (uint16_t)(sign | ((uint32_t)e << 10) | (mant >> 13));
+}
+
+/* Stochastic rounding of a store (the SR storage forms, cfd__gb300/csrc/lbm_core.cuh
+ * sr_seed / sr_cell_hash / sr_mult): r, the top `bits` bits of
+ * hash(cell, step) * (odd multiplier of direction i), is added to the fp32
+ * bit pattern of the value in the stored scale, which is then truncated. */
+static inline uint32_t orc_sr_seed(int64_t step) { return (uint32_t)((uint64_t)step * 0x632BE5ABull); }
+static inline uint32_t orc_sr_hash(uint32_t cell, uint32_t seed) {
+  uint32_t h = cell * 0x9E3779B1u + seed;
+  h ^= h >> 16;
+  h *= 0x7FEB352Du;
+  h ^= h >> 15;
+  h *= 0x846CA68Bu;
+  h ^= h >> 16;
+  return h;
+}
+static inline uint32_t orc_sr_bits(uint32_t h, int i, int bits) {
+  return (h * (0x9E3779B1u * (2u * (uint32_t)i + 1u))) >> (32 - bits);
+}
+
 static inline int orc_is_solid(uint32_t t) {
   return t == ORC_SOLIDO || t == ORC_SOLIDO_MOVEL || t == ORC_PAREDE;
 }
@@ -216,5 +255,9 @@ void orc_quantize_f32(float* v, int64_t n, int storage) {
 }
 
 uint16_t orc_f16_bits(float f) { return orc_f32_to_f16(f); }
+/* One stochastically rounded store of value v (unscaled) for direction i of a
+ * cell with rounding hash hsr (tests). */
+float orc_sr_store_f32(float v, int storage, uint32_t hsr, int i) { return orc_qs_f32(v, storage, hsr, i); }
+uint32_t orc_sr_cell_hash(uint32_t cell, int64_t step) { return orc_sr_hash(cell, orc_sr_seed(step)); }
 float orc_f16_value(uint16_t h) { return orc_f16_to_f32(h); }
 uint16_t orc_bf16_bits(float f) { return orc_f32_to_bf16(f); }

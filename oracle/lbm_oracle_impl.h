@@ -25,12 +25,32 @@
 /* Quantisation of stored populations (16-bit forms); identity for plain. */
 static inline REAL FN(orc_q)(REAL v, int storage) {
 #if ORC_IS_FLOAT
-  if (storage == ORC_F16S) return orc_f16_to_f32(orc_f32_to_f16(v * 1024.0f)) * (1.0f / 1024.0f);
-  if (storage == ORC_BF16S) return orc_bf16_to_f32(orc_f32_to_bf16(v));
+  if (storage == ORC_F16S || storage == ORC_F16SR) return orc_f16_to_f32(orc_f32_to_f16(v * 1024.0f)) * (1.0f / 1024.0f);
+  if (storage == ORC_BF16S || storage == ORC_BF16SR) return orc_bf16_to_f32(orc_f32_to_bf16(v));
 #else
   (void)storage;
 #endif
   return v;
+}
+
+/* Quantisation of a step's output population i of a cell whose rounding hash
+ * is hsr: stochastic for the SR forms, else orc_q. */
+static inline REAL FN(orc_qs)(REAL v, int storage, uint32_t hsr, int i) {
+#if ORC_IS_FLOAT
+  if (storage == ORC_F16SR || storage == ORC_BF16SR) {
+    const int f16 = storage == ORC_F16SR;
+    float s = f16 ? v * 1024.0f : v;
+    uint32_t x;
+    memcpy(&x, &s, 4);
+    x += orc_sr_bits(hsr, i, f16 ? 13 : 16);
+    memcpy(&s, &x, 4);
+    if (f16) return orc_f16_to_f32(orc_f32_to_f16_rz(s)) * (1.0f / 1024.0f);
+    return orc_bf16_to_f32((uint16_t)(x >> 16));
+  }
+#else
+  (void)hsr; (void)i;
+#endif
+  return FN(orc_q)(v, storage);
 }
 
 /* c_i . v in the order dotC (src/core/emit/ir.js:116-126) emits it. */
@@ -79,7 +99,9 @@ static inline void FN(orc_equilibrium_fast)(REAL delta, REAL rho, REAL ux, REAL 
  * dst untouched (src/core/emit/wgsl.js:201-204).
  */
 void FN(orc_step)(const orc_params* P, int nx, int ny, int nz, const uint32_t* tipo,
-                  const REAL* src, REAL* dst, float* macros, int storage, int nthreads, int fast_in) {
+                  const REAL* src, REAL* dst, float* macros, int storage, int nthreads, int fast_in,
+                  int64_t step) {
+  const uint32_t sr_seed = orc_sr_seed(step);   /* SR storage forms: the step's rounding seed */
   /* FAST restatement: fixed fused multiply-adds (ORC_FMA), u = m (1/rho),
    * omega- = (tau - 1/2) / (Lambda + (tau - 1/2)/2).  The fp64 reference form is
    * always STRICT. */
@@ -98,6 +120,7 @@ void FN(orc_step)(const orc_params* P, int nx, int ny, int nz, const uint32_t* t
     for (int y = 0; y < ny; ++y) {
       for (int x = 0; x < nx; ++x) {
         const int64_t cell = ((int64_t)z * ny + y) * nx + x;
+        const uint32_t hsr = orc_sr_hash((uint32_t)cell, sr_seed);
         const uint32_t ct = tipo[cell];
         if (orc_is_solid(ct)) {
           if (macros) { macros[4 * cell] = 0; macros[4 * cell + 1] = 0; macros[4 * cell + 2] = 0; macros[4 * cell + 3] = 0; }
@@ -192,37 +215,37 @@ void FN(orc_step)(const orc_params* P, int nx, int ny, int nz, const uint32_t* t
           /* blocoEspelho (src/core/emit/ir.js:383-390) */
           const int ax = ct == ORC_ESPELHO_Y ? 1 : 2;
           ORC_UNROLL
-          for (int i = 0; i < ORC_Q; ++i) *out[i] = FN(orc_q)(g[ORC_MIRROR[ax][i]], storage);
+          for (int i = 0; i < ORC_Q; ++i) *out[i] = FN(orc_qs)(g[ORC_MIRROR[ax][i]], storage, hsr, i);
         } else if (ct == ORC_ENTRADA && fast) {
           const REAL uuIn = ORC_FMA(uez, uez, ORC_FMA(uey, uey, uex * uex));
           const REAL uuIn15 = LIT(1.5) * uuIn;
           REAL e[ORC_Q];
           FN(orc_equilibrium_fast)(LIT(0.0), LIT(1.0), uex, uey, uez, uuIn15, e);
-          for (int i = 0; i < ORC_Q; ++i) *out[i] = FN(orc_q)(e[i], storage);
+          for (int i = 0; i < ORC_Q; ++i) *out[i] = FN(orc_qs)(e[i], storage, hsr, i);
         } else if (ct == ORC_ENTRADA) {
           /* blocoEntrada (src/core/emit/ir.js:405-422) */
           const REAL deltaIn = LIT(0.0), rhoIn = LIT(1.0);
           const REAL uuIn = uex * uex + uey * uey + uez * uez;
-          *out[0] = FN(orc_q)(FN(W_)[0] * (deltaIn - LIT(1.5) * rhoIn * uuIn), storage);
+          *out[0] = FN(orc_qs)(FN(W_)[0] * (deltaIn - LIT(1.5) * rhoIn * uuIn), storage, hsr, 0);
           ORC_UNROLL
           for (int i = 1; i < ORC_Q; ++i) {
             const REAL ci = FN(orc_dotc)(i, uex, uey, uez);
-            *out[i] = FN(orc_q)(FN(W_)[i] * (deltaIn + rhoIn * (LIT(3.0) * ci + LIT(4.5) * ci * ci - LIT(1.5) * uuIn)), storage);
+            *out[i] = FN(orc_qs)(FN(W_)[i] * (deltaIn + rhoIn * (LIT(3.0) * ci + LIT(4.5) * ci * ci - LIT(1.5) * uuIn)), storage, hsr, i);
           }
         } else if (ct == ORC_SAIDA && fast) {
-          *out[0] = FN(orc_q)(FN(W_)[0] * (-uu15), storage);
+          *out[0] = FN(orc_qs)(FN(W_)[0] * (-uu15), storage, hsr, 0);
           ORC_UNROLL
           for (int i = 1; i < ORC_Q; ++i) {
             const REAL cu = FN(orc_dotc)(i, ux, uy, uz);
-            *out[i] = FN(orc_q)(FN(W_)[i] * ORC_FMA(cu, ORC_FMA(LIT(4.5), cu, LIT(3.0)), -uu15), storage);
+            *out[i] = FN(orc_qs)(FN(W_)[i] * ORC_FMA(cu, ORC_FMA(LIT(4.5), cu, LIT(3.0)), -uu15), storage, hsr, i);
           }
         } else if (ct == ORC_SAIDA) {
           /* blocoSaida with the pulled u (src/core/emit/ir.js:432-444, :512-515) */
-          *out[0] = FN(orc_q)(FN(W_)[0] * (LIT(-1.5) * uu), storage);
+          *out[0] = FN(orc_qs)(FN(W_)[0] * (LIT(-1.5) * uu), storage, hsr, 0);
           ORC_UNROLL
           for (int i = 1; i < ORC_Q; ++i) {
             const REAL cu = FN(orc_dotc)(i, ux, uy, uz);
-            *out[i] = FN(orc_q)(FN(W_)[i] * (LIT(3.0) * cu + LIT(4.5) * cu * cu - LIT(1.5) * uu), storage);
+            *out[i] = FN(orc_qs)(FN(W_)[i] * (LIT(3.0) * cu + LIT(4.5) * cu * cu - LIT(1.5) * uu), storage, hsr, i);
           }
         } else if (fast) {
           /* FLUIDO, FAST pair form: e_i + e_j = 2w (delta + rho (4.5 cu^2 - 1.5 uu)),
@@ -296,7 +319,7 @@ void FN(orc_step)(const orc_params* P, int nx, int ny, int nz, const uint32_t* t
             }
           }
           ORC_UNROLL
-          for (int i = 0; i < ORC_Q; ++i) *out[i] = FN(orc_q)(o[i], storage);
+          for (int i = 0; i < ORC_Q; ++i) *out[i] = FN(orc_qs)(o[i], storage, hsr, i);
         } else {
           /* FLUIDO: blocoEquilibrio, blocoLES, blocoColisao, blocoEsponja */
           REAL e[ORC_Q];
@@ -394,7 +417,7 @@ void FN(orc_step)(const orc_params* P, int nx, int ny, int nz, const uint32_t* t
             }
           }
           ORC_UNROLL
-          for (int i = 0; i < ORC_Q; ++i) *out[i] = FN(orc_q)(o[i], storage);
+          for (int i = 0; i < ORC_Q; ++i) *out[i] = FN(orc_qs)(o[i], storage, hsr, i);
         }
         if (macros) {
           macros[4 * cell] = (float)ux; macros[4 * cell + 1] = (float)uy;
@@ -563,14 +586,15 @@ double FN(orc_mass)(int nx, int ny, int nz, const uint32_t* tipo, const REAL* po
   return s;
 }
 
-/* n steps with ping-pong; returns 0 when the state ends in a, 1 in b. */
+/* n steps with ping-pong (numbered from step0: the SR forms' seeds); returns
+ * 0 when the state ends in a, 1 in b. */
 int FN(orc_run)(const orc_params* P, int nx, int ny, int nz, const uint32_t* tipo, REAL* a, REAL* b,
-                int nsteps, int storage, int nthreads, int fast) {
+                int nsteps, int storage, int nthreads, int fast, int64_t step0) {
   REAL* s = a;
   REAL* d = b;
   ORC_UNROLL
   for (int k = 0; k < nsteps; ++k) {
-    FN(orc_step)(P, nx, ny, nz, tipo, s, d, NULL, storage, nthreads, fast);
+    FN(orc_step)(P, nx, ny, nz, tipo, s, d, NULL, storage, nthreads, fast, step0 + k);
     REAL* t = s; s = d; d = t;
   }
   return s == a ? 0 : 1;

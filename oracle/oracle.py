@@ -29,7 +29,7 @@ _LIB_PATH = os.path.join(_HERE, "_build", "liborc.so")
 _lock = threading.Lock()
 _lib = None
 
-F32, F16S, BF16S = 0, 1, 2
+F32, F16S, BF16S, F16SR, BF16SR = 0, 1, 2, 4, 5
 
 
 class OrcParams(C.Structure):
@@ -71,14 +71,16 @@ def lib():
             P = C.POINTER
             vp = C.c_void_p
             for sfx in ("f32", "f64"):
-                getattr(L, f"orc_step_{sfx}").argtypes = [P(OrcParams), C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, C.c_int, C.c_int, C.c_int]
+                getattr(L, f"orc_step_{sfx}").argtypes = [P(OrcParams), C.c_int, C.c_int, C.c_int, vp, vp, vp, vp, C.c_int, C.c_int, C.c_int,
+                                                          C.c_int64]
                 getattr(L, f"orc_init_{sfx}").argtypes = [P(OrcParams), C.c_int, C.c_int, C.c_int, vp, vp, C.c_int]
                 getattr(L, f"orc_macros_{sfx}").argtypes = [C.c_int, C.c_int, C.c_int, vp, vp, vp, C.c_int]
                 getattr(L, f"orc_forces_acc64_{sfx}").argtypes = [C.c_int, C.c_int, C.c_int, vp, vp, vp]
                 getattr(L, f"orc_forces_faithful_{sfx}").argtypes = [C.c_int, C.c_int, C.c_int, vp, vp, vp]
                 getattr(L, f"orc_mass_{sfx}").argtypes = [C.c_int, C.c_int, C.c_int, vp, vp]
                 getattr(L, f"orc_mass_{sfx}").restype = C.c_double
-                getattr(L, f"orc_run_{sfx}").argtypes = [P(OrcParams), C.c_int, C.c_int, C.c_int, vp, vp, vp, C.c_int, C.c_int, C.c_int, C.c_int]
+                getattr(L, f"orc_run_{sfx}").argtypes = [P(OrcParams), C.c_int, C.c_int, C.c_int, vp, vp, vp, C.c_int, C.c_int, C.c_int, C.c_int,
+                                                         C.c_int64]
                 getattr(L, f"orc_run_{sfx}").restype = C.c_int
             L.orc_tables_out.argtypes = [vp] * 6
             L.orc_quantize_f32.argtypes = [vp, C.c_int64, C.c_int]
@@ -88,6 +90,10 @@ def lib():
             L.orc_f16_value.restype = C.c_float
             L.orc_bf16_bits.argtypes = [C.c_float]
             L.orc_bf16_bits.restype = C.c_uint16
+            L.orc_sr_store_f32.argtypes = [C.c_float, C.c_int, C.c_uint32, C.c_int]
+            L.orc_sr_store_f32.restype = C.c_float
+            L.orc_sr_cell_hash.argtypes = [C.c_uint32, C.c_int64]
+            L.orc_sr_cell_hash.restype = C.c_uint32
             L.orc_voxelize.argtypes = [vp, C.c_int64, vp, C.c_int64, C.c_int, C.c_int, C.c_int, C.c_double, C.c_int, vp, vp, P(OrcVoxStats)]
             L.orc_rasterize.argtypes = [vp, vp, C.c_int64, C.c_int, C.c_int, C.c_int, C.c_double, vp, vp]
             L.orc_rasterize.restype = C.c_int64
@@ -145,6 +151,7 @@ class Lattice:
         self.tipo = np.zeros(self.N, np.uint32)
         self.macros = np.zeros(4 * self.N, np.float32)
         self.p = params(1.0)
+        self.steps = 0          # step count (the SR storage forms' rounding seeds); 0 after init / set
 
     def set_types(self, tipo):
         self.tipo = np.ascontiguousarray(tipo, dtype=np.uint32).reshape(-1)
@@ -156,27 +163,33 @@ class Lattice:
     def init(self):
         getattr(lib(), f"orc_init_{self.sfx}")(C.byref(self.p), self.nx, self.ny, self.nz,
                                                _ptr(self.tipo), _ptr(self.a), self.storage)
+        self.steps = 0
 
     def set_populations(self, g):
         g = np.asarray(g, np.float64).reshape(-1)
         self.a[:] = g.astype(self.dtype)
         if self.dtype == np.float32 and self.storage != F32:
             lib().orc_quantize_f32(_ptr(self.a), self.a.size, self.storage)
+        self.steps = 0
 
     def step(self, n=1, macros=False):
         L = lib()
         for k in range(n):
             m = _ptr(self.macros) if (macros and k == n - 1) else None
             getattr(L, f"orc_step_{self.sfx}")(C.byref(self.p), self.nx, self.ny, self.nz, _ptr(self.tipo),
-                                               _ptr(self.a), _ptr(self.b), m, self.storage, self.nthreads, self.fast)
+                                               _ptr(self.a), _ptr(self.b), m, self.storage, self.nthreads, self.fast,
+                                               self.steps)
             self.a, self.b = self.b, self.a
+            self.steps += 1
 
     def run(self, n):
         """n steps in C without returning to Python between steps."""
         which = getattr(lib(), f"orc_run_{self.sfx}")(C.byref(self.p), self.nx, self.ny, self.nz, _ptr(self.tipo),
-                                                     _ptr(self.a), _ptr(self.b), n, self.storage, self.nthreads, self.fast)
+                                                     _ptr(self.a), _ptr(self.b), n, self.storage, self.nthreads, self.fast,
+                                                     self.steps)
         if which == 1:
             self.a, self.b = self.b, self.a
+        self.steps += n
 
     def populations(self):
         return self.a.astype(np.float64)
