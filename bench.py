@@ -528,6 +528,15 @@ def run_ours(args):
                                       "traffic": ncu_traffic(st, args.grid), "algorithmic_bytes_per_cell": 76}}
             s2.destruir()
         forms["precision_study"] = precision_study(args.grid)
+        # the metric's comparison in one place: each 16-bit store form's speed
+        # against the fp32 step (this run) and its recorded Cd error vs fp64
+        ps = (forms["precision_study"] or {}).get("forms", {})
+        cmp16 = {}
+        for st in ("f16s", "bf16s", "f16sr", "bf16sr"):
+            e = ps.get(st, {}).get("cd_err_vs_f64")
+            cmp16[st] = {"MLUPS": forms[st]["MLUPS"], "vs_f32": forms[st]["vs_f32"], "cd_err_vs_f64": e,
+                         "meets_1pct_cd": None if e is None else abs(e) <= 0.01}
+        forms["fp16_store_vs_fp32"] = cmp16
         # the step kernel's addressing variants side by side (lbm_set_launch
         # codes) in each storage form's default layout: AoSoA for fp32 (where
         # nx is a multiple of 32), SoA for the 16-bit forms
