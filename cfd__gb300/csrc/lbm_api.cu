@@ -146,6 +146,7 @@ struct lbm_ctx {
   int flags = 0;
   bool inplace = true;
   bool aos = false;       // in-place set in the AoSoA layout (lbm_kernels.cuh, elem_off)
+  int aos_b = 32;         // its block width (cells along x)
   Ops ops{};
   void* pop = nullptr;    // in-place set, or ping-pong front
   void* pop2 = nullptr;   // ping-pong back
@@ -244,6 +245,15 @@ Launch cell_launch(const lbm_ctx* c) {
   return L;
 }
 
+// Population set layout as reported by lbm_get_info and stored in a
+// checkpoint: 0 in-place SoA, 1 ping-pong, 2 in-place AoSoA in blocks of 32
+// cells, 3 in blocks of 64.
+int layout_code(const lbm_ctx* c) {
+  if (!c->inplace) return 1;
+  if (!c->aos) return 0;
+  return c->aos_b == 64 ? 3 : 2;
+}
+
 Dev dev_of(const lbm_ctx* c) {
   Dev d;
   d.nx = c->dims.nx; d.ny = c->dims.ny; d.nz = c->dims.nz;
@@ -253,7 +263,7 @@ Dev dev_of(const lbm_ctx* c) {
   d.macros = c->macros;
   d.force = nullptr;
   d.blf = c->blf_on ? c->blf : nullptr;
-  d.aos = c->aos ? 1 : 0;
+  d.aos = c->aos ? c->aos_b : 0;
   d.seed = sr_seed(c->steps);
   return d;
 }
@@ -389,12 +399,15 @@ int lbm_create(const lbm_dims* dims, int storage, int flags, lbm_ctx** out) {
   // AoSoA where the in-place FAST step can use it (nx a multiple of the
   // 32-cell block, fp32 arithmetic, 32-bit element offsets) and it is the
   // layout asked for, the one lbm_autotune_layout measured faster for this
-  // grid, or by default for fp32 and the stochastically rounded 16-bit forms
-  // (measured on GB300: faster for those, slower than SoA on 512x256x192 for
-  // the round-to-nearest 16-bit forms)
+  // grid, or by default for fp32, for the stochastically rounded 16-bit forms
+  // and for every 16-bit form whose nx allows blocks of 64 cells (measured on
+  // GB300: with blocks of 32 cells the round-to-nearest 16-bit forms ran
+  // slower than SoA on most grids, with 64 faster)
   const bool aos_ok = c->inplace && !(flags & LBM_FLAG_STRICT) && storage != LBM_F64 && dims->nx % 32 == 0 &&
                       (int64_t)Q * c->N < (int64_t)INT32_MAX;
-  bool want_aos = storage == LBM_F32 || is_sr(storage);   // the SR forms: AoSoA measured faster on both grids
+  // 16-bit forms: blocks of 64 cells (one 128-byte line per slot row)
+  const bool is16 = storage != LBM_F32 && storage != LBM_F64;
+  bool want_aos = storage == LBM_F32 || is_sr(storage) || (is16 && dims->nx % 64 == 0);
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_layout.find(LayoutKey(dims->nx, dims->ny, dims->nz, storage, flags & ~LBM_FLAG_WRITE_MACROS));
@@ -403,6 +416,7 @@ int lbm_create(const lbm_dims* dims, int storage, int flags, lbm_ctx** out) {
   if (flags & LBM_FLAG_AOS) want_aos = true;
   if (flags & LBM_FLAG_SOA) want_aos = false;
   c->aos = aos_ok && want_aos;
+  c->aos_b = (c->aos && is16 && dims->nx % 64 == 0) ? 64 : 32;
   c->ops = ops_for(storage);
   const size_t set_bytes = (size_t)c->N * Q * c->ops.elem_bytes;
   int r = dalloc(c, &c->pop, set_bytes, "populations");
@@ -739,7 +753,7 @@ int lbm_save_state(lbm_ctx* c, void* dst, size_t bytes) {
   h.version = LBM_STATE_VERSION;
   h.nx = c->dims.nx; h.ny = c->dims.ny; h.nz = c->dims.nz;
   h.storage = c->storage;
-  h.layout = c->inplace ? (c->aos ? 2 : 0) : 1;
+  h.layout = layout_code(c);
   h.parity = parity(c);
   h.steps = c->steps;
   h.payload_bytes = need - sizeof h;
@@ -761,7 +775,7 @@ int lbm_load_state(lbm_ctx* c, const void* src, size_t bytes) {
   if (h.nx != c->dims.nx || h.ny != c->dims.ny || h.nz != c->dims.nz)
     return fail(LBM_EINVAL, "checkpoint grid differs from the context's");
   if (h.storage != c->storage) return fail(LBM_EINVAL, "checkpoint storage form differs from the context's");
-  if (h.layout != (c->inplace ? (c->aos ? 2 : 0) : 1))
+  if (h.layout != layout_code(c))
     return fail(LBM_EINVAL, "checkpoint layout differs from the context's");
   if (h.payload_bytes + sizeof h != need || bytes < need) return fail(LBM_EINVAL, "checkpoint size does not match");
   if (c->inplace && h.parity != (int)(h.steps & 1)) return fail(LBM_EINVAL, "checkpoint parity and step count disagree");
@@ -912,7 +926,7 @@ int lbm_get_info(lbm_ctx* c, lbm_info* info) {
   info->steps = c->steps;
   info->parity = (int)(c->steps & 1);
   info->block_x = (int)cell_launch(c).block.x;
-  info->layout = c->inplace ? (c->aos ? 2 : 0) : 1;
+  info->layout = layout_code(c);
   return LBM_OK;
 }
 
@@ -1019,7 +1033,7 @@ int lbm_autotune_layout(const lbm_dims* dims, int storage, int flags, int steps,
     lbm_ctx* c = nullptr;
     int r = lbm_create(dims, storage, flags | (q == 0 ? LBM_FLAG_AOS : LBM_FLAG_SOA), &c);
     if (r) return r;
-    lay[q] = c->inplace ? (c->aos ? 2 : 0) : 1;
+    lay[q] = layout_code(c);
     lbm_params p{};
     p.omega_plus = 1.9f; p.magic = 0.1875f; p.les_cs = 0.1f;
     p.inlet_u[0] = 0.05f;
@@ -1045,13 +1059,14 @@ int lbm_autotune_layout(const lbm_dims* dims, int storage, int flags, int steps,
     if (e != cudaSuccess) return cuda_fail(e, "layout tuner");
     ms[q] /= (float)steps;
   }
-  const bool aos = lay[0] == 2 && ms[0] < ms[1];
+  const bool aos_applies = lay[0] == 2 || lay[0] == 3;
+  const bool aos = aos_applies && ms[0] < ms[1];
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     g_layout[LayoutKey(dims->nx, dims->ny, dims->nz, storage, flags)] = aos;
   }
-  *layout = aos ? 2 : lay[1];
-  if (ms_aos) *ms_aos = lay[0] == 2 ? ms[0] : -1.f;
+  *layout = aos ? lay[0] : lay[1];
+  if (ms_aos) *ms_aos = aos_applies ? ms[0] : -1.f;
   if (ms_soa) *ms_soa = ms[1];
   return LBM_OK;
 }

@@ -61,7 +61,8 @@ struct BatchArgs {
 };
 static_assert(sizeof(BatchArgs) < 32000, "kernel parameter space");
 
-template <class St, int PAR, bool FAST, int MINB, bool AOS>
+// AB: the launch's AoSoA block width (0: its tunnels are SoA).
+template <class St, int PAR, bool FAST, int MINB, int AB>
 __global__ void __launch_bounds__(kTile, MINB) k_batch_step(const __grid_constant__ BatchArgs A) {
   // A tile's tunnel is found by a search over the launch's first-tile
   // prefix: the index is the same for the whole CTA, so the search and the
@@ -84,9 +85,9 @@ __global__ void __launch_bounds__(kTile, MINB) k_batch_step(const __grid_constan
     const int z = w.w;
     if (x < D.d.nx && y < D.d.ny) {
       const int32_t cell = (z * D.d.ny + y) * D.d.nx + x;
-      if constexpr (AOS && FAST)
+      if constexpr (AB != 0 && FAST)
         step_cell_at<St, PAR, false, false, false, FAST>(D.d, D.P, D.U, x, y, z, cell,
-                                                         AddrAos<St, PAR, int32_t>(D.d, cell, x, y, z));
+                                                         AddrAos<St, PAR, int32_t, true, AB>(D.d, cell, x, y, z));
       else
         step_cell<St, PAR, false, false, false, FAST>(D.d, D.P, D.U, x, y, z);
     }
@@ -263,12 +264,15 @@ int sync_desc(lbm_batch* b) {
 
 template <class St, bool FAST, int MINB>
 void launch_batch_m(lbm_batch* b, const BatchArgs& A, int parity, int grid) {
-  if (A.aos) {
-    if (parity == 0) k_batch_step<St, 0, FAST, MINB, true><<<grid, kTile, 0, b->stream>>>(A);
-    else k_batch_step<St, 1, FAST, MINB, true><<<grid, kTile, 0, b->stream>>>(A);
+  if (A.aos == 64) {
+    if (parity == 0) k_batch_step<St, 0, FAST, MINB, 64><<<grid, kTile, 0, b->stream>>>(A);
+    else k_batch_step<St, 1, FAST, MINB, 64><<<grid, kTile, 0, b->stream>>>(A);
+  } else if (A.aos) {
+    if (parity == 0) k_batch_step<St, 0, FAST, MINB, 32><<<grid, kTile, 0, b->stream>>>(A);
+    else k_batch_step<St, 1, FAST, MINB, 32><<<grid, kTile, 0, b->stream>>>(A);
   } else {
-    if (parity == 0) k_batch_step<St, 0, FAST, MINB, false><<<grid, kTile, 0, b->stream>>>(A);
-    else k_batch_step<St, 1, FAST, MINB, false><<<grid, kTile, 0, b->stream>>>(A);
+    if (parity == 0) k_batch_step<St, 0, FAST, MINB, 0><<<grid, kTile, 0, b->stream>>>(A);
+    else k_batch_step<St, 1, FAST, MINB, 0><<<grid, kTile, 0, b->stream>>>(A);
   }
 }
 
@@ -364,7 +368,9 @@ int lbm_batch_create(const lbm_dims* dims, int ntunnels, int storage, int flags,
     TunnelDesc& D = b->host[k];
     memset(&D, 0, sizeof D);
     D.d.nx = d.nx; D.d.ny = d.ny; D.d.nz = d.nz; D.d.N = N;
-    D.d.aos = (b->fast && d.nx % kAosB == 0) ? 1 : 0;   // the AoSoA layout where the FAST step can use it
+    // the AoSoA layout where the FAST step can use it: blocks of 64 cells for
+    // the 16-bit forms where nx allows, else 32
+    D.d.aos = !b->fast ? 0 : (storage != LBM_F32 && d.nx % 64 == 0) ? 64 : (d.nx % kAosB == 0 ? kAosB : 0);
     void* p = nullptr;
     const size_t sb = (size_t)N * Q * b->ops.elem_bytes;
     if ((r = balloc(b, &p, sb, "populations"))) break;

@@ -57,9 +57,12 @@ struct Dev {
 // covers 32 consecutive elements, and every slot of a location is a
 // constant offset (32 k elements) from the location's slot 0.
 constexpr int kAosB = 32;
-__host__ __device__ __forceinline__ int64_t aos_base(int64_t c) { return (c & ~(int64_t)(kAosB - 1)) * 19 + (c & (kAosB - 1)); }
+__host__ __device__ __forceinline__ int64_t aos_base(int64_t c, int B = kAosB) {
+  return (c & ~(int64_t)(B - 1)) * 19 + (c & (B - 1));
+}
+// d.aos: 0 (SoA) or the AoSoA block width
 __device__ __forceinline__ int64_t elem_off(const Dev& d, int k, int64_t c) {
-  return d.aos ? aos_base(c) + (int64_t)kAosB * k : (int64_t)k * d.N + c;
+  return d.aos ? aos_base(c, d.aos) + (int64_t)d.aos * k : (int64_t)k * d.N + c;
 }
 
 struct Wrap {
@@ -262,13 +265,15 @@ struct AddrOffs {
 // a y or z displacement is a whole number of blocks, so it is 19 times the
 // cell displacement; +1 in x is +1 inside a block, the next block's lane 0
 // (19 * 32 - 31) from lane 31, and the row's first block from x = nx - 1.
-template <class Off>
+template <class Off, int B = kAosB>
 struct DeltasAos {
   Off xp, yp, ym, zp, zm;
-  __device__ __forceinline__ DeltasAos(int x, int y, int z, int nx, int ny, int nz) {
+  // bw: the block width when B = 0 (chosen at run time)
+  __device__ __forceinline__ DeltasAos(int x, int y, int z, int nx, int ny, int nz, int bw = B) {
     const Deltas<Off> D(x, y, z, nx, ny, nz);
-    constexpr Off next = (Off)(19 * kAosB - (kAosB - 1));
-    xp = (x & (kAosB - 1)) != kAosB - 1 ? (Off)1 : (x == nx - 1 ? next - (Off)19 * (Off)nx : next);
+    const int W = B ? B : bw;
+    const Off next = (Off)(19 * W - (W - 1));
+    xp = (x & (W - 1)) != W - 1 ? (Off)1 : (x == nx - 1 ? next - (Off)19 * (Off)nx : next);
     yp = (Off)19 * D.yp;
     ym = (Off)19 * D.ym;
     zp = (Off)19 * D.zp;
@@ -294,23 +299,23 @@ struct DeltasAos {
 // state opaque to the compiler before the collide, so that the store
 // addresses are formed again instead of being kept in registers since the
 // loads (fewer live registers, more instructions); the tuner picks.
-template <class St, int PAR, class Off, bool RF = true>
+template <class St, int PAR, class Off, bool RF = true, int B = kAosB>
 struct AddrAos {
   using S = typename St::store_t;
   S* F;
   Off ob;
-  DeltasAos<Off> D;
+  DeltasAos<Off, B> D;
   __device__ __forceinline__ AddrAos(const Dev& d, Off cell, int x, int y, int z)
-      : F(static_cast<S*>(d.pop)), ob((Off)aos_base(cell)), D(x, y, z, d.nx, d.ny, d.nz) {}
+      : F(static_cast<S*>(d.pop)), ob((Off)aos_base(cell, B)), D(x, y, z, d.nx, d.ny, d.nz) {}
   __device__ __forceinline__ void refresh() {
     if constexpr (RF) { opaque(ob); opaque(D.xp); opaque(D.yp); opaque(D.ym); opaque(D.zp); opaque(D.zm); }
   }
   __device__ __forceinline__ S* rest() const { return F + ob; }
   __device__ __forceinline__ S* a(int k, bool nb) const {
-    return (F + (nb ? ob + D.odd(2 * k + 1) : ob)) + kAosB * slot_a(k, PAR);
+    return (F + (nb ? ob + D.odd(2 * k + 1) : ob)) + B * slot_a(k, PAR);
   }
   __device__ __forceinline__ S* b(int k, bool nb) const {
-    return (F + (nb ? ob + D.odd(2 * k + 1) : ob)) + kAosB * slot_b(k, PAR);
+    return (F + (nb ? ob + D.odd(2 * k + 1) : ob)) + B * slot_b(k, PAR);
   }
 };
 
@@ -322,14 +327,14 @@ struct AddrRt {
   using S = typename St::store_t;
   S* F;
   Off N, own;
-  bool aos;
+  int bw;   // AoSoA block width, 0 for SoA
   Deltas<Off> D;
-  DeltasAos<Off> DA;
+  DeltasAos<Off, 0> DA;
   __device__ __forceinline__ AddrRt(const Dev& d, Off cell, int x, int y, int z)
-      : F(static_cast<S*>(d.pop)), N((Off)d.N), own(d.aos ? (Off)aos_base(cell) : cell), aos(d.aos != 0),
-        D(x, y, z, d.nx, d.ny, d.nz), DA(x, y, z, d.nx, d.ny, d.nz) {}
+      : F(static_cast<S*>(d.pop)), N((Off)d.N), own(d.aos ? (Off)aos_base(cell, d.aos) : cell), bw(d.aos),
+        D(x, y, z, d.nx, d.ny, d.nz), DA(x, y, z, d.nx, d.ny, d.nz, d.aos ? d.aos : kAosB) {}
   __device__ __forceinline__ Off at(int slot, int k, bool nb) const {
-    if (aos) return (nb ? own + DA.odd(2 * k + 1) : own) + (Off)(kAosB * slot);
+    if (bw) return (nb ? own + DA.odd(2 * k + 1) : own) + (Off)(bw * slot);
     return (nb ? own + D.odd(2 * k + 1) : own) + (Off)slot * N;
   }
   __device__ __forceinline__ S* rest() const { return F + own; }
@@ -463,7 +468,7 @@ __device__ __forceinline__ void step_cell(const Dev& d, const Params& P, const U
 // offsets (AddrOffs), 2 one base and slot x N (AddrSet); 1 and 2 need
 // 19 N < 2^31.
 template <class St, int PAR, bool MAC, bool FRC, bool W64, bool FAST, int MINB, bool AOS = false, bool RF = true,
-          int SOAV = 0>
+          int SOAV = 0, int AB = kAosB>
 __global__ void __launch_bounds__(128, MINB)
 k_step_inplace(Dev d, Params P, Uni<typename St::real> U, SlotPtrs T) {
   using Off = typename OffT<W64>::type;
@@ -474,7 +479,7 @@ k_step_inplace(Dev d, Params P, Uni<typename St::real> U, SlotPtrs T) {
     const Off cell = ((Off)z * d.ny + y) * d.nx + x;
     if constexpr (AOS)
       step_cell_at<St, PAR, MAC, FRC, W64, FAST>(d, P, U, x, y, z, cell,
-                                                 AddrAos<St, PAR, Off, RF>(d, cell, x, y, z));
+                                                 AddrAos<St, PAR, Off, RF, AB>(d, cell, x, y, z));
     else if constexpr (SOAV == 1 && !W64)
       step_cell_at<St, PAR, MAC, FRC, W64, FAST>(d, P, U, x, y, z, cell, AddrOffs<St, PAR>(d, T, cell, x, y, z));
     else if constexpr (SOAV == 2 && !W64)
@@ -701,7 +706,8 @@ struct HeldRates {
 
 // A held closure step: the plain in-place step's cell code and addressing
 // (either layout), with HeldRates for FLUIDO cells.
-template <class St, int PAR, bool MAC, bool FRC, bool AOS>
+// AB: the AoSoA block width, 0 for the SoA layout.
+template <class St, int PAR, bool MAC, bool FRC, int AB>
 __global__ void __launch_bounds__(128, 8) k_step_held(Dev d, Params P, Uni<typename St::real> U, SlotPtrs T,
                                                       const float* __restrict__ nu, int coef) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -710,9 +716,9 @@ __global__ void __launch_bounds__(128, 8) k_step_held(Dev d, Params P, Uni<typen
   if (x < d.nx && y < d.ny) {
     const int32_t cell = (z * d.ny + y) * d.nx + x;
     const HeldRates rates{__ldg(nu + cell), coef};
-    if constexpr (AOS)
-      step_cell_at<St, PAR, MAC, FRC, false, true>(d, P, U, x, y, z, cell, AddrAos<St, PAR, int32_t>(d, cell, x, y, z),
-                                                   rates);
+    if constexpr (AB != 0)
+      step_cell_at<St, PAR, MAC, FRC, false, true>(d, P, U, x, y, z, cell,
+                                                   AddrAos<St, PAR, int32_t, true, AB>(d, cell, x, y, z), rates);
     else
       step_cell_at<St, PAR, MAC, FRC, false, true>(d, P, U, x, y, z, cell,
                                                    AddrSlots<St, PAR, int32_t>(d, T, cell, x, y, z), rates);
@@ -720,7 +726,7 @@ __global__ void __launch_bounds__(128, 8) k_step_held(Dev d, Params P, Uni<typen
 }
 
 constexpr int kClosureTcPerSm = 6;
-template <class St, int PAR, bool MAC, bool FRC, bool W64, int MODE, bool AOS>
+template <class St, int PAR, bool MAC, bool FRC, bool W64, int MODE, int AB>
 __global__ void __launch_bounds__(128, kClosureTcPerSm)
 k_step_closure_tc(Dev d, Params P, Uni<float> U, CloArgs A, SlotPtrs T, int gx, int gy) {
   using R = float;
@@ -747,9 +753,10 @@ k_step_closure_tc(Dev d, Params P, Uni<float> U, CloArgs A, SlotPtrs T, int gx, 
     // addressing of the context's layout (32-bit offsets), or either layout
     // chosen at run time for sets past 2^31 elements
     using Ad = std::conditional_t<W64, AddrRt<St, PAR, Off>,
-                                  std::conditional_t<AOS, AddrAos<St, PAR, Off>, AddrSlots<St, PAR, Off>>>;
+                                  std::conditional_t<AB != 0, AddrAos<St, PAR, Off, true, AB ? AB : kAosB>,
+                                                     AddrSlots<St, PAR, Off>>>;
     const Ad ad = [&]() {
-      if constexpr (W64 || AOS) return Ad(d, cell, inr ? x : 0, inr ? y : 0, z);
+      if constexpr (W64 || AB != 0) return Ad(d, cell, inr ? x : 0, inr ? y : 0, z);
       else return Ad(d, T, cell, inr ? x : 0, inr ? y : 0, z);
     }();
     auto emit = [&](int i, R v) {
@@ -1259,6 +1266,13 @@ struct OpsImpl {
     if (d.aos) {
       if constexpr (FAST && sizeof(R) == 4) {
         // variant 9: store addresses kept in registers from the loads
+        if (d.aos == 64) {
+          if (!MAC && !FRC && L.occ == 9)
+            k_step_inplace<St, PAR, MAC, FRC, false, FAST, kDefault, true, false, 0, 64><<<L.grid, L.block, 0, s>>>(d, P, U, T);
+          else
+            k_step_inplace<St, PAR, MAC, FRC, false, FAST, kDefault, true, true, 0, 64><<<L.grid, L.block, 0, s>>>(d, P, U, T);
+          return;
+        }
         if (!MAC && !FRC && L.occ == 9)
           k_step_inplace<St, PAR, MAC, FRC, false, FAST, kDefault, true, false><<<L.grid, L.block, 0, s>>>(d, P, U, T);
         else
@@ -1347,8 +1361,9 @@ struct OpsImpl {
   static void go_closure_tc(const Dev& d, const Params& P, const Uni<float>& U, const CloArgs& A, cudaStream_t s) {
     if constexpr (sizeof(R) == 4) {
       const SlotPtrs T = make_slots<St>(d, PAR);
-      auto* k = (!W64 && d.aos) ? &k_step_closure_tc<St, PAR, MAC, FRC, W64, MODE, true>
-                                : &k_step_closure_tc<St, PAR, MAC, FRC, W64, MODE, false>;
+      auto* k = (!W64 && d.aos == 64) ? &k_step_closure_tc<St, PAR, MAC, FRC, W64, MODE, 64>
+                : (!W64 && d.aos) ? &k_step_closure_tc<St, PAR, MAC, FRC, W64, MODE, 32>
+                                  : &k_step_closure_tc<St, PAR, MAC, FRC, W64, MODE, 0>;
       // the kernel is built for kClosureTcPerSm resident CTAs per SM
       // (launch bounds), each holding 32 of the SM's 512 TMEM columns
       int dev = 0, sms = 1;
@@ -1384,8 +1399,9 @@ struct OpsImpl {
       if (mode == 2) {
         const Uni<R> Us = make_uni<R>(P, R(St::kScale));
         const SlotPtrs T = make_slots<St>(d, PAR);
-        if (d.aos) k_step_held<St, PAR, MAC, FRC, true><<<L.grid, L.block, 0, s>>>(d, P, Us, T, A.nu, A.coef);
-        else k_step_held<St, PAR, MAC, FRC, false><<<L.grid, L.block, 0, s>>>(d, P, Us, T, A.nu, A.coef);
+        if (d.aos == 64) k_step_held<St, PAR, MAC, FRC, 64><<<L.grid, L.block, 0, s>>>(d, P, Us, T, A.nu, A.coef);
+        else if (d.aos) k_step_held<St, PAR, MAC, FRC, 32><<<L.grid, L.block, 0, s>>>(d, P, Us, T, A.nu, A.coef);
+        else k_step_held<St, PAR, MAC, FRC, 0><<<L.grid, L.block, 0, s>>>(d, P, Us, T, A.nu, A.coef);
         return;
       }
     }

@@ -91,20 +91,22 @@ extern "C" {
                                      are reproduced bit for bit by the oracle */
 #define LBM_FLAG_SOA           8  /* keep the in-place set in the SoA layout
                                      (slot k of cell c at k N + c) */
-#define LBM_FLAG_AOS          16  /* keep it in the AoSoA layout (blocks of 32
+#define LBM_FLAG_AOS          16  /* keep it in the AoSoA layout (blocks of
                                      cells along x, their 19 slots one after
-                                     the other) where that applies: nx a
-                                     multiple of 32, the FAST in-place step,
-                                     fp32 arithmetic, 19 N < 2^31.
+                                     the other: 64 cells for the 16-bit forms
+                                     where nx is a multiple of 64, else 32)
+                                     where that applies: nx a multiple of 32,
+                                     the FAST in-place step, fp32
+                                     arithmetic, 19 N < 2^31.
                                      Without either flag: the layout
                                      lbm_autotune_layout measured faster for
                                      this grid, storage and flags earlier in
-                                     the process, else AoSoA for LBM_F32 and
-                                     the SR forms and SoA for LBM_F16S and
-                                     LBM_BF16S (the faster one of each on
-                                     GB300).  The layout is
-                                     internal: populations in and out are
-                                     always the natural layout. */
+                                     the process, else AoSoA for LBM_F32, the
+                                     SR forms and the 16-bit forms with nx a
+                                     multiple of 64, SoA for the others (the
+                                     faster one of each on GB300).  The
+                                     layout is internal: populations in and
+                                     out are always the natural layout. */
 
 typedef struct lbm_ctx lbm_ctx;
 
@@ -135,7 +137,8 @@ typedef struct {
   int64_t steps;           /* steps done since init / set_populations */
   int32_t parity;          /* steps & 1 — the in-place layout's phase */
   int32_t block_x;         /* chosen launch shape of the step kernel */
-  int32_t layout;          /* population set: 0 in-place SoA, 1 ping-pong, 2 in-place AoSoA */
+  int32_t layout;          /* population set: 0 in-place SoA, 1 ping-pong, 2 in-place AoSoA
+                              in blocks of 32 cells, 3 in blocks of 64 */
 } lbm_info;
 
 /* SolverWebGPU.criar (src/backend/webgpu/solver.js:93-124): allocates; fails
@@ -238,7 +241,7 @@ int lbm_autotune(lbm_ctx* ctx, int steps, int* block_x, int* block_y, int* varia
  * an all-fluid box of these dimensions runs `steps` steps in each layout
  * (timed with CUDA events; two contexts created and destroyed in turn); the
  * faster layout becomes the default of lbm_create for this grid, storage and
- * flags in this process.  layout: 2 AoSoA, 0 SoA (1 if flags ask for the
+ * flags in this process.  layout: 2 or 3 AoSoA (blocks of 32 / 64 cells), 0 SoA (1 if flags ask for the
  * ping-pong set); ms_*: milliseconds per step (-1 where AoSoA does not
  * apply; nullable).  No counterpart in the reference. */
 int lbm_autotune_layout(const lbm_dims* dims, int storage, int flags, int steps, int* layout, float* ms_aos,

@@ -32,7 +32,7 @@ typedef struct {
   uint32_t magic, version;
   int32_t nx, ny, nz;
   int32_t storage;        /* LBM_F32 / LBM_F16S / LBM_BF16S / LBM_F64 */
-  int32_t layout;         /* 0 in-place SoA, 1 ping-pong, 2 in-place AoSoA */
+  int32_t layout;         /* 0 in-place SoA, 1 ping-pong, 2 in-place AoSoA in blocks of 32 cells, 3 of 64 */
   int32_t parity;         /* in-place: step parity of the stored set */
   int64_t steps;          /* steps taken when saved */
   uint64_t payload_bytes; /* 19 * N * bytes per stored value */

@@ -14,14 +14,15 @@ pytestmark = pytest.mark.gpu
 CFG = dict(omegaPlus=1.85, lesCs=0.12, inletU=[0.05, 0.0, 0.01], beltU=[0.05, 0.0, 0.0], espessuraCL=2)
 
 
-def _pair(storage, soa_too=True):
+def _pair(storage, soa_too=True, nx=64):
     from cfd__gb300 import SolverCUDA
-    grade, tipo, esp = all_types_tunnel(nx=64, ny=24, nz=20)
+    grade, tipo, esp = all_types_tunnel(nx=nx, ny=24, nz=20)
     g0 = random_state(int(np.prod(list(grade.values()))), seed=21)
     out = []
     for soa in ((False, True) if soa_too else (False,)):
         s = SolverCUDA(grade, storage=storage, soa=soa)
-        assert s.info()["layout"] == (0 if soa else 2)
+        # AoSoA blocks: 64 cells for the 16-bit forms where nx allows (layout 3), else 32 (2)
+        assert s.info()["layout"] == (0 if soa else (3 if storage != "f32" and nx % 64 == 0 else 2))
         s.definirTipos(tipo)
         s.configurar(**CFG, esponja=esp)
         s.definirPopulacoes(g0)
@@ -29,10 +30,11 @@ def _pair(storage, soa_too=True):
     return grade, tipo, esp, g0, out
 
 
-@pytest.mark.parametrize("storage", ["f32", "f16s", "bf16s"])
-def test_aos_step_bit_exact_against_oracle(native, storage):
+@pytest.mark.parametrize("storage,nx", [("f32", 64), ("f16s", 64), ("bf16s", 64), ("f16s", 96)])
+def test_aos_step_bit_exact_against_oracle(native, storage, nx):
+    """nx = 64: the 16-bit forms in blocks of 64 cells; nx = 96: in blocks of 32."""
     from oracle import oracle as O
-    grade, tipo, esp, g0, (s,) = _pair(storage, soa_too=False)
+    grade, tipo, esp, g0, (s,) = _pair(storage, soa_too=False, nx=nx)
     dt, q = {"f32": (np.float32, 0), "f16s": (np.float32, 1), "bf16s": (np.float32, 2)}[storage]
     o = O.Lattice((grade["nx"], grade["ny"], grade["nz"]), dtype=dt, storage=q, nthreads=8, fast=True)
     o.set_types(tipo)

@@ -44,7 +44,7 @@ def test_sr_step_bit_exact(native, storage, soa, strict):
     if strict and not soa:
         pytest.skip("the AoSoA layout is the FAST step's")
     grade, tipo, g0, s, o = _pair(storage, soa, strict, 2)
-    assert s.info()["layout"] == (0 if soa else 2)
+    assert s.info()["layout"] == (0 if soa else 3)   # AoSoA in blocks of 64 cells
     fl = ~np.isin(tipo, [1, 4, 7])
     for n in (1, 1, 7, 30):
         s.passo(n)

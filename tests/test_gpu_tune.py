@@ -81,11 +81,11 @@ def test_layout_tuner_sets_the_default(native):
     from cfd__gb300._native import LbmError
     g = {"nx": 64, "ny": 32, "nz": 24}
     r = SolverCUDA.autoajustarLayout(g, "f16s", passos=4)
-    assert r["layout"] in (0, 2) and r["ms_soa"] > 0 and r["ms_aosoa"] > 0
+    assert r["layout"] in (0, 3) and r["ms_soa"] > 0 and r["ms_aosoa"] > 0
     s = SolverCUDA(g, storage="f16s")
     assert s.info()["layout"] == r["layout"]
     assert SolverCUDA(g, storage="f16s", soa=True).info()["layout"] == 0
-    assert SolverCUDA(g, storage="f16s", soa=False).info()["layout"] == 2
+    assert SolverCUDA(g, storage="f16s", soa=False).info()["layout"] == 3   # blocks of 64 cells
     assert SolverCUDA({"nx": 70, "ny": 32, "nz": 24}, storage="f32", soa=False).info()["layout"] == 0  # nx % 32
     from cfd__gb300 import _native as nat
     import ctypes as C
