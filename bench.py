@@ -13,7 +13,7 @@ are also timed.  One "step" = one D3Q19 step over every cell (MLUPS counts
 all nx*ny*nz cells, as the reference's tests/desempenho.html:67-70).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--grid 512x256x192|320x160x128] [--storage f32|f16s|bf16s|f64]
+                    [--grid 512x256x192|320x160x128] [--storage f32|f16s|bf16s|f16sr|bf16sr|f64]
 
 Timing: W + 2W untimed warm-up steps, then K steps between CUDA events on
 the solver's stream, repeated R >= 5 times so the repeats span at least a
@@ -606,7 +606,8 @@ def run_ours(args):
             "value": mlups, "unit": "MLUPS", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms_step, "repeats": R, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": {"f32": "f32", "f16s": "f16 storage / f32 math", "bf16s": "bf16 storage / f32 math",
-                      "f64": "f64"}[args.storage],
+                      "f16sr": "f16 storage, stochastic rounding / f32 math",
+                      "bf16sr": "bf16 storage, stochastic rounding / f32 math", "f64": "f64"}[args.storage],
             "data": "synthetic",
             "config": {"workload": desc, "cells": N, "storage": args.storage, "layout": "in-place (esoteric pull)",
                        "parallelism": "replicas" if world > 1 else "single",
