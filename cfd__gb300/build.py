@@ -37,6 +37,8 @@ UNITS = {
     "lbm_inst_bf16s.cu": ["-fmad=false"],
     "lbm_inst_f16sr.cu": ["-fmad=false"],
     "lbm_inst_bf16sr.cu": ["-fmad=false"],
+    "lbm_inst_f16sr_clo.cu": ["-fmad=false"],
+    "lbm_inst_bf16sr_clo.cu": ["-fmad=false"],
     "lbm_inst_f32_clo.cu": ["-fmad=false"],
     "lbm_inst_f16s_clo.cu": ["-fmad=false"],
     "lbm_inst_bf16s_clo.cu": ["-fmad=false"],

@@ -264,10 +264,14 @@ int sync_desc(lbm_batch* b) {
 
 template <class St, bool FAST, int MINB>
 void launch_batch_m(lbm_batch* b, const BatchArgs& A, int parity, int grid) {
-  if (A.aos == 64) {
-    if (parity == 0) k_batch_step<St, 0, FAST, MINB, 64><<<grid, kTile, 0, b->stream>>>(A);
-    else k_batch_step<St, 1, FAST, MINB, 64><<<grid, kTile, 0, b->stream>>>(A);
-  } else if (A.aos) {
+  if constexpr (sizeof(typename St::store_t) == 2) {   // blocks of 64 cells: 16-bit forms only
+    if (A.aos == 64) {
+      if (parity == 0) k_batch_step<St, 0, FAST, MINB, 64><<<grid, kTile, 0, b->stream>>>(A);
+      else k_batch_step<St, 1, FAST, MINB, 64><<<grid, kTile, 0, b->stream>>>(A);
+      return;
+    }
+  }
+  if (A.aos) {
     if (parity == 0) k_batch_step<St, 0, FAST, MINB, 32><<<grid, kTile, 0, b->stream>>>(A);
     else k_batch_step<St, 1, FAST, MINB, 32><<<grid, kTile, 0, b->stream>>>(A);
   } else {

@@ -3,5 +3,9 @@
 #include "lbm_kernels.cuh"
 
 namespace lbm {
-Ops ops_bf16sr() { return OpsImpl<StBF16SR>::make(); }
+Ops ops_bf16sr() {
+  Ops o = OpsImpl<StBF16SR>::make();
+  o.step_closure = closure_bf16sr();
+  return o;
+}
 }  // namespace lbm

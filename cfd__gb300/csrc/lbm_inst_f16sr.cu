@@ -3,5 +3,9 @@
 #include "lbm_kernels.cuh"
 
 namespace lbm {
-Ops ops_f16sr() { return OpsImpl<StF16SR>::make(); }
+Ops ops_f16sr() {
+  Ops o = OpsImpl<StF16SR>::make();
+  o.step_closure = closure_f16sr();
+  return o;
+}
 }  // namespace lbm

@@ -342,6 +342,28 @@ struct AddrRt {
   __device__ __forceinline__ S* b(int k, bool nb) const { return F + at(slot_b(k, PAR), k, nb); }
 };
 
+// A store of an unscaled population value: rounded to nearest, or for the SR
+// storage forms stochastically with the cell's hash (the offset is formed
+// when the value exists: the empty asm ties the hash to it).
+template <class St>
+struct PopStore {
+  uint32_t h;
+  __device__ __forceinline__ PopStore(const Dev& d, uint32_t cell) : h(0u) {
+    if constexpr (St::kSR) h = sr_cell_hash(cell, d.seed);
+  }
+  template <class S, class R>
+  __device__ __forceinline__ void operator()(S* p, R v, int i) const {
+    if constexpr (St::kSR) {
+      uint32_t hh = h;
+      const R vs = v * R(St::kScale);
+      asm volatile("" : "+r"(hh) : "f"(vs));
+      St::st_sr(p, vs, (hh * sr_mult(i)) >> (32 - St::kSRBits));
+    } else {
+      St::st(p, v);
+    }
+  }
+};
+
 // In-place step.  Grid: (ceil(nx/bx), ceil(ny/by), nz), block (bx, by).
 // PAR: step parity (0 even).  MAC: write (u, delta).  FRC: accumulate the
 // momentum-exchange force of the state being streamed.
@@ -544,10 +566,11 @@ k_step_closure(Dev d, Params P, Uni<float> U, CloArgs A) {
   const Off cell = ((Off)z * ny + y) * nx + x;
   const AddrRt<St, PAR, Off> ad(d, cell, x, y, z);
   double fx = 0.0, fy = 0.0, fz = 0.0;
+  const PopStore<St> put(d, (uint32_t)cell);
   auto emit = [&](int i, R v) {
-    if (i == 0) St::st(ad.rest(), v);
-    else if (i & 1) St::st(ad.b((i - 1) >> 1, true), v);
-    else St::st(ad.a((i - 2) >> 1, false), v);
+    if (i == 0) put(ad.rest(), v, 0);
+    else if (i & 1) put(ad.b((i - 1) >> 1, true), v, i);
+    else put(ad.a((i - 2) >> 1, false), v, i);
   };
   R g[Q];
   R delta = R(0.0), rho = R(1.0), ux = R(0.0), uy = R(0.0), uz = R(0.0), uu = R(0.0), rinv = R(1.0);
@@ -759,10 +782,11 @@ k_step_closure_tc(Dev d, Params P, Uni<float> U, CloArgs A, SlotPtrs T, int gx, 
       if constexpr (W64 || AB != 0) return Ad(d, cell, inr ? x : 0, inr ? y : 0, z);
       else return Ad(d, T, cell, inr ? x : 0, inr ? y : 0, z);
     }();
+    const PopStore<St> put(d, (uint32_t)cell);
     auto emit = [&](int i, R v) {
-      if (i == 0) St::st(ad.rest(), v);
-      else if (i & 1) St::st(ad.b((i - 1) >> 1, true), v);
-      else St::st(ad.a((i - 2) >> 1, false), v);
+      if (i == 0) put(ad.rest(), v, 0);
+      else if (i & 1) put(ad.b((i - 1) >> 1, true), v, i);
+      else put(ad.a((i - 2) >> 1, false), v, i);
     };
     R g[Q];
     R delta = R(0.0), rho = R(1.0), ux = R(0.0), uy = R(0.0), uz = R(0.0), uu = R(0.0), rinv = R(1.0);
@@ -1266,12 +1290,15 @@ struct OpsImpl {
     if (d.aos) {
       if constexpr (FAST && sizeof(R) == 4) {
         // variant 9: store addresses kept in registers from the loads
-        if (d.aos == 64) {
-          if (!MAC && !FRC && L.occ == 9)
-            k_step_inplace<St, PAR, MAC, FRC, false, FAST, kDefault, true, false, 0, 64><<<L.grid, L.block, 0, s>>>(d, P, U, T);
-          else
-            k_step_inplace<St, PAR, MAC, FRC, false, FAST, kDefault, true, true, 0, 64><<<L.grid, L.block, 0, s>>>(d, P, U, T);
-          return;
+        // blocks of 64 cells: the 16-bit forms only (lbm_create)
+        if constexpr (sizeof(typename St::store_t) == 2) {
+          if (d.aos == 64) {
+            if (!MAC && !FRC && L.occ == 9)
+              k_step_inplace<St, PAR, MAC, FRC, false, FAST, kDefault, true, false, 0, 64><<<L.grid, L.block, 0, s>>>(d, P, U, T);
+            else
+              k_step_inplace<St, PAR, MAC, FRC, false, FAST, kDefault, true, true, 0, 64><<<L.grid, L.block, 0, s>>>(d, P, U, T);
+            return;
+          }
         }
         if (!MAC && !FRC && L.occ == 9)
           k_step_inplace<St, PAR, MAC, FRC, false, FAST, kDefault, true, false><<<L.grid, L.block, 0, s>>>(d, P, U, T);
@@ -1361,9 +1388,11 @@ struct OpsImpl {
   static void go_closure_tc(const Dev& d, const Params& P, const Uni<float>& U, const CloArgs& A, cudaStream_t s) {
     if constexpr (sizeof(R) == 4) {
       const SlotPtrs T = make_slots<St>(d, PAR);
-      auto* k = (!W64 && d.aos == 64) ? &k_step_closure_tc<St, PAR, MAC, FRC, W64, MODE, 64>
-                : (!W64 && d.aos) ? &k_step_closure_tc<St, PAR, MAC, FRC, W64, MODE, 32>
-                                  : &k_step_closure_tc<St, PAR, MAC, FRC, W64, MODE, 0>;
+      constexpr bool k16 = sizeof(typename St::store_t) == 2;   // blocks of 64 cells: 16-bit forms only
+      auto* k = (!W64 && d.aos) ? &k_step_closure_tc<St, PAR, MAC, FRC, W64, MODE, 32>
+                                : &k_step_closure_tc<St, PAR, MAC, FRC, W64, MODE, 0>;
+      if constexpr (k16)
+        if (!W64 && d.aos == 64) k = &k_step_closure_tc<St, PAR, MAC, FRC, W64, MODE, k16 ? 64 : 32>;
       // the kernel is built for kClosureTcPerSm resident CTAs per SM
       // (launch bounds), each holding 32 of the SM's 512 TMEM columns
       int dev = 0, sms = 1;
@@ -1399,8 +1428,13 @@ struct OpsImpl {
       if (mode == 2) {
         const Uni<R> Us = make_uni<R>(P, R(St::kScale));
         const SlotPtrs T = make_slots<St>(d, PAR);
-        if (d.aos == 64) k_step_held<St, PAR, MAC, FRC, 64><<<L.grid, L.block, 0, s>>>(d, P, Us, T, A.nu, A.coef);
-        else if (d.aos) k_step_held<St, PAR, MAC, FRC, 32><<<L.grid, L.block, 0, s>>>(d, P, Us, T, A.nu, A.coef);
+        if constexpr (sizeof(typename St::store_t) == 2) {   // blocks of 64 cells: 16-bit forms only
+          if (d.aos == 64) {
+            k_step_held<St, PAR, MAC, FRC, 64><<<L.grid, L.block, 0, s>>>(d, P, Us, T, A.nu, A.coef);
+            return;
+          }
+        }
+        if (d.aos) k_step_held<St, PAR, MAC, FRC, 32><<<L.grid, L.block, 0, s>>>(d, P, Us, T, A.nu, A.coef);
         else k_step_held<St, PAR, MAC, FRC, 0><<<L.grid, L.block, 0, s>>>(d, P, Us, T, A.nu, A.coef);
         return;
       }
@@ -1453,6 +1487,8 @@ Ops ops_bf16s();
 StepClosureFn closure_f32();
 StepClosureFn closure_f16s();
 StepClosureFn closure_bf16s();
+StepClosureFn closure_f16sr();
+StepClosureFn closure_bf16sr();
 Ops ops_f16sr();
 Ops ops_bf16sr();
 

@@ -171,8 +171,12 @@ def _run_pair(p_closure, cfg_a, cfg_b, steps=(1, 7, 16), storage="f32", motor=0)
 
 
 @pytest.mark.parametrize("storage,motor,every", [("f32", 0, 1), ("f16s", 0, 1), ("bf16s", 0, 1), ("f32", 1, 1),
-                                                 ("f32", 0, 4), ("f16s", 1, 3)])
+                                                 ("f32", 0, 4), ("f16s", 1, 3), ("f16sr", 0, 1), ("f16sr", 1, 1),
+                                                 ("bf16sr", 0, 3)])
 def test_unusable_output_falls_back_bit_exact(native, storage, motor, every):
+    """f16sr / bf16sr: the closure steps round their stores stochastically
+    with the same cell hash as the plain step, so the fallback is still the
+    plain step bit for bit."""
     from cfd__gb300 import fecho
     p = fecho.pesos_vazios()
     p["b3"] = np.float32(np.nan)

@@ -121,3 +121,4 @@ def test_sr_refusals(native):
     rc = L.lbm_batch_create(C.cast(dims, C.c_void_p), 1, nat.F16SR, 0, C.byref(b))
     with pytest.raises(LbmError, match="ENOTSUP"):
         nat.check(rc)
+
