@@ -70,15 +70,17 @@ def test_aos_equals_soa_with_fused_force(native, storage):
         s.destruir()
 
 
-@pytest.mark.parametrize("motor,every", [(0, 1), (1, 1), (0, 4)])
-def test_aos_closure_equals_soa(native, motor, every):
-    """The closure steps address either layout: same states bit for bit."""
+@pytest.mark.parametrize("storage,motor,every", [("f32", 0, 1), ("f32", 1, 1), ("f32", 0, 4), ("f16s", 0, 1),
+                                                 ("f16s", 1, 1), ("f16sr", 1, 4)])
+def test_aos_closure_equals_soa(native, storage, motor, every):
+    """The closure steps address either layout (blocks of 32 cells for fp32,
+    64 for the 16-bit forms): same states bit for bit."""
     import os
 
     from cfd__gb300.fecho import carregar
     p = carregar(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "cfd__gb300", "pesos",
                               "fecho_coef.npz"))
-    grade, tipo, esp, g0, (a, b) = _pair("f32")
+    grade, tipo, esp, g0, (a, b) = _pair(storage)
     fl = ~np.isin(tipo, [1, 4, 7])
     for s in (a, b):
         s.configurar(**CFG, esponja=esp, closure=every)
