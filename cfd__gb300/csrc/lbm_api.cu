@@ -265,6 +265,7 @@ Dev dev_of(const lbm_ctx* c) {
   d.blf = c->blf_on ? c->blf : nullptr;
   d.aos = c->aos ? c->aos_b : 0;
   d.seed = sr_seed(c->steps);
+  d.seed_base = nullptr;
   return d;
 }
 

@@ -94,6 +94,11 @@ __global__ void __launch_bounds__(kTile, MINB) k_batch_step(const __grid_constan
   }
 }
 
+// The device copy of the batch's step count advances with the steps (stream
+// order, so a captured graph advances it on every replay).
+__global__ void k_steps_add(uint32_t* c, uint32_t n) { *c += n; }
+__global__ void k_steps_set(uint32_t* c, uint32_t v) { *c = v; }
+
 int bfail(int code, const std::string& m) { return lbm_internal_fail(code, m.c_str()); }
 
 #define BCK(call, what)                                                                  \
@@ -110,6 +115,8 @@ Ops ops_for_batch(int storage) {
   switch (storage) {
     case LBM_F16S: return ops_f16s();
     case LBM_BF16S: return ops_bf16s();
+    case LBM_F16SR: return ops_f16sr();
+    case LBM_BF16SR: return ops_bf16sr();
     default: return ops_f32();
   }
 }
@@ -147,6 +154,7 @@ struct lbm_batch {
   cudaEvent_t fork = nullptr;
   std::vector<cudaEvent_t> joins;
   std::vector<void*> blf;            // per tunnel: nz inlet boundary-layer factors
+  uint32_t* steps_dev = nullptr;     // the step count on the device: the SR forms' rounding seeds
   int4* tiles = nullptr;             // tile table of the persistent launches (mode 1)
   size_t tiles_cap = 0;              // its capacity in tiles
 };
@@ -263,7 +271,14 @@ int sync_desc(lbm_batch* b) {
 }
 
 template <class St, bool FAST, int MINB>
-void launch_batch_m(lbm_batch* b, const BatchArgs& A, int parity, int grid) {
+void launch_batch_m(lbm_batch* b, const BatchArgs& A0, int parity, int grid, uint32_t off) {
+  // the SR forms: each tunnel's seed is the device step count + off
+  BatchArgs A1;
+  if constexpr (St::kSR) {
+    A1 = A0;
+    for (int i = 0; i < A1.ntun; ++i) A1.t[i].d.seed = off;
+  }
+  const BatchArgs& A = St::kSR ? A1 : A0;
   if constexpr (sizeof(typename St::store_t) == 2) {   // blocks of 64 cells: 16-bit forms only
     if (A.aos == 64) {
       if (parity == 0) k_batch_step<St, 0, FAST, MINB, 64><<<grid, kTile, 0, b->stream>>>(A);
@@ -281,25 +296,28 @@ void launch_batch_m(lbm_batch* b, const BatchArgs& A, int parity, int grid) {
 }
 
 template <class St>
-void launch_batch(lbm_batch* b, int parity) {
+void launch_batch(lbm_batch* b, int parity, uint32_t off) {
   for (const BatchArgs& A : b->args) {
     const int per_sm = b->minb;
     const int grid = std::min(b->sms * per_sm, std::max(1, A.ntiles));
     if (b->fast) {
-      if (per_sm == 6) launch_batch_m<St, true, 6>(b, A, parity, grid);
-      else launch_batch_m<St, true, 8>(b, A, parity, grid);
+      if (per_sm == 6) launch_batch_m<St, true, 6>(b, A, parity, grid, off);
+      else launch_batch_m<St, true, 8>(b, A, parity, grid, off);
     } else {
-      if (per_sm == 6) launch_batch_m<St, false, 6>(b, A, parity, grid);
-      else launch_batch_m<St, false, 8>(b, A, parity, grid);
+      if (per_sm == 6) launch_batch_m<St, false, 6>(b, A, parity, grid, off);
+      else launch_batch_m<St, false, 8>(b, A, parity, grid, off);
     }
   }
 }
 
-void launch_one(lbm_batch* b, int parity) {
+// One persistent-mode step; off: its place after the device step count.
+void launch_one(lbm_batch* b, int parity, uint32_t off) {
   switch (b->storage) {
-    case LBM_F16S: launch_batch<StF16S>(b, parity); break;
-    case LBM_BF16S: launch_batch<StBF16S>(b, parity); break;
-    default: launch_batch<StF32>(b, parity); break;
+    case LBM_F16S: launch_batch<StF16S>(b, parity, off); break;
+    case LBM_BF16S: launch_batch<StBF16S>(b, parity, off); break;
+    case LBM_F16SR: launch_batch<StF16SR>(b, parity, off); break;
+    case LBM_BF16SR: launch_batch<StBF16SR>(b, parity, off); break;
+    default: launch_batch<StF32>(b, parity, off); break;
   }
 }
 
@@ -315,8 +333,10 @@ cudaError_t launch_chains(lbm_batch* b, int parity, int nsteps) {
     cudaStream_t L = b->lanes[k];
     if ((e = cudaStreamWaitEvent(L, b->fork, 0)) != cudaSuccess) return e;
     const TunnelDesc& D = b->host[k];
+    Dev dd = D.d;
     for (int s = 0; s < nsteps; ++s) {
-      e = b->ops.step(D.d, D.P, (parity + s) & 1, true, false, false, b->fast, tunnel_launch(b->dims[k]), L);
+      dd.seed = (uint32_t)s;   // the SR forms' seed: the device step count + s
+      e = b->ops.step(dd, D.P, (parity + s) & 1, true, false, false, b->fast, tunnel_launch(b->dims[k]), L);
       if (e != cudaSuccess) return e;
     }
     if ((e = cudaEventRecord(b->joins[k], L)) != cudaSuccess) return e;
@@ -351,8 +371,9 @@ extern "C" {
 int lbm_batch_create(const lbm_dims* dims, int ntunnels, int storage, int flags, lbm_batch** out) {
   if (!dims || !out || ntunnels < 1) return bfail(LBM_EINVAL, "need at least one tunnel and an output handle");
   *out = nullptr;
-  if (storage != LBM_F32 && storage != LBM_F16S && storage != LBM_BF16S)
-    return bfail(LBM_ENOTSUP, "batched tunnels support LBM_F32, LBM_F16S and LBM_BF16S");
+  if (storage != LBM_F32 && storage != LBM_F16S && storage != LBM_BF16S && storage != LBM_F16SR &&
+      storage != LBM_BF16SR)
+    return bfail(LBM_ENOTSUP, "batched tunnels support LBM_F32 and the 16-bit forms");
   if (flags & ~LBM_FLAG_STRICT) return bfail(LBM_EINVAL, "batched tunnels accept LBM_FLAG_STRICT only");
   lbm_batch* b = new lbm_batch();
   b->storage = storage;
@@ -390,7 +411,10 @@ int lbm_batch_create(const lbm_dims* dims, int ntunnels, int storage, int flags,
   void* p = nullptr;
   if (!r) r = balloc(b, &p, 3 * sizeof(double), "reduction result");
   b->red = static_cast<double*>(p);
+  if (!r) r = balloc(b, &p, sizeof(uint32_t), "step count");
+  b->steps_dev = static_cast<uint32_t*>(p);
   if (r) { lbm_batch_destroy(b); return r; }
+  for (auto& D : b->host) D.d.seed_base = b->steps_dev;
   cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) { lbm_batch_destroy(b); return bfail(LBM_ECUDA, "stream creation failed"); }
   b->own_stream = true;
@@ -399,6 +423,7 @@ int lbm_batch_create(const lbm_dims* dims, int ntunnels, int storage, int flags,
     cudaMemsetAsync(D.d.pop, 0, (size_t)D.d.N * Q * b->ops.elem_bytes, b->stream);
     cudaMemsetAsync((void*)D.d.tipo, 0, (size_t)D.d.N, b->stream);
   }
+  cudaMemsetAsync(b->steps_dev, 0, sizeof(uint32_t), b->stream);
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -452,7 +477,7 @@ int lbm_batch_configure(lbm_batch* b, int k, const lbm_params* p) {
   }
   b->host[k].d.blf = on ? b->blf[k] : nullptr;
   b->host[k].P = P;
-  b->host[k].U = make_uni<float>(P, b->storage == LBM_F16S ? StF16S::kScale : 1.0f);
+  b->host[k].U = make_uni<float>(P, (b->storage == LBM_F16S || b->storage == LBM_F16SR) ? StF16S::kScale : 1.0f);
   b->configured[k] = true;
   b->desc_dirty = true;
   return LBM_OK;
@@ -483,6 +508,8 @@ int lbm_batch_init_equilibrium(lbm_batch* b) {
     BCK(b->ops.init(D.d, D.P, true, tunnel_launch(b->dims[k]), b->stream), "init kernel");
   }
   b->steps = 0;
+  k_steps_set<<<1, 1, 0, b->stream>>>(b->steps_dev, 0u);
+  BCK(cudaGetLastError(), "step count");
   return LBM_OK;
 }
 
@@ -517,7 +544,8 @@ int lbm_batch_step(lbm_batch* b, int n) {
       BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal), "graph capture begin");
       cudaError_t ce = cudaSuccess;
       if (b->mode == 0) ce = launch_chains(b, par, G);
-      else for (int s = 0; s < G; ++s) launch_one(b, (par + s) & 1);
+      else for (int s = 0; s < G; ++s) launch_one(b, (par + s) & 1, (uint32_t)s);
+      k_steps_add<<<1, 1, 0, b->stream>>>(b->steps_dev, (uint32_t)G);
       cudaError_t e = cudaStreamEndCapture(b->stream, &g);
       if (ce != cudaSuccess) e = ce;
       if (e != cudaSuccess) return bfail(LBM_ECUDA, std::string("graph capture: ") + cudaGetErrorString(e));
@@ -531,13 +559,19 @@ int lbm_batch_step(lbm_batch* b, int n) {
   }
   if (n > 0 && b->mode == 0) {
     BCK(launch_chains(b, (int)(b->steps & 1), n), "batch step launch");
+    k_steps_add<<<1, 1, 0, b->stream>>>(b->steps_dev, (uint32_t)n);
+    BCK(cudaGetLastError(), "step count");
     b->steps += n;
     n = 0;
   }
-  for (; n > 0; --n) {
-    launch_one(b, (int)(b->steps & 1));
+  for (int s = 0; s < n; ++s) {
+    launch_one(b, (int)((b->steps + s) & 1), (uint32_t)s);
     BCK(cudaGetLastError(), "batch step launch");
-    b->steps++;
+  }
+  if (n > 0) {
+    k_steps_add<<<1, 1, 0, b->stream>>>(b->steps_dev, (uint32_t)n);
+    BCK(cudaGetLastError(), "step count");
+    b->steps += n;
   }
   return LBM_OK;
 }
@@ -682,6 +716,7 @@ int lbm_batch_autotune(lbm_batch* b, int steps, int* mode_out, int* minb_out, fl
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   b->steps = steps0;
+  k_steps_set<<<1, 1, 0, b->stream>>>(b->steps_dev, (uint32_t)steps0);
   drop_graphs(b);
   b->desc_dirty = true;
   if (r) { b->mode = mode0; b->minb = minb0; b->tile_req = tiles0; return r; }

@@ -46,8 +46,14 @@ struct Dev {
   double* force;         // nullable: kForceSlots x 3 doubles accumulated by the fused force
   const void* blf;       // nullable: nz inlet boundary-layer factors in the arithmetic type
   int aos;               // in-place set in the AoSoA layout (elem_off) instead of SoA
-  uint32_t seed;         // sr_seed(step count): the stochastic rounding of the SR storage forms
+  uint32_t seed;         // the SR storage forms' rounding seed: sr_seed(step count), or with
+  const uint32_t* seed_base;   // a device step counter (batches) sr_seed(*seed_base + seed)
 };
+
+// The step's rounding seed (the SR storage forms).
+__device__ __forceinline__ uint32_t dev_seed(const Dev& d) {
+  return d.seed_base ? sr_seed((int64_t)(uint32_t)(*d.seed_base + d.seed)) : d.seed;
+}
 
 // The in-place set's two layouts.  SoA: slot k of location c at k N + c.
 // AoSoA (nx a multiple of 32): the cells are cut into blocks of 32 along x;
@@ -349,7 +355,7 @@ template <class St>
 struct PopStore {
   uint32_t h;
   __device__ __forceinline__ PopStore(const Dev& d, uint32_t cell) : h(0u) {
-    if constexpr (St::kSR) h = sr_cell_hash(cell, d.seed);
+    if constexpr (St::kSR) h = sr_cell_hash(cell, dev_seed(d));
   }
   template <class S, class R>
   __device__ __forceinline__ void operator()(S* p, R v, int i) const {
@@ -449,7 +455,7 @@ __device__ __forceinline__ void step_cell_at(const Dev& d, const Params& P, cons
   ad.refresh();
   // the SR storage forms round each store stochastically (sr_cell_hash)
   uint32_t hsr = 0;
-  if constexpr (St::kSR) hsr = sr_cell_hash((uint32_t)cell, d.seed);
+  if constexpr (St::kSR) hsr = sr_cell_hash((uint32_t)cell, dev_seed(d));
   auto put = [&](S* p, R v, int i) {
     if constexpr (St::kSR) {
       // the hash passes through an empty asm that also reads the stored

@@ -72,9 +72,9 @@ extern "C" {
                           rounding direction against a per-cell, per-step,
                           per-direction hash (unbiased; reproducible: the hash
                           depends on the cell, the step count and the
-                          direction only; the learned closure's steps round
-                          the same way).  In-place set only; not in
-                          batches. */
+                          direction only; the learned closure's steps and
+                          batched tunnels round the same way).  In-place set
+                          only. */
 #define LBM_BF16SR 5   /* as LBM_BF16S, stores rounded stochastically (16
                           dropped bits), same limits as LBM_F16SR */
 

@@ -12,10 +12,12 @@ def _tunnels():
     return sorteio_lote(n=5, seed=11, nx_min=32, nx_max=80)
 
 
-@pytest.mark.parametrize("storage", ["f32", "f16s"])
+@pytest.mark.parametrize("storage", ["f32", "f16s", "f16sr"])
 @pytest.mark.parametrize("tile", [0, 32])
 @pytest.mark.parametrize("mode", [0, 1])
 def test_batch_equals_separate_solvers(native, storage, tile, mode):
+    """f16sr: the stochastic rounding's seeds follow each tunnel's step count
+    through the graph replays and the direct launches."""
     from cfd__gb300 import SolverCUDA
     from cfd__gb300.lote import LoteCUDA
     tun = _tunnels()
