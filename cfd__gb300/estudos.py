@@ -150,7 +150,7 @@ def precisao(steps=10000, grade=None, forms=("f64", "f32", "f16s", "bf16s", "f16
     return out
 
 
-def lote(n_tunnels=64, steps=256, storages=("f32", "f16s"), seed=2026):
+def lote(n_tunnels=64, steps=256, storages=("f32", "f16s", "f16sr"), seed=2026):
     """Batched workload: n tunnels drawn by sorteio_lote (96x48x48 to
     256x128x128).  Aggregate MLUPS = sum N_k * steps / time, for the batch in
     mode 0 (a captured graph of per-tunnel chains), in mode 1 (one persistent
