@@ -45,7 +45,7 @@ struct Dev {
   float4* macros;        // nullable
   double* force;         // nullable: kForceSlots x 3 doubles accumulated by the fused force
   const void* blf;       // nullable: nz inlet boundary-layer factors in the arithmetic type
-  int aos;               // in-place set in the AoSoA layout (elem_off) instead of SoA
+  int aos;               // 0: the in-place set in SoA; else its AoSoA block width (32 or 64, elem_off)
   uint32_t seed;         // the SR storage forms' rounding seed: sr_seed(step count), or with
   const uint32_t* seed_base;   // a device step counter (batches) sr_seed(*seed_base + seed)
 };
@@ -56,12 +56,14 @@ __device__ __forceinline__ uint32_t dev_seed(const Dev& d) {
 }
 
 // The in-place set's two layouts.  SoA: slot k of location c at k N + c.
-// AoSoA (nx a multiple of 32): the cells are cut into blocks of 32 along x;
-// a block holds its 19 slots one after the other, 32 elements each, so
-// slot k of location c sits at (c / 32) 19 * 32 + 32 k + c % 32 =
-// (c & ~31) 19 + 32 k + (c & 31).  A warp's access to one slot still
+// AoSoA (nx a multiple of the block width B): the cells are cut into blocks
+// of B along x; a block holds its 19 slots one after the other, B elements
+// each, so slot k of location c sits at (c / B) 19 B + B k + c % B =
+// (c & ~(B-1)) 19 + B k + (c & (B-1)).  A warp's access to one slot still
 // covers 32 consecutive elements, and every slot of a location is a
-// constant offset (32 k elements) from the location's slot 0.
+// constant offset (B k elements) from the location's slot 0.  B = 32 for
+// fp32 (a slot row is a 128-byte line), 64 for the 16-bit forms where nx
+// allows (again a 128-byte line, read by a CTA's two warps together).
 constexpr int kAosB = 32;
 __host__ __device__ __forceinline__ int64_t aos_base(int64_t c, int B = kAosB) {
   return (c & ~(int64_t)(B - 1)) * 19 + (c & (B - 1));
