@@ -424,8 +424,8 @@ def run_ours(args):
     vox = voxelizer_timing() if not args.no_forms else None
 
     def maker(tp, cf, gr):
-        def make(storage, closure=0, pesos=None):
-            s = SolverCUDA(gr, storage=storage, escrever_macros=False)
+        def make(storage, closure=0, pesos=None, soa=None):
+            s = SolverCUDA(gr, storage=storage, escrever_macros=False, soa=soa)
             s.definirStream(stream.cuda_stream)
             s.definirTipos(tp)
             s.configurar(**cf, closure=closure)
@@ -538,18 +538,20 @@ def run_ours(args):
                          "meets_1pct_cd": None if e is None else abs(e) <= 0.01}
         forms["fp16_store_vs_fp32"] = cmp16
         # the step kernel's addressing variants side by side (lbm_set_launch
-        # codes) in each storage form's default layout: AoSoA for fp32 (where
-        # nx is a multiple of 32), SoA for the 16-bit forms
+        # codes): in the AoSoA layout (the default where nx allows; blocks of
+        # 64 cells for the 16-bit forms) and, for the 16-bit forms, in SoA
         variants = {}
+        aos_ok = GRIDS[args.grid]["nx"] % 32 == 0
         for st in ("f32", "f16s", "bf16s"):
             row = {}
-            if GRIDS[args.grid]["nx"] % 32 == 0 and st == "f32":
-                codes = (("aosoa_recompute_addresses", 8), ("aosoa_keep_addresses", 9))
-            else:
-                codes = (("soa_slot_pointers", 8), ("soa_slot_offsets_32bit", 20), ("soa_base_plus_slot_times_n", 21),
-                         ("soa_80_registers", 6))
-            for name, code in codes:
-                s2 = make(st)
+            codes = []
+            if aos_ok:
+                codes += [("aosoa_recompute_addresses", 8, False), ("aosoa_keep_addresses", 9, False)]
+            if st != "f32" or not aos_ok:
+                codes += [("soa_slot_pointers", 8, True), ("soa_slot_offsets_32bit", 20, True),
+                          ("soa_base_plus_slot_times_n", 21, True), ("soa_80_registers", 6, True)]
+            for name, code, soa in codes:
+                s2 = make(st, soa=soa)
                 s2.definirBloco(64, code)
                 s2.passo(args.warmup)
                 ms2, _ = timed(s2, stream, args.steps, min_total_ms=300.0)
@@ -559,9 +561,10 @@ def run_ours(args):
             variants[st] = row
         forms["step_variants"] = variants
         # the in-place set's two layouts side by side (AoSoA is the default
-        # where nx is a multiple of 32)
+        # where nx allows: blocks of 32 cells for fp32, 64 for the 16-bit
+        # forms; the layout code says which)
         lay = {}
-        for st in ("f32", "f16s", "bf16s"):
+        for st in ("f32", "f16s", "bf16s", "f16sr"):
             row = {}
             for name, soa in (("aosoa", False), ("soa", True)):
                 s2 = SolverCUDA(grade, storage=st, escrever_macros=False, soa=soa)
