@@ -147,6 +147,8 @@ struct lbm_ctx {
   bool inplace = true;
   bool aos = false;       // in-place set in the AoSoA layout (lbm_kernels.cuh, elem_off)
   int aos_b = 32;         // its block width (cells along x)
+  int nxp = 0;            // its row length: nx rounded up to the block width (nx for SoA)
+  int64_t nset = 0;       // cells per population slot, padding included
   Ops ops{};
   void* pop = nullptr;    // in-place set, or ping-pong front
   void* pop2 = nullptr;   // ping-pong back
@@ -264,6 +266,7 @@ Dev dev_of(const lbm_ctx* c) {
   d.force = nullptr;
   d.blf = c->blf_on ? c->blf : nullptr;
   d.aos = c->aos ? c->aos_b : 0;
+  d.nxp = c->nxp;
   d.seed = sr_seed(c->steps);
   d.seed_base = nullptr;
   return d;
@@ -397,18 +400,18 @@ int lbm_create(const lbm_dims* dims, int storage, int flags, lbm_ctx** out) {
   c->storage = storage;
   c->flags = flags;
   c->inplace = !(flags & LBM_FLAG_PINGPONG);
-  // AoSoA where the in-place FAST step can use it (nx a multiple of the
-  // 32-cell block, fp32 arithmetic, 32-bit element offsets) and it is the
-  // layout asked for, the one lbm_autotune_layout measured faster for this
-  // grid, or by default for fp32, for the stochastically rounded 16-bit forms
-  // and for every 16-bit form whose nx allows blocks of 64 cells (measured on
-  // GB300: with blocks of 32 cells the round-to-nearest 16-bit forms ran
-  // slower than SoA on most grids, with 64 faster)
-  const bool aos_ok = c->inplace && !(flags & LBM_FLAG_STRICT) && storage != LBM_F64 && dims->nx % 32 == 0 &&
-                      (int64_t)Q * c->N < (int64_t)INT32_MAX;
-  // 16-bit forms: blocks of 64 cells (one 128-byte line per slot row)
+  // AoSoA where the in-place FAST step can use it (fp32 arithmetic, 32-bit
+  // element offsets over the padded rows), in blocks of 32 cells for fp32
+  // and 64 for the 16-bit forms (one 128-byte line per slot row), rows
+  // padded to a multiple of the block; the default unless the layout asked
+  // for or the one lbm_autotune_layout measured faster for this grid says
+  // otherwise (measured on GB300: faster than SoA for every form)
   const bool is16 = storage != LBM_F32 && storage != LBM_F64;
-  bool want_aos = storage == LBM_F32 || is_sr(storage) || (is16 && dims->nx % 64 == 0);
+  const int ab = is16 ? 64 : 32;
+  const int nxp_a = (dims->nx + ab - 1) / ab * ab;
+  const bool aos_ok = c->inplace && !(flags & LBM_FLAG_STRICT) && storage != LBM_F64 &&
+                      (int64_t)Q * nxp_a * dims->ny * dims->nz < (int64_t)INT32_MAX;
+  bool want_aos = true;
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_layout.find(LayoutKey(dims->nx, dims->ny, dims->nz, storage, flags & ~LBM_FLAG_WRITE_MACROS));
@@ -417,9 +420,11 @@ int lbm_create(const lbm_dims* dims, int storage, int flags, lbm_ctx** out) {
   if (flags & LBM_FLAG_AOS) want_aos = true;
   if (flags & LBM_FLAG_SOA) want_aos = false;
   c->aos = aos_ok && want_aos;
-  c->aos_b = (c->aos && is16 && dims->nx % 64 == 0) ? 64 : 32;
+  c->aos_b = ab;
+  c->nxp = c->aos ? nxp_a : dims->nx;
+  c->nset = (int64_t)c->nxp * dims->ny * dims->nz;
   c->ops = ops_for(storage);
-  const size_t set_bytes = (size_t)c->N * Q * c->ops.elem_bytes;
+  const size_t set_bytes = (size_t)c->nset * Q * c->ops.elem_bytes;
   int r = dalloc(c, &c->pop, set_bytes, "populations");
   if (!r && !c->inplace) r = dalloc(c, &c->pop2, set_bytes, "second population set");
   if (!r) r = dalloc(c, (void**)&c->tipo, (size_t)c->N, "cell types");
@@ -736,7 +741,7 @@ static_assert(sizeof(lbm_state_header) == 48, "lbm_state_header layout");
 
 int lbm_state_bytes(lbm_ctx* c, size_t* bytes) {
   if (!c || !bytes) return fail(LBM_EINVAL, "null argument");
-  *bytes = sizeof(lbm_state_header) + (size_t)Q * (size_t)c->N * (size_t)c->ops.elem_bytes;
+  *bytes = sizeof(lbm_state_header) + (size_t)Q * (size_t)c->nset * (size_t)c->ops.elem_bytes;
   return LBM_OK;
 }
 
@@ -976,7 +981,7 @@ int lbm_autotune(lbm_ctx* c, int steps, int* block_x, int* block_y, int* variant
       for (int kz : {4, 8, 16}) cand.push_back({64, 1, 8, kz});
   }
   // the state is saved and put back: the trials advance a copy of it
-  const size_t set_bytes = (size_t)c->N * Q * c->ops.elem_bytes;
+  const size_t set_bytes = (size_t)c->nset * Q * c->ops.elem_bytes;
   void* keep = nullptr;
   cudaError_t e = cudaMalloc(&keep, set_bytes);
   if (e != cudaSuccess) { cudaGetLastError(); return fail(LBM_ENOMEM, "no device memory for the tuner's copy of the state"); }

@@ -101,6 +101,9 @@ __global__ void k_steps_set(uint32_t* c, uint32_t v) { *c = v; }
 
 int bfail(int code, const std::string& m) { return lbm_internal_fail(code, m.c_str()); }
 
+// Cells per population slot of a tunnel's set, the AoSoA rows' padding included.
+size_t set_cells(const Dev& d) { return (size_t)d.nxp * d.ny * d.nz; }
+
 #define BCK(call, what)                                                                  \
   do {                                                                                   \
     cudaError_t _e = (call);                                                             \
@@ -394,10 +397,14 @@ int lbm_batch_create(const lbm_dims* dims, int ntunnels, int storage, int flags,
     memset(&D, 0, sizeof D);
     D.d.nx = d.nx; D.d.ny = d.ny; D.d.nz = d.nz; D.d.N = N;
     // the AoSoA layout where the FAST step can use it: blocks of 64 cells for
-    // the 16-bit forms where nx allows, else 32
-    D.d.aos = !b->fast ? 0 : (storage != LBM_F32 && d.nx % 64 == 0) ? 64 : (d.nx % kAosB == 0 ? kAosB : 0);
+    // the 16-bit forms, 32 for fp32, rows padded to a multiple of the block
+    const int ab = storage != LBM_F32 ? 64 : kAosB;
+    const int nxp = (d.nx + ab - 1) / ab * ab;
+    const bool aos = b->fast && (int64_t)Q * nxp * d.ny * d.nz < (int64_t)INT32_MAX;
+    D.d.aos = aos ? ab : 0;
+    D.d.nxp = aos ? nxp : d.nx;
     void* p = nullptr;
-    const size_t sb = (size_t)N * Q * b->ops.elem_bytes;
+    const size_t sb = set_cells(D.d) * Q * b->ops.elem_bytes;
     if ((r = balloc(b, &p, sb, "populations"))) break;
     D.d.pop = p;
     if ((r = balloc(b, &p, (size_t)N, "cell types"))) break;
@@ -420,7 +427,7 @@ int lbm_batch_create(const lbm_dims* dims, int ntunnels, int storage, int flags,
   b->own_stream = true;
   for (int k = 0; k < ntunnels; ++k) {
     TunnelDesc& D = b->host[k];
-    cudaMemsetAsync(D.d.pop, 0, (size_t)D.d.N * Q * b->ops.elem_bytes, b->stream);
+    cudaMemsetAsync(D.d.pop, 0, set_cells(D.d) * Q * b->ops.elem_bytes, b->stream);
     cudaMemsetAsync((void*)D.d.tipo, 0, (size_t)D.d.N, b->stream);
   }
   cudaMemsetAsync(b->steps_dev, 0, sizeof(uint32_t), b->stream);
@@ -645,7 +652,7 @@ int lbm_batch_autotune(lbm_batch* b, int steps, int* mode_out, int* minb_out, fl
   // every tunnel's set is saved and put back: the trials advance copies
   std::vector<void*> keep(b->host.size(), nullptr);
   for (size_t k = 0; k < b->host.size(); ++k) {
-    const size_t bytes = (size_t)b->host[k].d.N * Q * b->ops.elem_bytes;
+    const size_t bytes = set_cells(b->host[k].d) * Q * b->ops.elem_bytes;
     if (cudaMalloc(&keep[k], bytes) != cudaSuccess) {
       cudaGetLastError();
       for (void* p : keep) if (p) cudaFree(p);
@@ -708,7 +715,7 @@ int lbm_batch_autotune(lbm_batch* b, int steps, int* mode_out, int* minb_out, fl
   if (!r && best1 < best) { best = best1; best_mode = 1; best_minb = minb1; best_tiles = b->tile_req; }
   // put the states back
   for (size_t k = 0; k < b->host.size(); ++k) {
-    const size_t bytes = (size_t)b->host[k].d.N * Q * b->ops.elem_bytes;
+    const size_t bytes = set_cells(b->host[k].d) * Q * b->ops.elem_bytes;
     cudaMemcpyAsync(b->host[k].d.pop, keep[k], bytes, cudaMemcpyDeviceToDevice, b->stream);
   }
   cudaError_t e = cudaStreamSynchronize(b->stream);

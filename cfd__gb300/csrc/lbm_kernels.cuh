@@ -46,6 +46,7 @@ struct Dev {
   double* force;         // nullable: kForceSlots x 3 doubles accumulated by the fused force
   const void* blf;       // nullable: nz inlet boundary-layer factors in the arithmetic type
   int aos;               // 0: the in-place set in SoA; else its AoSoA block width (32 or 64, elem_off)
+  int nxp;               // AoSoA: the row length in cells, nx rounded up to the block width
   uint32_t seed;         // the SR storage forms' rounding seed: sr_seed(step count), or with
   const uint32_t* seed_base;   // a device step counter (batches) sr_seed(*seed_base + seed)
 };
@@ -56,21 +57,27 @@ __device__ __forceinline__ uint32_t dev_seed(const Dev& d) {
 }
 
 // The in-place set's two layouts.  SoA: slot k of location c at k N + c.
-// AoSoA (nx a multiple of the block width B): the cells are cut into blocks
-// of B along x; a block holds its 19 slots one after the other, B elements
-// each, so slot k of location c sits at (c / B) 19 B + B k + c % B =
-// (c & ~(B-1)) 19 + B k + (c & (B-1)).  A warp's access to one slot still
-// covers 32 consecutive elements, and every slot of a location is a
-// constant offset (B k elements) from the location's slot 0.  B = 32 for
-// fp32 (a slot row is a 128-byte line), 64 for the 16-bit forms where nx
-// allows (again a 128-byte line, read by a CTA's two warps together).
+// AoSoA: each row of nx cells is padded to nxp, a multiple of the block
+// width B, and the padded cells are cut into blocks of B along x; a block
+// holds its 19 slots one after the other, B elements each, so slot k of the
+// location with padded index p = (z ny + y) nxp + x sits at
+// (p / B) 19 B + B k + p % B = (p & ~(B-1)) 19 + B k + (p & (B-1)).  A
+// warp's access to one slot still covers 32 consecutive elements, and every
+// slot of a location is a constant offset (B k elements) from the location's
+// slot 0.  B = 32 for fp32 (a slot row is a 128-byte line), 64 for the
+// 16-bit forms (again a 128-byte line, read by a CTA's two warps together).
+// The padding cells are never read or written.
 constexpr int kAosB = 32;
 __host__ __device__ __forceinline__ int64_t aos_base(int64_t c, int B = kAosB) {
   return (c & ~(int64_t)(B - 1)) * 19 + (c & (B - 1));
 }
+// The padded index of cell c (AoSoA).
+__device__ __forceinline__ int64_t padded_cell(const Dev& d, int64_t c) {
+  return d.nxp == d.nx ? c : c + (c / d.nx) * (int64_t)(d.nxp - d.nx);
+}
 // d.aos: 0 (SoA) or the AoSoA block width
 __device__ __forceinline__ int64_t elem_off(const Dev& d, int k, int64_t c) {
-  return d.aos ? aos_base(c, d.aos) + (int64_t)d.aos * k : (int64_t)k * d.N + c;
+  return d.aos ? aos_base(padded_cell(d, c), d.aos) + (int64_t)d.aos * k : (int64_t)k * d.N + c;
 }
 
 struct Wrap {
@@ -276,12 +283,14 @@ struct AddrOffs {
 template <class Off, int B = kAosB>
 struct DeltasAos {
   Off xp, yp, ym, zp, zm;
-  // bw: the block width when B = 0 (chosen at run time)
-  __device__ __forceinline__ DeltasAos(int x, int y, int z, int nx, int ny, int nz, int bw = B) {
-    const Deltas<Off> D(x, y, z, nx, ny, nz);
+  // bw: the block width when B = 0 (chosen at run time); nxp: the padded
+  // row length.  +1 in x from the row's last cell wraps to its first.
+  __device__ __forceinline__ DeltasAos(int x, int y, int z, int nx, int nxp, int ny, int nz, int bw = B) {
+    const Deltas<Off> D(x, y, z, nxp, ny, nz);   // y and z strides of the padded rows
     const int W = B ? B : bw;
     const Off next = (Off)(19 * W - (W - 1));
-    xp = (x & (W - 1)) != W - 1 ? (Off)1 : (x == nx - 1 ? next - (Off)19 * (Off)nx : next);
+    const int l = nx - 1;
+    xp = x == l ? -((Off)(l & ~(W - 1)) * 19 + (Off)(l & (W - 1))) : ((x & (W - 1)) != W - 1 ? (Off)1 : next);
     yp = (Off)19 * D.yp;
     ym = (Off)19 * D.ym;
     zp = (Off)19 * D.zp;
@@ -314,7 +323,9 @@ struct AddrAos {
   Off ob;
   DeltasAos<Off, B> D;
   __device__ __forceinline__ AddrAos(const Dev& d, Off cell, int x, int y, int z)
-      : F(static_cast<S*>(d.pop)), ob((Off)aos_base(cell, B)), D(x, y, z, d.nx, d.ny, d.nz) {}
+      : F(static_cast<S*>(d.pop)),
+        ob((Off)aos_base(cell + ((Off)z * d.ny + y) * (Off)(d.nxp - d.nx), B)),
+        D(x, y, z, d.nx, d.nxp, d.ny, d.nz) {}
   __device__ __forceinline__ void refresh() {
     if constexpr (RF) { opaque(ob); opaque(D.xp); opaque(D.yp); opaque(D.ym); opaque(D.zp); opaque(D.zm); }
   }
@@ -339,8 +350,9 @@ struct AddrRt {
   Deltas<Off> D;
   DeltasAos<Off, 0> DA;
   __device__ __forceinline__ AddrRt(const Dev& d, Off cell, int x, int y, int z)
-      : F(static_cast<S*>(d.pop)), N((Off)d.N), own(d.aos ? (Off)aos_base(cell, d.aos) : cell), bw(d.aos),
-        D(x, y, z, d.nx, d.ny, d.nz), DA(x, y, z, d.nx, d.ny, d.nz, d.aos ? d.aos : kAosB) {}
+      : F(static_cast<S*>(d.pop)), N((Off)d.N),
+        own(d.aos ? (Off)aos_base(cell + ((Off)z * d.ny + y) * (Off)(d.nxp - d.nx), d.aos) : cell), bw(d.aos),
+        D(x, y, z, d.nx, d.ny, d.nz), DA(x, y, z, d.nx, d.nxp, d.ny, d.nz, d.aos ? d.aos : kAosB) {}
   __device__ __forceinline__ Off at(int slot, int k, bool nb) const {
     if (bw) return (nb ? own + DA.odd(2 * k + 1) : own) + (Off)(bw * slot);
     return (nb ? own + D.odd(2 * k + 1) : own) + (Off)slot * N;

@@ -42,10 +42,10 @@ class SolverCUDA:
         restatement; soa: True keeps the in-place set in the SoA layout,
         False asks for the AoSoA layout where it applies, None (default)
         takes the library's choice (autotuneLayout's measurement, else AoSoA
-        for f32, the SR forms and the 16-bit forms whose nx is a multiple of
-        64 (blocks of 64 cells), SoA for the others); info()["layout"] says
-        which is in use (0 SoA, 1 ping-pong, 2 AoSoA in blocks of 32 cells,
-        3 in blocks of 64)."""
+        where it applies: blocks of 32 cells for f32, 64 for the 16-bit
+        forms, rows padded to a multiple of the block); info()["layout"]
+        says which is in use (0 SoA, 1 ping-pong, 2 AoSoA in blocks of 32
+        cells, 3 in blocks of 64)."""
         self._lib = nat.load()
         self.nx, self.ny, self.nz = int(grade["nx"]), int(grade["ny"]), int(grade["nz"])
         self.N = self.nx * self.ny * self.nz

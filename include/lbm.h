@@ -94,20 +94,18 @@ extern "C" {
                                      (slot k of cell c at k N + c) */
 #define LBM_FLAG_AOS          16  /* keep it in the AoSoA layout (blocks of
                                      cells along x, their 19 slots one after
-                                     the other: 64 cells for the 16-bit forms
-                                     where nx is a multiple of 64, else 32)
-                                     where that applies: nx a multiple of 32,
-                                     the FAST in-place step, fp32
-                                     arithmetic, 19 N < 2^31.
+                                     the other: 64 cells for the 16-bit
+                                     forms, 32 for fp32; rows padded to a
+                                     multiple of the block) where that
+                                     applies: the FAST in-place step, fp32
+                                     arithmetic, 19 x (padded cells) < 2^31.
                                      Without either flag: the layout
                                      lbm_autotune_layout measured faster for
                                      this grid, storage and flags earlier in
-                                     the process, else AoSoA for LBM_F32, the
-                                     SR forms and the 16-bit forms with nx a
-                                     multiple of 64, SoA for the others (the
-                                     faster one of each on GB300).  The
-                                     layout is internal: populations in and
-                                     out are always the natural layout. */
+                                     the process, else AoSoA where it applies
+                                     (the faster one on GB300).  The layout
+                                     is internal: populations in and out are
+                                     always the natural layout. */
 
 typedef struct lbm_ctx lbm_ctx;
 

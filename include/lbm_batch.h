@@ -12,12 +12,12 @@
  * those tunnels.  Arithmetic is identical to lbm_step (same per-cell code), so
  * each tunnel's state equals the state a separate lbm_ctx would reach.
  * Storage forms: LBM_F32 and the 16-bit forms, LBM_F16SR / LBM_BF16SR
- * included (in-place layout only; a tunnel whose nx is a multiple of 32 keeps
- * its set in the AoSoA layout of lbm.h's LBM_FLAG_AOS note, in blocks of 64
- * cells for the 16-bit forms where nx allows, unless the batch is
- * LBM_FLAG_STRICT).  The SR forms round each tunnel's stores with the same
- * seeds as a separate context: the batch keeps its step count on the device
- * as well, advanced in stream order by the captured graphs.
+ * included (in-place layout only; every tunnel keeps its set in the AoSoA
+ * layout of lbm.h's LBM_FLAG_AOS note, blocks of 64 cells for the 16-bit
+ * forms and 32 for fp32, rows padded, unless the batch is LBM_FLAG_STRICT).
+ * The SR forms round each tunnel's stores with the same seeds as a separate
+ * context: the batch keeps its step count on the device as well, advanced in
+ * stream order by the captured graphs.
  */
 #ifndef CFD_GB300_LBM_BATCH_H
 #define CFD_GB300_LBM_BATCH_H

@@ -8,7 +8,8 @@
  *
  * A checkpoint is a 48-byte lbm_state_header followed by the population set
  * exactly as it sits in device memory (in-place layout with its step parity,
- * or the current set of the ping-pong layout), so a context restored from it
+ * or the current set of the ping-pong layout; AoSoA rows with their padding
+ * cells, which stay zero), so a context restored from it
  * continues bit for bit as the saved one would have.  The learned closure's
  * held output is not part of it: after a restore the network is evaluated
  * again on the first step.
@@ -35,7 +36,7 @@ typedef struct {
   int32_t layout;         /* 0 in-place SoA, 1 ping-pong, 2 in-place AoSoA in blocks of 32 cells, 3 of 64 */
   int32_t parity;         /* in-place: step parity of the stored set */
   int64_t steps;          /* steps taken when saved */
-  uint64_t payload_bytes; /* 19 * N * bytes per stored value */
+  uint64_t payload_bytes; /* 19 * cells (AoSoA: rows padded) * bytes per stored value */
 } lbm_state_header;
 
 /* Bytes a checkpoint of ctx takes (header + payload). */

@@ -1,6 +1,7 @@
-"""The in-place set's AoSoA layout (blocks of 32 cells along x, the 19 slots
-of a block one after the other), used whenever nx is a multiple of 32 and
-the step is the FAST in-place one with fp32 arithmetic.  The layout is
+"""The in-place set's AoSoA layout (blocks of 32 cells along x for fp32, 64
+for the 16-bit forms, the 19 slots of a block one after the other, rows
+padded to a multiple of the block), used whenever the step is the FAST
+in-place one with fp32 arithmetic.  The layout is
 internal: it must give exactly the states the SoA layout and the oracle
 give, in every cell class, for the plain step, the fused force, both
 closure engines and checkpoints."""
@@ -21,8 +22,8 @@ def _pair(storage, soa_too=True, nx=64):
     out = []
     for soa in ((False, True) if soa_too else (False,)):
         s = SolverCUDA(grade, storage=storage, soa=soa)
-        # AoSoA blocks: 64 cells for the 16-bit forms where nx allows (layout 3), else 32 (2)
-        assert s.info()["layout"] == (0 if soa else (3 if storage != "f32" and nx % 64 == 0 else 2))
+        # AoSoA blocks: 64 cells for the 16-bit forms (layout 3), 32 for fp32 (2)
+        assert s.info()["layout"] == (0 if soa else (3 if storage != "f32" else 2))
         s.definirTipos(tipo)
         s.configurar(**CFG, esponja=esp)
         s.definirPopulacoes(g0)
@@ -30,12 +31,15 @@ def _pair(storage, soa_too=True, nx=64):
     return grade, tipo, esp, g0, out
 
 
-@pytest.mark.parametrize("storage,nx", [("f32", 64), ("f16s", 64), ("bf16s", 64), ("f16s", 96)])
+@pytest.mark.parametrize("storage,nx", [("f32", 64), ("f16s", 64), ("bf16s", 64), ("f16s", 96), ("f32", 40),
+                                        ("f16sr", 40)])
 def test_aos_step_bit_exact_against_oracle(native, storage, nx):
-    """nx = 64: the 16-bit forms in blocks of 64 cells; nx = 96: in blocks of 32."""
+    """nx = 64: whole blocks; nx = 96 (16-bit, blocks of 64) and 40: rows
+    padded to a multiple of the block, the last block partly empty."""
     from oracle import oracle as O
     grade, tipo, esp, g0, (s,) = _pair(storage, soa_too=False, nx=nx)
-    dt, q = {"f32": (np.float32, 0), "f16s": (np.float32, 1), "bf16s": (np.float32, 2)}[storage]
+    dt, q = {"f32": (np.float32, 0), "f16s": (np.float32, 1), "bf16s": (np.float32, 2),
+             "f16sr": (np.float32, 4)}[storage]
     o = O.Lattice((grade["nx"], grade["ny"], grade["nz"]), dtype=dt, storage=q, nthreads=8, fast=True)
     o.set_types(tipo)
     o.configure(omega_plus=CFG["omegaPlus"], les_cs=CFG["lesCs"], inlet_u=CFG["inletU"], belt_u=CFG["beltU"],
