@@ -315,8 +315,10 @@ struct DeltasAos {
 // neighbour's) plus the slot as a constant 32 k elements.  RF: make the index
 // state opaque to the compiler before the collide, so that the store
 // addresses are formed again instead of being kept in registers since the
-// loads (fewer live registers, more instructions); the tuner picks.
-template <class St, int PAR, class Off, bool RF = true, int B = kAosB>
+// loads (fewer live registers, more instructions); the tuner picks.  PAD:
+// the rows may be padded (nxp > nx); without it the padded index is the cell
+// index, one term less for the register allocation of the tightest kernels.
+template <class St, int PAR, class Off, bool RF = true, int B = kAosB, bool PAD = true>
 struct AddrAos {
   using S = typename St::store_t;
   S* F;
@@ -324,7 +326,7 @@ struct AddrAos {
   DeltasAos<Off, B> D;
   __device__ __forceinline__ AddrAos(const Dev& d, Off cell, int x, int y, int z)
       : F(static_cast<S*>(d.pop)),
-        ob((Off)aos_base(cell + ((Off)z * d.ny + y) * (Off)(d.nxp - d.nx), B)),
+        ob((Off)aos_base(PAD ? cell + ((Off)z * d.ny + y) * (Off)(d.nxp - d.nx) : cell, B)),
         D(x, y, z, d.nx, d.nxp, d.ny, d.nz) {}
   __device__ __forceinline__ void refresh() {
     if constexpr (RF) { opaque(ob); opaque(D.xp); opaque(D.yp); opaque(D.ym); opaque(D.zp); opaque(D.zm); }
@@ -509,8 +511,9 @@ __device__ __forceinline__ void step_cell(const Dev& d, const Params& P, const U
 // SOAV (SoA set): 0 slot pointers (AddrSlots), 1 one base and 32-bit slot
 // offsets (AddrOffs), 2 one base and slot x N (AddrSet); 1 and 2 need
 // 19 N < 2^31.
+// PAD (AoSoA): rows padded to the block width (false: nx is a multiple of it).
 template <class St, int PAR, bool MAC, bool FRC, bool W64, bool FAST, int MINB, bool AOS = false, bool RF = true,
-          int SOAV = 0, int AB = kAosB>
+          int SOAV = 0, int AB = kAosB, bool PAD = true>
 __global__ void __launch_bounds__(128, MINB)
 k_step_inplace(Dev d, Params P, Uni<typename St::real> U, SlotPtrs T) {
   using Off = typename OffT<W64>::type;
@@ -521,7 +524,7 @@ k_step_inplace(Dev d, Params P, Uni<typename St::real> U, SlotPtrs T) {
     const Off cell = ((Off)z * d.ny + y) * d.nx + x;
     if constexpr (AOS)
       step_cell_at<St, PAR, MAC, FRC, W64, FAST>(d, P, U, x, y, z, cell,
-                                                 AddrAos<St, PAR, Off, RF, AB>(d, cell, x, y, z));
+                                                 AddrAos<St, PAR, Off, RF, AB, PAD>(d, cell, x, y, z));
     else if constexpr (SOAV == 1 && !W64)
       step_cell_at<St, PAR, MAC, FRC, W64, FAST>(d, P, U, x, y, z, cell, AddrOffs<St, PAR>(d, T, cell, x, y, z));
     else if constexpr (SOAV == 2 && !W64)
@@ -1293,6 +1296,25 @@ struct OpsImpl {
   using R = typename St::real;
   // The fp64 reference form is always STRICT.
   static constexpr bool kFastOK = sizeof(R) == 4;
+  template <int PAR, bool MAC, bool FRC, bool FAST, bool PAD>
+  static void go_aos(const Dev& d, const Params& P, const Uni<R>& U, Launch L, cudaStream_t s, const SlotPtrs& T) {
+    constexpr int kDefault = MAC ? 6 : 8;
+    // variant 9: store addresses kept in registers from the loads
+    // blocks of 64 cells: the 16-bit forms only (lbm_create)
+    if constexpr (sizeof(typename St::store_t) == 2) {
+      if (d.aos == 64) {
+        if (!MAC && !FRC && L.occ == 9)
+          k_step_inplace<St, PAR, MAC, FRC, false, FAST, kDefault, true, false, 0, 64, PAD><<<L.grid, L.block, 0, s>>>(d, P, U, T);
+        else
+          k_step_inplace<St, PAR, MAC, FRC, false, FAST, kDefault, true, true, 0, 64, PAD><<<L.grid, L.block, 0, s>>>(d, P, U, T);
+        return;
+      }
+    }
+    if (!MAC && !FRC && L.occ == 9)
+      k_step_inplace<St, PAR, MAC, FRC, false, FAST, kDefault, true, false, 0, kAosB, PAD><<<L.grid, L.block, 0, s>>>(d, P, U, T);
+    else
+      k_step_inplace<St, PAR, MAC, FRC, false, FAST, kDefault, true, true, 0, kAosB, PAD><<<L.grid, L.block, 0, s>>>(d, P, U, T);
+  }
   template <int PAR, bool MAC, bool FRC, bool FAST>
   static void go_inplace(const Dev& d, const Params& P, const Uni<R>& U, Launch L, cudaStream_t s) {
     constexpr int kDefault = sizeof(R) == 8 ? 4 : (MAC ? 6 : 8);
@@ -1309,21 +1331,8 @@ struct OpsImpl {
     const SlotPtrs T = make_slots<St>(d, PAR);
     if (d.aos) {
       if constexpr (FAST && sizeof(R) == 4) {
-        // variant 9: store addresses kept in registers from the loads
-        // blocks of 64 cells: the 16-bit forms only (lbm_create)
-        if constexpr (sizeof(typename St::store_t) == 2) {
-          if (d.aos == 64) {
-            if (!MAC && !FRC && L.occ == 9)
-              k_step_inplace<St, PAR, MAC, FRC, false, FAST, kDefault, true, false, 0, 64><<<L.grid, L.block, 0, s>>>(d, P, U, T);
-            else
-              k_step_inplace<St, PAR, MAC, FRC, false, FAST, kDefault, true, true, 0, 64><<<L.grid, L.block, 0, s>>>(d, P, U, T);
-            return;
-          }
-        }
-        if (!MAC && !FRC && L.occ == 9)
-          k_step_inplace<St, PAR, MAC, FRC, false, FAST, kDefault, true, false><<<L.grid, L.block, 0, s>>>(d, P, U, T);
-        else
-          k_step_inplace<St, PAR, MAC, FRC, false, FAST, kDefault, true><<<L.grid, L.block, 0, s>>>(d, P, U, T);
+        if (d.nxp == d.nx) go_aos<PAR, MAC, FRC, FAST, false>(d, P, U, L, s, T);
+        else go_aos<PAR, MAC, FRC, FAST, true>(d, P, U, L, s, T);
       }
       return;
     }
