@@ -538,16 +538,13 @@ def run_ours(args):
                          "meets_1pct_cd": None if e is None else abs(e) <= 0.01}
         forms["fp16_store_vs_fp32"] = cmp16
         # the step kernel's addressing variants side by side (lbm_set_launch
-        # codes): in the AoSoA layout (the default where nx allows; blocks of
-        # 64 cells for the 16-bit forms) and, for the 16-bit forms, in SoA
+        # codes): in the AoSoA layout (the default; blocks of 64 cells for
+        # the 16-bit forms) and, for the 16-bit forms, in SoA
         variants = {}
-        aos_ok = GRIDS[args.grid]["nx"] % 32 == 0
         for st in ("f32", "f16s", "bf16s"):
             row = {}
-            codes = []
-            if aos_ok:
-                codes += [("aosoa_recompute_addresses", 8, False), ("aosoa_keep_addresses", 9, False)]
-            if st != "f32" or not aos_ok:
+            codes = [("aosoa_recompute_addresses", 8, False), ("aosoa_keep_addresses", 9, False)]
+            if st != "f32":
                 codes += [("soa_slot_pointers", 8, True), ("soa_slot_offsets_32bit", 20, True),
                           ("soa_base_plus_slot_times_n", 21, True), ("soa_80_registers", 6, True)]
             for name, code, soa in codes:
@@ -560,9 +557,9 @@ def run_ours(args):
                 s2.destruir()
             variants[st] = row
         forms["step_variants"] = variants
-        # the in-place set's two layouts side by side (AoSoA is the default
-        # where nx allows: blocks of 32 cells for fp32, 64 for the 16-bit
-        # forms; the layout code says which)
+        # the in-place set's two layouts side by side (AoSoA is the default:
+        # blocks of 32 cells for fp32, 64 for the 16-bit forms, rows padded
+        # to a multiple of the block; the layout code says which)
         lay = {}
         for st in ("f32", "f16s", "bf16s", "f16sr"):
             row = {}
