@@ -19,7 +19,8 @@ import time
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--grid", default="512x256x192")
+    ap.add_argument("--grid", default="512x256x192",
+                    help="a bench workload (512x256x192, 320x160x128) or any NXxNYxNZ: a free-stream tunnel")
     ap.add_argument("--storage", default="f32", choices=["f32", "f16s", "bf16s", "f64", "f16sr", "bf16sr"])
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
@@ -40,8 +41,18 @@ def main(argv=None):
     B.build()
     from .cargas import GRIDS, carga
     from .solver import SolverCUDA
-    tipo, cfg, desc = carga(a.grid)
-    s = SolverCUDA(GRIDS[a.grid], storage=a.storage, escrever_macros=False, soa=True if a.soa else (False if a.aos else None))
+    if a.grid in GRIDS:
+        grade = GRIDS[a.grid]
+        tipo, cfg, desc = carga(a.grid)
+    else:
+        from .tunel import montarTipos
+        nx, ny, nz = (int(v) for v in a.grid.split("x"))
+        grade = {"nx": nx, "ny": ny, "nz": nz}
+        mt = montarTipos(grade, esteira=False)
+        tipo = mt["tipo"]
+        cfg = dict(omegaPlus=1.85, lesCs=0.1, inletU=[0.05, 0.0, 0.0], beltU=[0.0, 0.0, 0.0], esponja=mt["esponja"])
+        desc = f"{a.grid} free-stream tunnel, u_in 0.05, omega+ 1.85, Cs 0.1"
+    s = SolverCUDA(grade, storage=a.storage, escrever_macros=False, soa=True if a.soa else (False if a.aos else None))
     s.definirTipos(tipo)
     s.configurar(**cfg, closure=a.closure)
     if a.closure:
