@@ -270,8 +270,8 @@ int lbm_set_launch(lbm_ctx* ctx, int block_x, int min_blocks);
  * Enqueues only; no synchronisation.  Allocates nothing: its per-row partial
  * sums live in a 1.5 MiB array built into the library, so ny*nz may be at
  * most 65536 (LBM_EINVAL beyond).  The first call on a device looks up that
- * array's device address with the device current; make it before any stream
- * capture.  The address is kept per device ordinal, so only the device's
+ * array's device address with the device current.  The address is kept per
+ * device ordinal, so only the device's
  * primary context (the CUDA runtime's default) is supported.  Every call
  * shares the one array: calls that overlap on the GPU (other streams, other
  * host threads) race, so callers must order them. */
