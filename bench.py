@@ -44,7 +44,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-# The metric string both arms print (the driver compares the two lines).
+# The metric string both arms print (so the two lines' values can be divided).
 METRIC = "MLUPS & % HBM roofline on 1 GB300, FP16-store vs FP32 plain, Cd err \u22641% vs FP64"
 from cfd__gb300.cargas import GRIDS  # noqa: E402
 
