@@ -302,7 +302,11 @@ template <class St>
 void launch_batch(lbm_batch* b, int parity, uint32_t off) {
   for (const BatchArgs& A : b->args) {
     const int per_sm = b->minb;
-    const int grid = std::min(b->sms * per_sm, std::max(1, A.ntiles));
+    // 16 times the CTAs the SMs hold at once, each walking every G-th tile:
+    // the block scheduler refills an SM as its CTAs finish, instead of one
+    // wave of CTAs that walk their shares in step (64 uneven tunnels: 0.85x
+    // of running them one after another with one wave, 0.93x with sixteen).
+    const int grid = std::min(b->sms * per_sm * 16, std::max(1, A.ntiles));
     if (b->fast) {
       if (per_sm == 6) launch_batch_m<St, true, 6>(b, A, parity, grid, off);
       else launch_batch_m<St, true, 8>(b, A, parity, grid, off);
