@@ -2,8 +2,8 @@
 //
 // Every tunnel keeps the single-tunnel data layout (its own in-place
 // population set, link words and types).  A device array of descriptors
-// (grid, pointers, parameters, tile shape, first tile) lets one persistent
-// kernel step all tunnels: CTA b walks global tiles b, b + G, b + 2G, ...;
+// (grid, pointers, parameters, tile shape, first tile) lets one kernel
+// step all tunnels: CTA b of G walks global tiles b, b + G, b + 2G, ...;
 // each tile is 128 threads covering tx cells along x and 128/tx rows along y
 // of one z-plane of one tunnel, located by a binary search over the
 // tunnels' first-tile prefix.  The per-cell work is step_cell(), the same
@@ -137,7 +137,7 @@ struct lbm_batch {
   std::vector<BatchArgs> args;       // one per launch of a step (64 tunnels each)
   long long ntiles = 0;
   int sms = 1;                       // multiprocessors of the device
-  int minb = 8;                      // resident CTAs per SM the persistent kernel is built for (8 or 6)
+  int minb = 8;                      // resident CTAs per SM the mode-1 kernel is built for (8 or 6)
   Ops ops{};
   double* partials = nullptr;
   int64_t npart = 0;
@@ -152,13 +152,13 @@ struct lbm_batch {
   bool desc_dirty = true;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};   // by start parity
   int graph_steps = 32;
-  int mode = 0;                      // 0: graph of per-tunnel chains, 1: persistent single launch
+  int mode = 0;                      // 0: graph of per-tunnel chains, 1: one launch over all tiles
   std::vector<cudaStream_t> lanes;   // capture-time streams, one per tunnel (mode 0)
   cudaEvent_t fork = nullptr;
   std::vector<cudaEvent_t> joins;
   std::vector<void*> blf;            // per tunnel: nz inlet boundary-layer factors
   uint32_t* steps_dev = nullptr;     // the step count on the device: the SR forms' rounding seeds
-  int4* tiles = nullptr;             // tile table of the persistent launches (mode 1)
+  int4* tiles = nullptr;             // tile table of the mode-1 launches
   size_t tiles_cap = 0;              // its capacity in tiles
 };
 
@@ -206,8 +206,8 @@ int sync_desc(lbm_batch* b) {
   long long total = 0;
   // One launch (or more, 64 tunnels each) per layout class, so that each
   // kernel instance carries a single addressing path.  Within a launch, tiles
-  // of the largest tunnels come first: the persistent CTAs then finish with
-  // the small ones, which evens out the tail.
+  // of the largest tunnels come first: the last CTAs then finish with the
+  // small ones, which evens out the tail.
   std::vector<size_t> order(b->host.size());
   for (size_t k = 0; k < order.size(); ++k) order[k] = k;
   std::stable_sort(order.begin(), order.end(), [&](size_t p, size_t q) {
@@ -317,7 +317,7 @@ void launch_batch(lbm_batch* b, int parity, uint32_t off) {
   }
 }
 
-// One persistent-mode step; off: its place after the device step count.
+// One mode-1 step; off: its place after the device step count.
 void launch_one(lbm_batch* b, int parity, uint32_t off) {
   switch (b->storage) {
     case LBM_F16S: launch_batch<StF16S>(b, parity, off); break;
@@ -438,7 +438,7 @@ int lbm_batch_create(const lbm_dims* dims, int ntunnels, int storage, int flags,
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  b->sms = std::max(1, sms);   // persistent: minb resident 128-thread CTAs per SM
+  b->sms = std::max(1, sms);   // mode 1: minb resident 128-thread CTAs per SM, sixteen waves
   e = cudaStreamSynchronize(b->stream);
   if (e != cudaSuccess) { lbm_batch_destroy(b); return bfail(LBM_ECUDA, "initial clear failed"); }
   *out = b;
@@ -630,7 +630,7 @@ int lbm_batch_forces(lbm_batch* b, double* f) {
 
 int lbm_batch_set_mode(lbm_batch* b, int mode) {
   if (!b) return bfail(LBM_EINVAL, "null batch");
-  if (mode != 0 && mode != 1) return bfail(LBM_EINVAL, "mode must be 0 (graph of tunnel chains) or 1 (persistent launch)");
+  if (mode != 0 && mode != 1) return bfail(LBM_EINVAL, "mode must be 0 (graph of tunnel chains) or 1 (one launch over all tiles)");
   BCK(cudaStreamSynchronize(b->stream), "stream sync");
   if (mode != b->mode) drop_graphs(b);
   b->desc_dirty = true;

@@ -2,7 +2,7 @@
 
 Each tunnel is configured like a SolverCUDA (configurar / definirTipos with
 the reference's arguments, src/backend/webgpu/solver.js:277-301); passo(n)
-advances all of them with one persistent launch per step, replayed from a
+advances all of them with one launch per step (mode 1), replayed from a
 CUDA graph.  Per-tunnel results equal what separate SolverCUDA objects give.
 """
 from __future__ import annotations
@@ -69,11 +69,11 @@ class LoteCUDA:
         nat.check(self._lib.lbm_batch_set_tile(self._h, int(k), int(tile_x)))
 
     def definirModo(self, modo):
-        """0: graph of per-tunnel chains (default); 1: one persistent launch per step."""
+        """0: graph of per-tunnel chains (default); 1: one launch per step whose CTAs walk all tunnels' tiles."""
         nat.check(self._lib.lbm_batch_set_mode(self._h, int(modo)))
 
     def ladrilho(self, k):
-        """Tile width along x of tunnel k in the persistent launch."""
+        """Tile width along x of tunnel k in the mode-1 launch."""
         t = C.c_int()
         nat.check(self._lib.lbm_batch_get_tile(self._h, int(k), C.byref(t)))
         return t.value

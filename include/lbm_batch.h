@@ -8,9 +8,10 @@
  * lbm_batch_step captures 32 steps of every tunnel into a CUDA graph and
  * replays it: by default one independent chain of single-tunnel launches per
  * tunnel (the GPU overlaps the chains), or (lbm_batch_set_mode 1) one
- * persistent launch per step and layout class whose CTAs walk the tiles of
- * those tunnels.  Arithmetic is identical to lbm_step (same per-cell code), so
- * each tunnel's state equals the state a separate lbm_ctx would reach.
+ * launch per step and layout class whose CTAs (sixteen times as many as the
+ * GPU holds at once) each walk every G-th tile of those tunnels.  Arithmetic
+ * is identical to lbm_step (same per-cell code), so each tunnel's state
+ * equals the state a separate lbm_ctx would reach.
  * Storage forms: LBM_F32 and the 16-bit forms, LBM_F16SR / LBM_BF16SR
  * included (in-place layout only; every tunnel keeps its set in the AoSoA
  * layout of lbm.h's LBM_FLAG_AOS note, blocks of 64 cells for the 16-bit
@@ -39,7 +40,7 @@ int lbm_batch_configure(lbm_batch* b, int k, const lbm_params* p);
 int lbm_batch_set_types(lbm_batch* b, int k, const uint32_t* tipo, size_t n);
 /* shaderInit in every tunnel; step counter to 0 */
 int lbm_batch_init_equilibrium(lbm_batch* b);
-/* n steps of every tunnel (CUDA-graph replay of one persistent launch per step) */
+/* n steps of every tunnel (CUDA-graph replay of the mode's launches) */
 int lbm_batch_step(lbm_batch* b, int n);
 /* tunnel k's state, 19*N_k doubles, natural layout (as lbm_get_populations) */
 int lbm_batch_get_populations(lbm_batch* b, int k, double* g, size_t n);
@@ -50,13 +51,13 @@ int lbm_batch_forces(lbm_batch* b, double* f);
 int lbm_batch_set_tile(lbm_batch* b, int k, int tile_x);
 /* 0 (default): each step of each tunnel is its own launch of the
  * single-tunnel kernel; the captured graph holds one chain per tunnel and
- * the GPU runs the chains concurrently.  1: one persistent launch per step
- * and layout class walks the tiles of those tunnels (descriptors in the
+ * the GPU runs the chains concurrently.  1: one launch per step and layout
+ * class whose CTAs walk the tiles of those tunnels (descriptors in the
  * launch parameters, tile origins in a device table of 16 bytes per tile
  * that the batch allocates when it first needs it). */
 int lbm_batch_set_mode(lbm_batch* b, int mode);
 int lbm_batch_info(lbm_batch* b, int64_t* total_cells, int64_t* device_bytes);
-/* The tile width along x tunnel k's tiles use in the persistent launch. */
+/* The tile width along x tunnel k's tiles use in the mode-1 launch. */
 int lbm_batch_get_tile(lbm_batch* b, int k, int* tile_x);
 /* Measured choice of how the batch steps: mode 0; mode 1 with the kernel
  * built for 8 or 6 resident 128-thread CTAs per SM; then, for mode 1, the
