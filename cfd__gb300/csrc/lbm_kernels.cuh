@@ -1298,6 +1298,7 @@ struct OpsImpl {
   static constexpr bool kFastOK = sizeof(R) == 4;
   template <int PAR, bool MAC, bool FRC, bool FAST, bool PAD>
   static void go_aos(const Dev& d, const Params& P, const Uni<R>& U, Launch L, cudaStream_t s, const SlotPtrs& T) {
+    static_assert(sizeof(R) == 4, "the AoSoA step runs fp32 arithmetic");
     constexpr int kDefault = MAC ? 6 : 8;
     // variant 9: store addresses kept in registers from the loads
     // blocks of 64 cells: the 16-bit forms only (lbm_create)
